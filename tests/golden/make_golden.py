@@ -1,0 +1,351 @@
+"""Generate the golden fixtures by running the unmodified reference implementation.
+
+Run in the build container (where the reference source is mounted):
+
+    python tests/golden/make_golden.py
+
+It imports the reference package through ``oracle/build_ref.py`` (which compiles
+the reference's Cython ``Domain`` extension into ``oracle/_ref/``) together with
+the molmod/h5py stand-ins under ``tests/golden/standin/``, runs the reference's
+own ``System``, ``ForcePartMechanical``, ``VerletIntegrator``, thermostats,
+barostat, builder and ``QNOptimizer`` on small seeded inputs, and writes the
+inputs and outputs as compressed ``.npz`` files next to this script. The tests
+read only those files; they never touch the reference at run time.
+
+Random draws the reference makes with ``np.random.normal`` (Langevin noise) are
+recorded into the fixtures so the GPU path can replay them.
+"""
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle.build_ref import import_reference  # noqa: E402
+
+import_reference()
+
+import micmec.pes.mmff as rmmff  # noqa: E402
+import micmec.pes.nanocell as r_nc  # noqa: E402
+import micmec.pes.nanocell_original as r_no  # noqa: E402
+from micmec.system import System  # noqa: E402
+from micmec.pes.mmff import MicMecForceField, ForcePartMechanical  # noqa: E402
+from micmec.sampling.verlet import VerletIntegrator  # noqa: E402
+from micmec.sampling.iterative import Hook  # noqa: E402
+from micmec.sampling.nvt import LangevinThermostat, NHCThermostat  # noqa: E402
+from micmec.sampling.npt import MTKBarostat  # noqa: E402
+from micmec.sampling.dof import CartesianDOF  # noqa: E402
+from micmec.sampling.opt import QNOptimizer  # noqa: E402
+from micmec import utils as rutils  # noqa: E402
+
+from micmec_gb300 import units  # noqa: E402
+from micmec_gb300 import lattices  # noqa: E402
+
+DATA = os.path.join(os.environ.get("MICMEC_REFERENCE", "/root/reference"), "data")
+NUMERIC_PARAM_FIELDS = ("cell", "elasticity", "free_energy", "effective_temp", "mass")
+
+
+def set_model(model):
+    src = r_nc if model == "nanocell" else r_no
+    rmmff.elastic_energy_nanocell = src.elastic_energy_nanocell
+    rmmff.grad_elastic_energy_nanocell = src.grad_elastic_energy_nanocell
+
+
+def system_arrays(s, prefix=""):
+    out = {
+        prefix + "pos": np.array(s.pos, dtype=np.float64),
+        prefix + "masses": np.array(s.masses, dtype=np.float64),
+        prefix + "rvecs": np.array(s.domain.rvecs, dtype=np.float64).reshape(-1, 3),
+        prefix + "surrounding_cells": np.array(s.surrounding_cells, dtype=np.int64),
+        prefix + "surrounding_nodes": np.array(s.surrounding_nodes, dtype=np.int64),
+        prefix + "grid": np.array(s.grid, dtype=np.int64),
+        prefix + "types": np.array(s.types, dtype=np.int64),
+    }
+    for key, value in s.params.items():
+        if key.split("/")[-1] in NUMERIC_PARAM_FIELDS:
+            out[prefix + "param:" + key] = np.array(value, dtype=np.float64)
+    return out
+
+
+def save(name, **arrays):
+    fn = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(fn, **arrays)
+    print("wrote", fn, os.path.getsize(fn), "bytes")
+
+
+def system_from_dict(d):
+    kw = dict(d)
+    params = {k: v for k, v in kw.items() if "/" in k}
+    for k in params:
+        kw.pop(k)
+    for k in ("pbc",):
+        kw.pop(k, None)
+    kw["params"] = params
+    kw["surrounding_cells"] = np.asarray(kw["surrounding_cells"])
+    kw["surrounding_nodes"] = np.asarray(kw["surrounding_nodes"])
+    kw["types"] = np.asarray(kw["types"])
+    kw["boundary_nodes"] = np.asarray(kw["boundary_nodes"])
+    return System(**kw)
+
+
+def synthetic_system(n, nstates, seed, sigma_angstrom, defect_fraction=0.0, pbc=True, vacancies=0):
+    """Reference ``build_system`` on the standard fcu/reo types."""
+    rng = np.random.default_rng(seed)
+    grid = lattices.defect_grid(n, defect_fraction, rng)
+    if vacancies:
+        flat = grid.reshape(-1)
+        flat[rng.permutation(flat.size)[:vacancies]] = 0
+    data = lattices.standard_types(nstates=nstates, with_reo=bool((grid == 2).any()))
+    if not (grid == 2).any():
+        data = {1: data[1]}
+    d = rutils.build_system(data, grid, pbc=pbc)
+    s = system_from_dict(d)
+    s.pos[:] = lattices.displace(s.pos, sigma_angstrom * units.angstrom, rng)
+    return s
+
+
+def compute_all(s, model):
+    set_model(model)
+    fp = ForcePartMechanical(s)
+    ff = MicMecForceField(s, [fp])
+    gpos = np.zeros((s.nnodes, 3))
+    vtens = np.zeros((3, 3))
+    e = ff.compute(gpos, vtens)
+    return e, gpos, vtens, fp.epot_cells, fp.gpos_cells
+
+
+# ------------------------------------------------------------------ forces
+
+
+def make_force_fixtures():
+    arrays = {}
+    cases = []
+    chk_names = [
+        "2x2x2_fcu_micmec", "2x2x2_fcu_hollow_micmec", "3x3x3_test_micmec",
+        "3x3x3_conf0_micmec", "3x3x3_fcu_hollow_micmec", "4x4x4_fcu_hollow_micmec",
+        "5x5x5_fcu_hollow_micmec",
+    ]
+    for i, name in enumerate(chk_names):
+        s = System.from_file(os.path.join(DATA, name + ".chk"))
+        rng = np.random.default_rng(100 + i)
+        s.pos[:] += rng.normal(0.0, 0.2 * units.angstrom, s.pos.shape)
+        cases.append((name, s))
+    cases.append(("synth_4x4x4_2types_2states", synthetic_system(4, 2, 7, 0.1, 0.25)))
+    # Non-periodic systems are not included: the reference's deformation() reads
+    # rvecs[0] unconditionally (micmec/pes/mmff.py:349) and raises IndexError
+    # when the domain has no vectors.
+    cases.append(("synth_5x4x3_vacancies_periodic", synthetic_system((5, 4, 3), 2, 9, 0.1, 0.2, pbc=True, vacancies=7)))
+    names = []
+    for name, s in cases:
+        for model in ("original", "nanocell"):
+            key = f"{name}/{model}/"
+            e, gpos, vtens, ecells, gcells = compute_all(s, model)
+            arrays[key + "energy"] = np.array(e)
+            arrays[key + "gpos"] = gpos
+            arrays[key + "vtens"] = vtens
+            arrays[key + "epot_cells"] = np.asarray(ecells)
+            arrays[key + "gpos_cells"] = np.asarray(gcells)
+        arrays.update(system_arrays(s, prefix=name + "/sys/"))
+        names.append(name)
+    arrays["cases"] = np.array(names)
+    save("forces", **arrays)
+
+
+# ------------------------------------------------------------------ builder
+
+
+def make_builder_fixture():
+    arrays = {}
+    rng = np.random.default_rng(11)
+    for pbc in (True, False):
+        grid = rng.integers(0, 3, size=(4, 3, 5))
+        grid[0, 0, 0] = 1
+        data = lattices.standard_types(nstates=2)
+        d = rutils.build_system(data, grid, pbc=pbc)
+        tag = "pbc" if pbc else "nopbc"
+        for k in ("pos", "rvecs", "surrounding_cells", "surrounding_nodes", "boundary_nodes", "masses", "types"):
+            arrays[f"{tag}/{k}"] = np.asarray(d[k])
+        arrays[f"{tag}/grid"] = grid
+    save("builder", **arrays)
+
+
+# ------------------------------------------------------------------ MD
+
+
+class Recorder(Hook):
+    def __init__(self, every_pos=1):
+        Hook.__init__(self, 0, 1)
+        self.rows = []
+        self.snap = {}
+        self.every_pos = every_pos
+
+    def __call__(self, it):
+        self.rows.append(
+            [it.counter, it.epot, it.ekin, it.econs, it.temp, getattr(it, "press", 0.0)]
+            + list(np.asarray(it.vtens).ravel())
+            + list(np.asarray(getattr(it, "ptens", np.zeros((3, 3)))).ravel())
+            + list(np.asarray(it.mmf.system.domain.rvecs).ravel())
+            + [it.mmf.system.domain.volume]
+        )
+        if it.counter % self.every_pos == 0:
+            self.snap[f"pos_{it.counter}"] = it.pos.copy()
+            self.snap[f"vel_{it.counter}"] = it.vel.copy()
+
+
+class NoiseLog(object):
+    """Wraps ``numpy.random.normal`` to record every draw the reference makes."""
+
+    def __enter__(self):
+        self.orig = np.random.normal
+        self.draws = []
+
+        def normal(*args, **kwargs):
+            out = self.orig(*args, **kwargs)
+            self.draws.append(np.array(out, dtype=np.float64))
+            return out
+
+        np.random.normal = normal
+        return self
+
+    def __exit__(self, *exc):
+        np.random.normal = self.orig
+
+
+def md_system(seed=1):
+    """Config-1 lattice: 3x3x3 fcu, one state, sigma = 0.05 A, MB velocities at 300 K."""
+    s = synthetic_system(3, 1, seed, 0.05)
+    rng = np.random.default_rng(seed + 1000)
+    kT = units.boltzmann * 300.0
+    vel = rng.normal(0.0, 1.0, s.pos.shape) * np.sqrt(kT / s.masses)[:, None]
+    vel -= (s.masses @ vel) / s.masses.sum()
+    return s, vel
+
+
+def run_md(tag, model, nsteps, hooks_fn, every_pos, seed=1, dt_fs=1.0, record_noise=False, extra=None):
+    set_model(model)
+    s, vel0 = md_system(seed)
+    arrays = system_arrays(s, prefix="sys/")
+    ff = MicMecForceField(s, [ForcePartMechanical(s)])
+    rec = Recorder(every_pos)
+    hooks, meta = hooks_fn(ff)
+    np.random.seed(seed + 2000)
+    with NoiseLog() as nl:
+        vi = VerletIntegrator(ff, dt_fs * units.femtosecond, hooks=hooks + [rec], vel0=vel0.copy())
+        vi.run(nsteps)
+    arrays["vel0"] = vel0
+    arrays["timestep"] = np.array(dt_fs * units.femtosecond)
+    arrays["records"] = np.array(rec.rows)
+    arrays["model"] = np.array(model)
+    arrays["ndof"] = np.array(vi.ndof)
+    for k, v in rec.snap.items():
+        arrays[k] = v
+    for k, v in meta.items():
+        arrays["meta/" + k] = np.asarray(v)
+    if record_noise:
+        arrays["noise"] = np.array([d for d in nl.draws if d.shape == s.pos.shape])
+    if extra:
+        extra(arrays, vi)
+    save("md_" + tag, **arrays)
+
+
+def make_md_fixtures():
+    T = 300.0 * units.kelvin
+    fs = units.femtosecond
+
+    if "md-fast" not in sys.argv:
+        run_md("nve_original", "original", 1000, lambda ff: ([], {}), 100)
+        run_md("nve_nanocell", "nanocell", 1000, lambda ff: ([], {}), 100)
+
+    def langevin(ff):
+        return [LangevinThermostat(T, timecon=100 * fs)], {"temp": T, "timecon": 100 * fs}
+
+    run_md("langevin_nanocell", "nanocell", 200, langevin, 50, record_noise=True)
+
+    rng = np.random.default_rng(5)
+    chain_vel0 = rng.normal(0, 1e-5, 3)
+
+    def nhc(ff):
+        return (
+            [NHCThermostat(T, timecon=100 * fs, chainlength=3, chain_vel0=chain_vel0.copy())],
+            {"temp": T, "timecon": 100 * fs, "chain_vel0": chain_vel0},
+        )
+
+    def nhc_extra(arrays, vi):
+        hook = [h for h in vi.hooks if isinstance(h, NHCThermostat)][0]
+        arrays["chain_pos_end"] = hook.chain.pos
+        arrays["chain_vel_end"] = hook.chain.vel
+
+    run_md("nhc_nanocell", "nanocell", 200, nhc, 50, extra=nhc_extra)
+
+    vp = rng.normal(0, 1e-6, (3, 3))
+    vp = 0.5 * (vp + vp.T)
+    press = 100e6 * units.pascal
+
+    def mtk(ff):
+        b = MTKBarostat(ff, T, press, timecon=1000 * fs, vel_press0=vp.copy())
+        return [b], {"temp": T, "press": press, "timecon": 1000 * fs, "vel_press0": vp}
+
+    def mtk_extra(arrays, vi):
+        hook = [h for h in vi.hooks if isinstance(h, MTKBarostat) or h.name == "TBCombination"][0]
+        baro = hook if isinstance(hook, MTKBarostat) else hook.barostat
+        arrays["vel_press_end"] = baro.vel_press
+        arrays["rvecs_end"] = vi.mmf.system.domain.rvecs
+        if hook.name == "TBCombination" and hasattr(hook.thermostat, "chain"):
+            arrays["chain_pos_end"] = hook.thermostat.chain.pos
+            arrays["chain_vel_end"] = hook.thermostat.chain.vel
+
+    run_md("mtk_nanocell", "nanocell", 100, mtk, 25, extra=mtk_extra)
+
+    def nhc_mtk(ff):
+        b = MTKBarostat(ff, T, press, timecon=1000 * fs, vel_press0=vp.copy())
+        t = NHCThermostat(T, timecon=100 * fs, chainlength=3, chain_vel0=chain_vel0.copy())
+        return [t, b], {"temp": T, "press": press, "timecon_baro": 1000 * fs,
+                        "timecon_thermo": 100 * fs, "vel_press0": vp, "chain_vel0": chain_vel0}
+
+    run_md("nhc_mtk_nanocell", "nanocell", 100, nhc_mtk, 25, extra=mtk_extra)
+
+    def lang_mtk(ff):
+        b = MTKBarostat(ff, T, press, timecon=1000 * fs, vel_press0=vp.copy())
+        t = LangevinThermostat(T, timecon=100 * fs)
+        return [t, b], {"temp": T, "press": press, "timecon_baro": 1000 * fs,
+                        "timecon_thermo": 100 * fs, "vel_press0": vp}
+
+    run_md("langevin_mtk_nanocell", "nanocell", 50, lang_mtk, 25, record_noise=True, extra=mtk_extra)
+
+
+# ------------------------------------------------------------------ optimiser
+
+
+def make_opt_fixture():
+    set_model("nanocell")
+    s = synthetic_system(3, 2, 21, 0.1, 0.3)
+    arrays = system_arrays(s, prefix="sys/")
+    ff = MicMecForceField(s, [ForcePartMechanical(s)])
+    energies = []
+
+    class E(Hook):
+        def __call__(self, it):
+            energies.append(it.epot)
+
+    dof = CartesianDOF(ff, gpos_rms=1e-6, dpos_rms=1e-4)
+    opt = QNOptimizer(dof, hooks=[E()])
+    opt.run(60)
+    arrays["energies"] = np.array(energies)
+    arrays["pos_end"] = s.pos.copy()
+    save("opt_qn_nanocell", **arrays)
+
+
+if __name__ == "__main__":
+    which = sys.argv[1:] or ["forces", "builder", "md", "opt"]
+    if "forces" in which:
+        make_force_fixtures()
+    if "builder" in which:
+        make_builder_fixture()
+    if "md" in which:
+        make_md_fixtures()
+    if "opt" in which:
+        make_opt_fixture()
