@@ -1,0 +1,142 @@
+/*
+ * micmec_gb300 — C ABI of the GB300-native MicMec force-evaluation and
+ * integration path (one GPU, sm_103a).
+ *
+ * The reference (molmod/micmec) is a Python package; its force path is the
+ * `ForcePart.compute(gpos, vtens)` call of micmec/pes/mmff.py:87-149 and the
+ * Verlet loop of micmec/sampling/verlet.py:140-166. This library is what a
+ * binding of that path calls (see INTEGRATION.md for the ctypes binding).
+ *
+ * Conventions
+ *  - All quantities are in atomic units and FP64 at the boundary.
+ *  - Arrays are C-contiguous; (N,3) means node-major xyz triples.
+ *  - Pointers marked "device" are CUDA device pointers (e.g. torch tensors);
+ *    "host" pointers are ordinary CPU memory.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *  - Every call returns an mm_status. Calls that take a stream only enqueue
+ *    work; results are valid after the stream is synchronised.
+ *  - A handle is used from one host thread at a time.
+ */
+#ifndef MICMEC_GB300_H
+#define MICMEC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  MM_OK = 0,
+  MM_ERR_NAN = 1,     /* NaN in energy, gradient or virial (reference: ValueError, mmff.py:135-148) */
+  MM_ERR_ARG = 2,     /* invalid argument */
+  MM_ERR_CUDA = 3,    /* CUDA runtime error */
+  MM_ERR_TIMEOUT = 4, /* a bounded device-side wait ran out */
+} mm_status;
+
+enum { MM_MODEL_ORIGINAL = 0, MM_MODEL_NANOCELL = 1 };
+enum { MM_PREC_FP64 = 0, MM_PREC_FP32 = 1 };
+enum { MM_THERMO_NONE = 0, MM_THERMO_LANGEVIN = 1 };
+
+/* Per-step MD record, MM_REC_LEN doubles per step (see mm_md_run). */
+enum {
+  MM_REC_EPOT = 0,      /* potential energy after the step */
+  MM_REC_EKIN = 1,      /* kinetic energy after the step (after the "post" thermostat) */
+  MM_REC_DECONS = 2,    /* change of the thermostat's conserved-energy correction during the step */
+  MM_REC_VTENS = 3,     /* 9: virial tensor, row-major */
+  MM_REC_KTENS = 12,    /* 9: kinetic tensor sum_i m_i v_i (x) v_i */
+  MM_REC_LEN = 21
+};
+
+typedef struct mm_handle mm_handle;
+
+/*
+ * Create a system.
+ *  nnodes, ncells      : N and M.
+ *  node_coords (N,3)   : host, integer lattice coordinates (kk,ll,mm) of every node,
+ *                        the reference's Grid.nodes (micmec/utils.py:113-136).
+ *  cell_nodes  (M,8)   : host, reference `surrounding_nodes` (corner order of utils.py:43-52).
+ *  node_cells  (N,8)   : host, reference `surrounding_cells` (-1 = no cell).
+ *  cell_type   (M)     : host, 0-based index into the type table.
+ *  lattice_shape[3]    : nodes per lattice direction (Grid.n?_nodes).
+ *  pbc                 : 1 = 3-D periodic, 0 = isolated.
+ *  ntypes, nstates[ntypes]
+ *  h0 [ntypes*4][9], C [ntypes*4][81], free_energy [ntypes*4], temp_eff [ntypes]:
+ *                        host, per (type, state) rest cell matrix (rows = cell vectors),
+ *                        3x3x3x3 elasticity tensor, state free energy; per type the
+ *                        effective temperature (kelvin). Slot (t, s) is t*4+s.
+ *  masses (N)          : host, node masses.
+ *  model               : MM_MODEL_*.  precision : MM_PREC_*.
+ * Replaces: ForcePartMechanical.__init__ (micmec/pes/mmff.py:207-245), which reads
+ * the same system arrays and type{k}/... parameters and builds a dense
+ * minimum-image table (mmff.py:258-286); here the image shift is implicit in the
+ * lattice coordinates.
+ */
+mm_status mm_create(int nnodes, int ncells, const int32_t* node_coords, const int32_t* cell_nodes,
+                    const int32_t* node_cells, const int32_t* cell_type, const int32_t* lattice_shape,
+                    int pbc, int ntypes, const int32_t* nstates, const double* h0, const double* C,
+                    const double* free_energy, const double* temp_eff, const double* masses, int model,
+                    int precision, mm_handle** out);
+
+/* Release all device memory of a handle. */
+mm_status mm_destroy(mm_handle* h);
+
+/*
+ * Set the domain. rvecs (3,3) host, rows = domain vectors (periodic systems), or
+ * NULL for an isolated system. `lattice` (3,3) host: the lattice matrix whose rows
+ * are the node spacings along the three lattice directions; NULL = rvecs[d]/n_d.
+ * Replaces: MicMecForceField.update_rvecs -> Domain.update_rvecs
+ * (micmec/pes/mmff.py:191-193, micmec/pes/ext.pyx:52-72).
+ */
+mm_status mm_set_domain(mm_handle* h, const double* rvecs, const double* lattice);
+
+/*
+ * Energy, gradient and virial at positions pos (N,3).
+ *  pos         : device (N,3).
+ *  gpos        : device (N,3) or NULL; the gradient is ADDED to its contents.
+ *  vtens       : device (3,3) or NULL; the virial is ADDED to its contents.
+ *  energy      : device double[1]; the energy is WRITTEN.
+ *  status_dev  : device int[1] or NULL; set to 1 if a NaN was produced.
+ * Replaces: ForcePart.compute(gpos, vtens) for the "micmec" part
+ * (micmec/pes/mmff.py:87-149, 288-323; the add-into semantics of mmff.py:143-148).
+ */
+mm_status mm_compute(mm_handle* h, const double* pos, double* gpos, double* vtens, double* energy,
+                     int* status_dev, void* stream);
+
+/*
+ * Same as mm_compute with host buffers: copies pos in, runs, copies results back and
+ * synchronises. gpos/vtens may be NULL. Returns MM_ERR_NAN if energy, gradient or
+ * virial contain a NaN (the reference raises ValueError, mmff.py:135-148).
+ */
+mm_status mm_compute_host(mm_handle* h, const double* pos, double* gpos, double* vtens, double* energy);
+
+/* Per-cell energies (M) and corner gradients (M,8,3) of the last compute: device outputs. */
+mm_status mm_cell_results(mm_handle* h, double* epot_cells, double* gpos_cells, void* stream);
+
+/*
+ * Velocity-Verlet MD on the device (micmec/sampling/verlet.py:119-166), optionally with
+ * the Langevin thermostat applied before and after every step (nvt.py:196-218).
+ *  pos, vel  : device (N,3); read at the start, overwritten with the final state.
+ *  nsteps    : number of steps.
+ *  timestep  : dt.   thermo : MM_THERMO_*.   temp, timecon : Langevin parameters.
+ *  seed      : Philox seed for the Langevin noise.
+ *  noise     : device (nsteps, 2, N, 3) standard normals to use instead of the
+ *              generator (index 0 = "pre", 1 = "post"), or NULL.
+ *  records   : device (nsteps, MM_REC_LEN) per-step observables, or NULL.
+ *  step0     : index of the first step (counter0), used as the noise counter.
+ */
+mm_status mm_md_run(mm_handle* h, double* pos, double* vel, int nsteps, double timestep, int thermo,
+                    double temp, double timecon, uint64_t seed, const double* noise, double* records,
+                    int64_t step0, void* stream);
+
+/* Last CUDA error string of the calling thread's last failing call. */
+const char* mm_last_error(void);
+
+/* Library version string. */
+const char* mm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MICMEC_GB300_H */

@@ -1,0 +1,351 @@
+// extern "C" entry points of libmicmec_gb300 (declared in include/micmec_gb300.h).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/micmec_gb300.h"
+#include "mm_handle.h"
+
+#define MM_VERSION "micmec_gb300 0.1 (sm_103a)"
+
+namespace {
+
+const double kBoltzmann = 1.3806505e-23 / 4.35974381e-18;  // Hartree / K (molmod value)
+
+bool cuda_ok(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return true;
+  mm::set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return false;
+}
+
+#define MM_CUDA(call)                                   \
+  do {                                                  \
+    if (!cuda_ok((call), #call)) return MM_ERR_CUDA;    \
+  } while (0)
+
+void inv3(const double* a, double* out, double* det) {
+  const double c00 = a[4] * a[8] - a[5] * a[7];
+  const double c01 = a[5] * a[6] - a[3] * a[8];
+  const double c02 = a[3] * a[7] - a[4] * a[6];
+  const double d = a[0] * c00 + a[1] * c01 + a[2] * c02;
+  out[0] = c00 / d;
+  out[1] = (a[2] * a[7] - a[1] * a[8]) / d;
+  out[2] = (a[1] * a[5] - a[2] * a[4]) / d;
+  out[3] = c01 / d;
+  out[4] = (a[0] * a[8] - a[2] * a[6]) / d;
+  out[5] = (a[2] * a[3] - a[0] * a[5]) / d;
+  out[6] = c02 / d;
+  out[7] = (a[1] * a[6] - a[0] * a[7]) / d;
+  out[8] = (a[0] * a[4] - a[1] * a[3]) / d;
+  *det = d;
+}
+
+// 6x6 map from the Voigt strain (00,11,22,12,02,01) to the symmetric part of
+// sigma_ij = C_ijkl eps_kl; off-diagonal strain columns collect the kl and lk terms.
+void voigt_stress_map(const double* C, double* A) {
+  const int P[6][2] = {{0, 0}, {1, 1}, {2, 2}, {1, 2}, {0, 2}, {0, 1}};
+  auto c = [&](int i, int j, int k, int l) { return C[((i * 3 + j) * 3 + k) * 3 + l]; };
+  for (int p = 0; p < 6; ++p) {
+    const int i = P[p][0], j = P[p][1];
+    for (int q = 0; q < 6; ++q) {
+      const int k = P[q][0], l = P[q][1];
+      double v = 0.5 * (c(i, j, k, l) + c(j, i, k, l));
+      if (k != l) v += 0.5 * (c(i, j, l, k) + c(j, i, l, k));
+      A[p * 6 + q] = v;
+    }
+  }
+}
+
+template <typename X>
+bool dev_alloc(X** p, size_t count) {
+  if (count == 0) count = 1;
+  return cuda_ok(cudaMalloc((void**)p, count * sizeof(X)), "cudaMalloc");
+}
+
+void free_handle(mm_handle* h) {
+  if (!h) return;
+  void* bufs[] = {h->d_tt, h->d_box, h->d_cell_nodes, h->d_node_cells, h->d_node_lat, h->d_cell_type,
+                  h->d_mass, h->d_invm, h->d_c2, h->d_u, h->d_v, h->d_disp, h->d_G, h->d_ecell,
+                  h->d_cpart, h->d_npart, h->d_ticket, h->d_carry, h->d_io, h->d_flag};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  delete h;
+}
+
+mm_status upload_box(mm_handle* h) {
+  MM_CUDA(cudaMemcpy(h->d_box, h->L, 9 * sizeof(double), cudaMemcpyHostToDevice));
+  return MM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* mm_last_error(void) { return mm::last_error(); }
+const char* mm_version(void) { return MM_VERSION; }
+
+mm_status mm_create(int nnodes, int ncells, const int32_t* node_coords, const int32_t* cell_nodes,
+                    const int32_t* node_cells, const int32_t* cell_type, const int32_t* lattice_shape, int pbc,
+                    int ntypes, const int32_t* nstates, const double* h0, const double* C,
+                    const double* free_energy, const double* temp_eff, const double* masses, int model,
+                    int precision, mm_handle** out) {
+  if (!out || nnodes <= 0 || ncells <= 0 || !node_coords || !cell_nodes || !node_cells || !cell_type ||
+      !lattice_shape || !nstates || !h0 || !C || !free_energy || !temp_eff || !masses) {
+    mm::set_error("mm_create: missing argument");
+    return MM_ERR_ARG;
+  }
+  if (ntypes < 1 || ntypes > MM_MAX_TYPES || (model != MM_MODEL_ORIGINAL && model != MM_MODEL_NANOCELL) ||
+      (precision != MM_PREC_FP64 && precision != MM_PREC_FP32)) {
+    mm::set_error("mm_create: bad ntypes/model/precision");
+    return MM_ERR_ARG;
+  }
+  const int N = nnodes, M = ncells;
+  for (int i = 0; i < M; ++i)
+    if (cell_type[i] < 0 || cell_type[i] >= ntypes) {
+      mm::set_error("mm_create: cell type out of range");
+      return MM_ERR_ARG;
+    }
+  for (int i = 0; i < 8 * M; ++i)
+    if (cell_nodes[i] < 0 || cell_nodes[i] >= N) {
+      mm::set_error("mm_create: cell_nodes out of range");
+      return MM_ERR_ARG;
+    }
+  for (int i = 0; i < 8 * N; ++i)
+    if (node_cells[i] < -1 || node_cells[i] >= M) {
+      mm::set_error("mm_create: node_cells out of range");
+      return MM_ERR_ARG;
+    }
+  mm_handle* h = new mm_handle();
+  h->N = N;
+  h->M = M;
+  h->pbc = pbc ? 1 : 0;
+  h->model = model;
+  h->prec = precision;
+  h->ntypes = ntypes;
+  for (int d = 0; d < 3; ++d) h->nn[d] = lattice_shape[d];
+
+  // parameter table
+  for (int t = 0; t < ntypes; ++t) {
+    if (nstates[t] < 1 || nstates[t] > MM_MAX_STATES) {
+      free_handle(h);
+      mm::set_error("mm_create: nstates out of range");
+      return MM_ERR_ARG;
+    }
+    mm::TypeTable& tt = h->tt[t];
+    std::memset(&tt, 0, sizeof(tt));
+    tt.nstates = nstates[t];
+    tt.kT = kBoltzmann * temp_eff[t];
+    for (int s = 0; s < MM_MAX_STATES; ++s) {
+      const int slot = t * MM_MAX_STATES + (s < nstates[t] ? s : 0);
+      mm::StateTable& st = tt.s[s];
+      std::memcpy(st.h0, h0 + 9 * slot, 9 * sizeof(double));
+      inv3(st.h0, st.hinv, &st.v0);
+      voigt_stress_map(C + 81 * slot, st.A);
+      st.df = free_energy[slot];
+    }
+  }
+
+  // structured lattice detection: periodic, every lattice site a node and a cell,
+  // tables identical to the implicit ones
+  bool structured = pbc && (N == M) && (N == lattice_shape[0] * lattice_shape[1] * lattice_shape[2]);
+  if (structured) {
+    const int nx = lattice_shape[0], ny = lattice_shape[1], nz = lattice_shape[2];
+    const int corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 1, 0}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
+    for (int c = 0; c < M && structured; ++c) {
+      const int i = c / (ny * nz), j = (c / nz) % ny, k = c % nz;
+      if (node_coords[3 * c] != i || node_coords[3 * c + 1] != j || node_coords[3 * c + 2] != k) structured = false;
+      for (int q = 0; q < 8 && structured; ++q) {
+        const int a = (i + corner[q][0]) % nx, b = (j + corner[q][1]) % ny, cc = (k + corner[q][2]) % nz;
+        if (cell_nodes[8 * c + q] != (a * ny + b) * nz + cc) structured = false;
+        const int ca = (i - corner[q][0] + nx) % nx, cb = (j - corner[q][1] + ny) % ny, ccc = (k - corner[q][2] + nz) % nz;
+        if (node_cells[8 * c + q] != (ca * ny + cb) * nz + ccc) structured = false;
+      }
+    }
+  }
+  h->structured = structured ? 1 : 0;
+
+  const size_t esz = (precision == MM_PREC_FP32) ? sizeof(float) : sizeof(double);
+  const int ncb = mm::cell_blocks(h), nnb = mm::node_blocks(h);
+  bool ok = dev_alloc(&h->d_tt, MM_MAX_TYPES) && dev_alloc(&h->d_box, 9) && dev_alloc(&h->d_cell_type, M) &&
+            dev_alloc(&h->d_mass, N) && dev_alloc(&h->d_invm, N) && dev_alloc(&h->d_c2, N) &&
+            dev_alloc(&h->d_u, 3 * (size_t)N) && dev_alloc(&h->d_v, 3 * (size_t)N) &&
+            dev_alloc((char**)&h->d_disp, 3 * (size_t)N * esz) && dev_alloc((char**)&h->d_G, 24 * (size_t)M * esz) &&
+            dev_alloc(&h->d_ecell, M) && dev_alloc(&h->d_cpart, (size_t)ncb * 10) &&
+            dev_alloc(&h->d_npart, (size_t)nnb * 9) && dev_alloc(&h->d_ticket, 1) && dev_alloc(&h->d_carry, 4) &&
+            dev_alloc(&h->d_io, 6 * (size_t)N + 10) && dev_alloc(&h->d_flag, 1);
+  if (ok && !structured)
+    ok = dev_alloc(&h->d_cell_nodes, 8 * (size_t)M) && dev_alloc(&h->d_node_cells, 8 * (size_t)N) &&
+         dev_alloc(&h->d_node_lat, 3 * (size_t)N);
+  if (!ok) {
+    free_handle(h);
+    return MM_ERR_CUDA;
+  }
+  // uploads
+  std::vector<uint8_t> ty(M);
+  for (int i = 0; i < M; ++i) ty[i] = (uint8_t)cell_type[i];
+  h->h_mass.assign(masses, masses + N);
+  std::vector<double> invm(N);
+  for (int i = 0; i < N; ++i) invm[i] = 1.0 / masses[i];
+  bool up = cuda_ok(cudaMemcpy(h->d_tt, h->tt, sizeof(h->tt), cudaMemcpyHostToDevice), "upload tt") &&
+            cuda_ok(cudaMemcpy(h->d_cell_type, ty.data(), M, cudaMemcpyHostToDevice), "upload types") &&
+            cuda_ok(cudaMemcpy(h->d_mass, masses, N * sizeof(double), cudaMemcpyHostToDevice), "upload mass") &&
+            cuda_ok(cudaMemcpy(h->d_invm, invm.data(), N * sizeof(double), cudaMemcpyHostToDevice), "upload invm") &&
+            cuda_ok(cudaMemset(h->d_ticket, 0, sizeof(unsigned)), "memset") &&
+            cuda_ok(cudaMemset(h->d_carry, 0, 4 * sizeof(double)), "memset") &&
+            cuda_ok(cudaMemset(h->d_v, 0, 3 * (size_t)N * sizeof(double)), "memset") &&
+            cuda_ok(cudaMemset(h->d_flag, 0, sizeof(int)), "memset");
+  if (up && !structured) {
+    std::vector<int32_t> cn(8 * (size_t)M), nc(8 * (size_t)N), nl(3 * (size_t)N);
+    for (int c = 0; c < M; ++c)
+      for (int q = 0; q < 8; ++q) cn[(size_t)q * M + c] = cell_nodes[8 * c + q];
+    for (int n = 0; n < N; ++n) {
+      for (int q = 0; q < 8; ++q) nc[(size_t)q * N + n] = node_cells[8 * n + q];
+      for (int d = 0; d < 3; ++d) nl[(size_t)d * N + n] = node_coords[3 * n + d];
+    }
+    up = cuda_ok(cudaMemcpy(h->d_cell_nodes, cn.data(), cn.size() * 4, cudaMemcpyHostToDevice), "upload cn") &&
+         cuda_ok(cudaMemcpy(h->d_node_cells, nc.data(), nc.size() * 4, cudaMemcpyHostToDevice), "upload nc") &&
+         cuda_ok(cudaMemcpy(h->d_node_lat, nl.data(), nl.size() * 4, cudaMemcpyHostToDevice), "upload nl");
+  }
+  if (!up) {
+    free_handle(h);
+    return MM_ERR_CUDA;
+  }
+  // default lattice matrix: unit spacing until mm_set_domain is called
+  for (int i = 0; i < 9; ++i) h->L[i] = (i % 4 == 0) ? 1.0 : 0.0;
+  if (upload_box(h) != MM_OK) {
+    free_handle(h);
+    return MM_ERR_CUDA;
+  }
+  *out = h;
+  return MM_OK;
+}
+
+mm_status mm_destroy(mm_handle* h) {
+  free_handle(h);
+  return MM_OK;
+}
+
+mm_status mm_set_domain(mm_handle* h, const double* rvecs, const double* lattice) {
+  if (!h) return MM_ERR_ARG;
+  if (h->pbc && !rvecs) {
+    mm::set_error("mm_set_domain: periodic system needs rvecs");
+    return MM_ERR_ARG;
+  }
+  if (!h->pbc && !lattice) {
+    mm::set_error("mm_set_domain: isolated system needs a lattice matrix");
+    return MM_ERR_ARG;
+  }
+  if (rvecs) {
+    std::memcpy(h->rvecs, rvecs, 9 * sizeof(double));
+    double inv[9], det;
+    inv3(rvecs, inv, &det);
+    h->volume = std::fabs(det);
+  } else {
+    std::memset(h->rvecs, 0, sizeof(h->rvecs));
+    h->volume = 0.0;
+  }
+  if (lattice) {
+    std::memcpy(h->L, lattice, 9 * sizeof(double));
+  } else {
+    for (int d = 0; d < 3; ++d)
+      for (int x = 0; x < 3; ++x) h->L[3 * d + x] = rvecs[3 * d + x] / h->nn[d];
+  }
+  return upload_box(h);
+}
+
+mm_status mm_compute(mm_handle* h, const double* pos, double* gpos, double* vtens, double* energy, int* status_dev,
+                     void* stream) {
+  if (!h || !pos || !energy) return MM_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  mm::launch_pos_to_state(h, pos, st);
+  mm::launch_cells(h, st, h->d_ecell);
+  if (gpos) mm::launch_gather(h, gpos, status_dev, st);
+  mm::launch_finalize(h, energy, vtens, status_dev, st);
+  MM_CUDA(cudaGetLastError());
+  return MM_OK;
+}
+
+mm_status mm_compute_host(mm_handle* h, const double* pos, double* gpos, double* vtens, double* energy) {
+  if (!h || !pos || !energy) return MM_ERR_ARG;
+  const size_t n3 = 3 * (size_t)h->N;
+  double* d_pos = h->d_io;
+  double* d_gpos = h->d_io + n3;
+  double* d_out = h->d_io + 2 * n3;  // energy, vtens(9)
+  cudaStream_t st = 0;
+  MM_CUDA(cudaMemcpyAsync(d_pos, pos, n3 * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (gpos) MM_CUDA(cudaMemcpyAsync(d_gpos, gpos, n3 * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (vtens) MM_CUDA(cudaMemcpyAsync(d_out + 1, vtens, 9 * sizeof(double), cudaMemcpyHostToDevice, st));
+  MM_CUDA(cudaMemsetAsync(h->d_flag, 0, sizeof(int), st));
+  mm_status s = mm_compute(h, d_pos, gpos ? d_gpos : nullptr, vtens ? d_out + 1 : nullptr, d_out, h->d_flag, st);
+  if (s != MM_OK) return s;
+  int flag = 0;
+  double out[10];
+  if (gpos) MM_CUDA(cudaMemcpyAsync(gpos, d_gpos, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MM_CUDA(cudaMemcpyAsync(out, d_out, 10 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MM_CUDA(cudaMemcpyAsync(&flag, h->d_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+  MM_CUDA(cudaStreamSynchronize(st));
+  *energy = out[0];
+  if (vtens) std::memcpy(vtens, out + 1, 9 * sizeof(double));
+  if (flag || std::isnan(out[0])) {
+    mm::set_error("NaN in energy, gradient or virial");
+    return MM_ERR_NAN;
+  }
+  return MM_OK;
+}
+
+mm_status mm_cell_results(mm_handle* h, double* epot_cells, double* gpos_cells, void* stream) {
+  if (!h) return MM_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (epot_cells)
+    MM_CUDA(cudaMemcpyAsync(epot_cells, h->d_ecell, h->M * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  if (gpos_cells) {
+    // corner-major SoA [k][x][M] -> (M, 8, 3), converted to FP64 on the host side of torch;
+    // here only the FP64 layout transform is offered for FP64 handles.
+    if (h->prec != MM_PREC_FP64) {
+      mm::set_error("mm_cell_results: gpos_cells is only available for FP64 handles");
+      return MM_ERR_ARG;
+    }
+    // strided transpose: one 2-D copy per (corner, component)
+    for (int q = 0; q < 24; ++q)
+      MM_CUDA(cudaMemcpy2DAsync(gpos_cells + q, 24 * sizeof(double), (double*)h->d_G + (size_t)q * h->M,
+                                sizeof(double), sizeof(double), h->M, cudaMemcpyDeviceToDevice, st));
+  }
+  return MM_OK;
+}
+
+mm_status mm_md_run(mm_handle* h, double* pos, double* vel, int nsteps, double timestep, int thermo, double temp,
+                    double timecon, uint64_t seed, const double* noise, double* records, int64_t step0,
+                    void* stream) {
+  if (!h || !pos || !vel || nsteps < 0 || !(timestep > 0.0)) return MM_ERR_ARG;
+  if (thermo != MM_THERMO_NONE && thermo != MM_THERMO_LANGEVIN) return MM_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  double c1 = 1.0;
+  if (thermo == MM_THERMO_LANGEVIN) {
+    if (!(timecon > 0.0) || !(temp >= 0.0)) return MM_ERR_ARG;
+    c1 = std::exp(-timestep / timecon / 2.0);
+    std::vector<double> c2(h->N);
+    for (int i = 0; i < h->N; ++i) c2[i] = std::sqrt((1.0 - c1 * c1) * temp * kBoltzmann / h->h_mass[i]);
+    MM_CUDA(cudaMemcpyAsync(h->d_c2, c2.data(), h->N * sizeof(double), cudaMemcpyHostToDevice, st));
+    MM_CUDA(cudaStreamSynchronize(st));
+  }
+  mm::launch_pos_to_state(h, pos, st);
+  mm::launch_aos_to_soa(h->N, vel, h->d_v, st);
+  const int64_t nstep0 = step0 + 1;
+  // forces at the initial positions, then the first "pre" half of step step0+1
+  mm::launch_cells(h, st, nullptr);
+  mm::launch_md_nodes(h, timestep, c1, seed, step0, nstep0, 0, nsteps > 0, thermo, noise, nullptr, st);
+  for (int s = 1; s <= nsteps; ++s) {
+    mm::launch_cells(h, st, nullptr);
+    mm::launch_md_nodes(h, timestep, c1, seed, step0 + s, nstep0, 1, s < nsteps, thermo, noise,
+                        records ? records + (size_t)(s - 1) * MM_REC_LEN : nullptr, st);
+  }
+  mm::launch_state_to_pos(h, pos, st);
+  mm::launch_soa_to_aos(h->N, h->d_v, vel, st);
+  MM_CUDA(cudaGetLastError());
+  return MM_OK;
+}
+
+}  // extern "C"

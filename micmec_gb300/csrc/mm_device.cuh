@@ -1,0 +1,301 @@
+// Device-side building blocks of the MicMec force path for sm_103a.
+//
+// One nanocell is a hexahedron with 8 corner nodes. Corner k of a cell sits at
+// lattice offset CORNER_OFF[k] from the cell's origin node, in the order of
+// micmec/utils.py:43-52. Inside the kernels the corners are addressed by their
+// offset bits (x | y<<1 | z<<2), which makes "the edge along d touching corner
+// b" a bit flip; BITS_TO_CORNER / CORNER_TO_BITS convert between the two.
+//
+// Node displacements: every node has a lattice site X = kk*L0 + ll*L1 + mm*L2,
+// with L the lattice matrix (rows L_d = rvecs_d / n_d for a periodic domain).
+// Kernels work with u = pos - X. The edge along d between corners lo and hi is
+// then exactly L_d + u_hi - u_lo, including edges that cross the periodic
+// boundary (the reference's minimum-image shift, micmec/pes/mmff.py:334-371),
+// and the deviation of a corner matrix from a rest matrix h0 is
+// W = (L - h0) + dU: a small number in every precision.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define MM_MAX_TYPES 8
+#define MM_MAX_STATES 4
+
+namespace mm {
+
+// corner index (reference order) <-> offset bits
+__host__ __device__ constexpr int bits_to_corner(int b) {
+  // (0,0,0)0 (1,0,0)1 (0,1,0)2 (1,1,0)4 (0,0,1)3 (1,0,1)5 (0,1,1)6 (1,1,1)7
+  return b == 3 ? 4 : (b == 4 ? 3 : b);
+}
+__host__ __device__ constexpr int corner_to_bits(int k) { return k == 3 ? 4 : (k == 4 ? 3 : k); }
+
+// Per (type, state) parameters in the precision T of the cell arithmetic.
+template <typename T>
+struct StateParams {
+  T hinv[9];   // h0^-1, row-major
+  T B[9];      // L - h0 (rows), for the current lattice matrix L
+  T A[36];     // 6x6: symmetric stress (Voigt 00,11,22,12,02,01) = A . strain
+  T v0;        // det(h0)
+  T df;        // state free energy
+};
+
+template <typename T>
+struct TypeParams {
+  StateParams<T> s[MM_MAX_STATES];
+  T kT;        // boltzmann * effective temperature
+  int nstates;
+};
+
+// Host-side FP64 table (uploaded once); B is derived per launch from L.
+struct StateTable {
+  double h0[9];
+  double hinv[9];
+  double A[36];
+  double v0;
+  double df;
+};
+struct TypeTable {
+  StateTable s[MM_MAX_STATES];
+  double kT;
+  int nstates;
+  int pad;
+};
+
+// Elastic energy of one state and its gradient with respect to the rows of W.
+// W = M - h0 (rows: edge deviations). F = M^T h0^-T = I + D with
+// D[i][k] = sum_j W[j][i] hinv[k][j]; eps = (D + D^T + D^T D)/2;
+// s = A eps; E = scale * eps:s / 2; dE/dW[j][i] = scale * sum_k (F S)[i][k] hinv[k][j].
+// This is the energy of nanocell_original.py:46-82 / nanocell.py:40-77 and the
+// gradient form of nanocell.py:98-132 (stress C_ijkl eps_kl against the
+// symmetric strain derivative).
+template <typename T>
+__device__ __forceinline__ T state_energy_grad(const T* __restrict__ W, const StateParams<T>& p, T scale,
+                                               T* __restrict__ GW) {
+  T D[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      D[i * 3 + k] = W[0 * 3 + i] * p.hinv[k * 3 + 0] + W[1 * 3 + i] * p.hinv[k * 3 + 1] + W[2 * 3 + i] * p.hinv[k * 3 + 2];
+  const T h = T(0.5);
+  T e[6];
+  e[0] = D[0] + h * (D[0] * D[0] + D[3] * D[3] + D[6] * D[6]);
+  e[1] = D[4] + h * (D[1] * D[1] + D[4] * D[4] + D[7] * D[7]);
+  e[2] = D[8] + h * (D[2] * D[2] + D[5] * D[5] + D[8] * D[8]);
+  e[3] = h * (D[5] + D[7] + D[1] * D[2] + D[4] * D[5] + D[7] * D[8]);
+  e[4] = h * (D[2] + D[6] + D[0] * D[2] + D[3] * D[5] + D[6] * D[8]);
+  e[5] = h * (D[1] + D[3] + D[0] * D[1] + D[3] * D[4] + D[6] * D[7]);
+  T s[6];
+#pragma unroll
+  for (int q = 0; q < 6; ++q) {
+    T acc = T(0);
+#pragma unroll
+    for (int r = 0; r < 6; ++r) acc += p.A[q * 6 + r] * e[r];
+    s[q] = acc;
+  }
+  T dens = e[0] * s[0] + e[1] * s[1] + e[2] * s[2] + T(2) * (e[3] * s[3] + e[4] * s[4] + e[5] * s[5]);
+  // S symmetric 3x3 from s
+  const T S[9] = {s[0], s[5], s[4], s[5], s[1], s[3], s[4], s[3], s[2]};
+  // GF = (I + D) S
+  T GF[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int l = 0; l < 3; ++l)
+      GF[i * 3 + l] = S[i * 3 + l] + D[i * 3 + 0] * S[0 * 3 + l] + D[i * 3 + 1] * S[1 * 3 + l] + D[i * 3 + 2] * S[2 * 3 + l];
+  // GW[j][i] = scale * sum_k GF[i][k] hinv[k][j]
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+      GW[j * 3 + i] = scale * (GF[i * 3 + 0] * p.hinv[0 * 3 + j] + GF[i * 3 + 1] * p.hinv[1 * 3 + j] + GF[i * 3 + 2] * p.hinv[2 * 3 + j]);
+  return h * scale * dens;
+}
+
+// Per-cell evaluation. du[b][c]: displacement of the corner with offset bits b.
+// Returns the cell energy (multi-state -kT log-sum-exp, micmec/pes/mmff.py:377-398)
+// and writes the corner gradient g[b][c] (bits order).
+// MODEL 0: single averaged matrix (nanocell_original.py); MODEL 1: eight corner
+// matrices (nanocell.py).
+template <typename T, int MODEL>
+__device__ __forceinline__ double cell_eval(const T (&du)[8][3], const TypeParams<T>& tp, T (&g)[8][3]) {
+  // edge displacement differences along d for the 4 edges with lower-corner bits b (bit d clear)
+  T ed[3][4][3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      // enumerate the 4 corners with bit d clear
+      const int lo = (d == 0) ? (e << 1) : (d == 1 ? ((e & 1) | ((e >> 1) << 2)) : e);
+      const int hi = lo | (1 << d);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) ed[d][e][c] = du[hi][c] - du[lo][c];
+    }
+  }
+  T gacc[8][3];
+  double m = 0.0, wsum = 0.0;
+  const int ns = tp.nstates;
+  for (int s = 0; s < ns; ++s) {
+    const StateParams<T>& p = tp.s[s];
+    T gs[8][3];
+#pragma unroll
+    for (int b = 0; b < 8; ++b)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) gs[b][c] = T(0);
+    T Es;
+    if (MODEL == 0) {
+      T W[9], GW[9];
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          W[d * 3 + c] = p.B[d * 3 + c] + T(0.25) * ((ed[d][0][c] + ed[d][1][c]) + (ed[d][2][c] + ed[d][3][c]));
+      Es = state_energy_grad<T>(W, p, p.v0, GW);
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int lo = (d == 0) ? (e << 1) : (d == 1 ? ((e & 1) | ((e >> 1) << 2)) : e);
+          const int hi = lo | (1 << d);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const T q = T(0.25) * GW[d * 3 + c];
+            gs[hi][c] += q;
+            gs[lo][c] -= q;
+          }
+        }
+    } else {
+      Es = T(0);
+      const T scale = T(0.125) * p.v0;
+#pragma unroll
+      for (int a = 0; a < 8; ++a) {
+        T W[9], GW[9];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const int lo = a & ~(1 << d);
+          // index of that edge among the 4 along d
+          const int e = (d == 0) ? (lo >> 1) : (d == 1 ? ((lo & 1) | ((lo >> 2) << 1)) : (lo & 3));
+#pragma unroll
+          for (int c = 0; c < 3; ++c) W[d * 3 + c] = p.B[d * 3 + c] + ed[d][e][c];
+        }
+        Es += state_energy_grad<T>(W, p, scale, GW);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const int lo = a & ~(1 << d);
+          const int hi = lo | (1 << d);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            gs[hi][c] += GW[d * 3 + c];
+            gs[lo][c] -= GW[d * 3 + c];
+          }
+        }
+      }
+    }
+    const double E = (double)Es + (double)p.df;
+    if (s == 0) {
+      m = E;
+      wsum = 1.0;
+#pragma unroll
+      for (int b = 0; b < 8; ++b)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) gacc[b][c] = gs[b][c];
+    } else {
+      // online -kT log-sum-exp with running minimum m
+      const T kT = tp.kT;
+      if (E < m) {
+        const T r = exp(-(T)(m - E) / kT);  // rescale old terms
+        wsum = wsum * (double)r + 1.0;
+#pragma unroll
+        for (int b = 0; b < 8; ++b)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) gacc[b][c] = gacc[b][c] * r + gs[b][c];
+        m = E;
+      } else {
+        const T w = exp(-(T)(E - m) / kT);
+        wsum += (double)w;
+#pragma unroll
+        for (int b = 0; b < 8; ++b)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) gacc[b][c] += w * gs[b][c];
+      }
+    }
+  }
+  double Ecell = m;
+  if (ns > 1) {
+    const T inv = T(1) / (T)wsum;
+#pragma unroll
+    for (int b = 0; b < 8; ++b)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) gacc[b][c] *= inv;
+    Ecell = m - (double)tp.kT * (double)log((T)wsum);
+  }
+#pragma unroll
+  for (int b = 0; b < 8; ++b)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) g[b][c] = gacc[b][c];
+  return Ecell;
+}
+
+// ---------------------------------------------------------------- reductions
+
+template <int NV>
+__device__ __forceinline__ void warp_sum(double (&v)[NV]) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+    for (int i = 0; i < NV; ++i) v[i] += __shfl_down_sync(0xffffffffu, v[i], off);
+}
+
+// Deterministic block sum of NV doubles; result valid in thread 0.
+// smem must hold NV * (blockDim.x / 32) doubles.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double* smem) {
+  warp_sum<NV>(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0)
+#pragma unroll
+    for (int i = 0; i < NV; ++i) smem[i * nw + wid] = v[i];
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) v[i] = (lane < nw) ? smem[i * nw + lane] : 0.0;
+    warp_sum<NV>(v);
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------- random numbers
+// Philox4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw, SC'11),
+// restated from the published round function and constants.
+struct U4 { uint32_t x, y, z, w; };
+
+__device__ __forceinline__ U4 philox4x32_10(U4 ctr, uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t hi0 = __umulhi(M0, ctr.x), lo0 = M0 * ctr.x;
+    const uint32_t hi1 = __umulhi(M1, ctr.z), lo1 = M1 * ctr.z;
+    ctr = U4{hi1 ^ ctr.y ^ k0, lo1, hi0 ^ ctr.w ^ k1, lo0};
+    k0 += W0;
+    k1 += W1;
+  }
+  return ctr;
+}
+
+// Three standard normals for (node, step, call) via Box-Muller on Philox output.
+__device__ __forceinline__ void normal3(uint64_t seed, uint32_t node, uint32_t step, uint32_t call, float (&z)[3]) {
+  U4 r = philox4x32_10(U4{node, step, call, 0x4d4d4543u}, (uint32_t)seed, (uint32_t)(seed >> 32));
+  const float s = 2.3283064365386963e-10f;  // 2^-32
+  const float u1 = ((float)r.x + 0.5f) * s, u2 = ((float)r.y + 0.5f) * s;
+  const float u3 = ((float)r.z + 0.5f) * s, u4 = ((float)r.w + 0.5f) * s;
+  const float r1 = sqrtf(-2.0f * logf(u1)), r2 = sqrtf(-2.0f * logf(u3));
+  float s1, c1, s2, c2;
+  sincospif(2.0f * u2, &s1, &c1);
+  sincospif(2.0f * u4, &s2, &c2);
+  z[0] = r1 * c1;
+  z[1] = r1 * s1;
+  z[2] = r2 * c2;
+}
+
+}  // namespace mm

@@ -1,0 +1,64 @@
+// Internal state of one mm_handle (a system living on the device) and the
+// kernel launchers shared by the C-ABI translation unit.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/micmec_gb300.h"
+#include "mm_device.cuh"
+
+struct mm_handle {
+  int N = 0, M = 0;
+  int structured = 0;  // implicit periodic lattice: node index == cell index
+  int nn[3] = {0, 0, 0};
+  int pbc = 1;
+  int model = MM_MODEL_NANOCELL;
+  int prec = MM_PREC_FP64;
+  int ntypes = 0;
+  mm::TypeTable tt[MM_MAX_TYPES];
+  double rvecs[9] = {0};
+  double L[9] = {0};
+  double volume = 0.0;
+  std::vector<double> h_mass;
+  // device buffers
+  mm::TypeTable* d_tt = nullptr;
+  double* d_box = nullptr;            // lattice matrix L (9)
+  int32_t* d_cell_nodes = nullptr;    // [8][M]
+  int32_t* d_node_cells = nullptr;    // [8][N]
+  int32_t* d_node_lat = nullptr;      // [3][N]
+  uint8_t* d_cell_type = nullptr;     // [M]
+  double* d_mass = nullptr;           // [N]
+  double* d_invm = nullptr;           // [N]
+  double* d_c2 = nullptr;             // [N] Langevin noise amplitude
+  double* d_u = nullptr;              // [3][N] displacement from lattice sites (FP64)
+  double* d_v = nullptr;              // [3][N] velocities (FP64)
+  void* d_disp = nullptr;             // [3][N] displacement in the cell precision
+  void* d_G = nullptr;                // [24][M] corner gradients in the cell precision
+  double* d_ecell = nullptr;          // [M] per-cell energies (last compute)
+  double* d_cpart = nullptr;          // per cell-block partials
+  double* d_npart = nullptr;          // per node-block partials
+  unsigned* d_ticket = nullptr;       // last-block ticket
+  double* d_carry = nullptr;          // values carried between MD kernels
+  double* d_io = nullptr;             // staging: pos (3N), gpos (3N), energy+vtens (10)
+  int* d_flag = nullptr;              // NaN flag
+};
+
+namespace mm {
+void set_error(const std::string& s);
+const char* last_error();
+int cell_blocks(const mm_handle* h);
+int node_blocks(const mm_handle* h);
+void launch_cells(mm_handle* h, cudaStream_t st, double* ecell);
+void launch_pos_to_state(mm_handle* h, const double* pos, cudaStream_t st);
+void launch_state_to_pos(mm_handle* h, double* pos, cudaStream_t st);
+void launch_gather(mm_handle* h, double* gpos, int* flag, cudaStream_t st);
+void launch_finalize(mm_handle* h, double* energy, double* vtens, int* flag, cudaStream_t st);
+void launch_aos_to_soa(int N, const double* a, double* s, cudaStream_t st);
+void launch_soa_to_aos(int N, const double* s, double* a, cudaStream_t st);
+void launch_md_nodes(mm_handle* h, double dt, double c1, uint64_t seed, int64_t step, int64_t noise_step0, int finish,
+                     int start, int thermo, const double* noise, double* record, cudaStream_t st);
+}  // namespace mm

@@ -1,0 +1,556 @@
+// Force evaluation and fused velocity-Verlet / Langevin steps for one lattice
+// spread over the whole GPU.
+//
+// Per force evaluation two kernels run:
+//   k_cells  : one thread per nanocell. Gathers its 8 corner displacements
+//              (SoA, coalesced along the fastest lattice direction), evaluates
+//              every metastable state and the -kT log-sum-exp combination
+//              (mm_device.cuh), writes the 8x3 corner gradient to a corner-major
+//              SoA buffer G[(corner*3+xyz)*M + cell], and reduces energy and
+//              virial per block in FP64 (deterministic tree).
+//   k_gather / k_md_nodes : one thread per node. Sums the <=8 corner gradients
+//              of its incident cells in corner order (no atomics; the order of
+//              micmec/pes/mmff.py:303-318), then either adds the result to the
+//              caller's gradient (ForcePart.compute) or performs the
+//              velocity-Verlet kick/drift and Langevin updates in FP64.
+// Grid-wide totals use a "last block" pattern: every block writes a partial,
+// an integer ticket picks the last block, and that block sums the partials in
+// block order, so results are bit-reproducible run to run.
+//
+// Periodic lattices whose cells fill the grid (N == M, node index == cell
+// index) use implicit topology (STRUCT = true): no index tables are read.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/micmec_gb300.h"
+#include "mm_device.cuh"
+#include "mm_handle.h"
+
+using namespace mm;
+
+namespace {
+
+constexpr int kCellThreads = 128;
+constexpr int kNodeThreads = 256;
+constexpr int kCellPart = 10;  // energy + virial(9)
+constexpr int kNodePart = 9;   // ekin_a, ekin_b, ekin_c, ktens(6)
+
+struct Topo {
+  int N, M, structured, nx, ny, nz;
+  const int32_t* cell_nodes;  // [8][M]
+  const int32_t* node_cells;  // [8][N]
+  const int32_t* node_lat;    // [3][N]
+  const uint8_t* cell_type;   // [M]
+};
+
+__device__ __forceinline__ void lattice_of(const Topo& t, int n, int& a, int& b, int& c) {
+  if (t.structured) {
+    const int nyz = t.ny * t.nz;
+    a = n / nyz;
+    const int r = n - a * nyz;
+    b = r / t.nz;
+    c = r - b * t.nz;
+  } else {
+    a = t.node_lat[n];
+    b = t.node_lat[t.N + n];
+    c = t.node_lat[2 * t.N + n];
+  }
+}
+
+// node index of corner (bits) of cell `cell` in the implicit periodic lattice
+__device__ __forceinline__ int struct_corner_node(const Topo& t, int i, int j, int k, int bits) {
+  int a = i + (bits & 1), b = j + ((bits >> 1) & 1), c = k + (bits >> 2);
+  a = (a == t.nx) ? 0 : a;
+  b = (b == t.ny) ? 0 : b;
+  c = (c == t.nz) ? 0 : c;
+  return (a * t.ny + b) * t.nz + c;
+}
+
+// cell that has node (i,j,k) as corner with offset bits
+__device__ __forceinline__ int struct_corner_cell(const Topo& t, int i, int j, int k, int bits) {
+  int a = i - (bits & 1), b = j - ((bits >> 1) & 1), c = k - (bits >> 2);
+  a = (a < 0) ? t.nx - 1 : a;
+  b = (b < 0) ? t.ny - 1 : b;
+  c = (c < 0) ? t.nz - 1 : c;
+  return (a * t.ny + b) * t.nz + c;
+}
+
+// Build the per-block parameter table in precision T from the FP64 table and
+// the current lattice matrix L: B = L - h0 is formed in FP64, then rounded.
+template <typename T>
+__device__ void load_params(TypeParams<T>* tp, const TypeTable* tt, int ntypes, const double* box) {
+  for (int idx = threadIdx.x; idx < ntypes * MM_MAX_STATES; idx += blockDim.x) {
+    const int ty = idx / MM_MAX_STATES, s = idx % MM_MAX_STATES;
+    const StateTable& src = tt[ty].s[s];
+    StateParams<T>& dst = tp[ty].s[s];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      dst.hinv[i] = (T)src.hinv[i];
+      dst.B[i] = (T)(box[i] - src.h0[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < 36; ++i) dst.A[i] = (T)src.A[i];
+    dst.v0 = (T)src.v0;
+    dst.df = (T)src.df;
+    if (s == 0) {
+      tp[ty].kT = (T)tt[ty].kT;
+      tp[ty].nstates = tt[ty].nstates;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ kernels
+
+template <typename T>
+__global__ void k_pos_to_state(Topo t, const double* __restrict__ pos, const double* __restrict__ box,
+                               double* __restrict__ u, T* __restrict__ disp) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= t.N) return;
+  int a, b, c;
+  lattice_of(t, n, a, b, c);
+#pragma unroll
+  for (int x = 0; x < 3; ++x) {
+    const double X = a * box[x] + b * box[3 + x] + c * box[6 + x];
+    const double val = pos[3 * n + x] - X;
+    u[x * t.N + n] = val;
+    disp[x * t.N + n] = (T)val;
+  }
+}
+
+__global__ void k_state_to_pos(Topo t, const double* __restrict__ u, const double* __restrict__ box,
+                               double* __restrict__ pos) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= t.N) return;
+  int a, b, c;
+  lattice_of(t, n, a, b, c);
+#pragma unroll
+  for (int x = 0; x < 3; ++x) pos[3 * n + x] = (a * box[x] + b * box[3 + x] + c * box[6 + x]) + u[x * t.N + n];
+}
+
+__global__ void k_aos_to_soa(int N, const double* __restrict__ a, double* __restrict__ s) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+#pragma unroll
+  for (int x = 0; x < 3; ++x) s[x * N + n] = a[3 * n + x];
+}
+
+__global__ void k_soa_to_aos(int N, const double* __restrict__ s, double* __restrict__ a) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+#pragma unroll
+  for (int x = 0; x < 3; ++x) a[3 * n + x] = s[x * N + n];
+}
+
+template <typename T, int MODEL, bool STRUCT>
+__global__ void __launch_bounds__(kCellThreads) k_cells(Topo t, const TypeTable* __restrict__ tt, int ntypes,
+                                                        const double* __restrict__ box, const T* __restrict__ disp,
+                                                        T* __restrict__ G, double* __restrict__ ecell,
+                                                        double* __restrict__ cpart) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TypeParams<T>* tp = reinterpret_cast<TypeParams<T>*>(smem_raw);
+  double* red = reinterpret_cast<double*>(smem_raw + ((sizeof(TypeParams<T>) * ntypes + 15) / 16) * 16);
+  __shared__ T Ls[9];
+  load_params<T>(tp, tt, ntypes, box);
+  if (threadIdx.x < 9) Ls[threadIdx.x] = (T)box[threadIdx.x];
+  __syncthreads();
+
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+  double acc[kCellPart];
+#pragma unroll
+  for (int i = 0; i < kCellPart; ++i) acc[i] = 0.0;
+  if (cell < t.M) {
+    T du[8][3];
+    if (STRUCT) {
+      const int nyz = t.ny * t.nz;
+      const int i = cell / nyz, r = cell - i * nyz, j = r / t.nz, k = r - j * t.nz;
+#pragma unroll
+      for (int b = 0; b < 8; ++b) {
+        const int node = struct_corner_node(t, i, j, k, b);
+#pragma unroll
+        for (int x = 0; x < 3; ++x) du[b][x] = disp[x * t.N + node];
+      }
+    } else {
+#pragma unroll
+      for (int kc = 0; kc < 8; ++kc) {
+        const int node = t.cell_nodes[kc * t.M + cell];
+        const int b = corner_to_bits(kc);
+#pragma unroll
+        for (int x = 0; x < 3; ++x) du[b][x] = disp[x * t.N + node];
+      }
+    }
+    const int ty = t.cell_type[cell];
+    T g[8][3];
+    const double E = cell_eval<T, MODEL>(du, tp[ty], g);
+#pragma unroll
+    for (int kc = 0; kc < 8; ++kc) {
+      const int b = corner_to_bits(kc);
+#pragma unroll
+      for (int x = 0; x < 3; ++x) G[(kc * 3 + x) * (size_t)t.M + cell] = g[b][x];
+    }
+    if (ecell) ecell[cell] = E;
+    acc[0] = E;
+    // virial: sum_b g_b (x) (r_b - r_0), r_b - r_0 = offset(b) . L + du_b - du_0
+    T vt[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) vt[i] = T(0);
+#pragma unroll
+    for (int b = 1; b < 8; ++b) {
+      T rel[3];
+#pragma unroll
+      for (int y = 0; y < 3; ++y) {
+        T r = du[b][y] - du[0][y];
+        if (b & 1) r += Ls[0 * 3 + y];
+        if (b & 2) r += Ls[1 * 3 + y];
+        if (b & 4) r += Ls[2 * 3 + y];
+        rel[y] = r;
+      }
+#pragma unroll
+      for (int x = 0; x < 3; ++x)
+#pragma unroll
+        for (int y = 0; y < 3; ++y) vt[x * 3 + y] += g[b][x] * rel[y];
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) acc[1 + i] = (double)vt[i];
+  }
+  block_sum<kCellPart>(acc, red);
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int i = 0; i < kCellPart; ++i) cpart[blockIdx.x * kCellPart + i] = acc[i];
+}
+
+template <typename T, bool STRUCT>
+__device__ __forceinline__ void gather_node(const Topo& t, const T* __restrict__ G, int n, T (&s)[3]) {
+  s[0] = s[1] = s[2] = T(0);
+  if (STRUCT) {
+    const int nyz = t.ny * t.nz;
+    const int i = n / nyz, r = n - i * nyz, j = r / t.nz, k = r - j * t.nz;
+#pragma unroll
+    for (int kc = 0; kc < 8; ++kc) {
+      const int cell = struct_corner_cell(t, i, j, k, corner_to_bits(kc));
+#pragma unroll
+      for (int x = 0; x < 3; ++x) s[x] += G[(kc * 3 + x) * (size_t)t.M + cell];
+    }
+  } else {
+#pragma unroll
+    for (int kc = 0; kc < 8; ++kc) {
+      const int cell = t.node_cells[kc * t.N + n];
+      if (cell < 0) continue;
+#pragma unroll
+      for (int x = 0; x < 3; ++x) s[x] += G[(kc * 3 + x) * (size_t)t.M + cell];
+    }
+  }
+}
+
+template <typename T, bool STRUCT>
+__global__ void k_gather(Topo t, const T* __restrict__ G, double* __restrict__ gpos, int* __restrict__ flag) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= t.N) return;
+  T s[3];
+  gather_node<T, STRUCT>(t, G, n, s);
+  bool bad = false;
+#pragma unroll
+  for (int x = 0; x < 3; ++x) {
+    const double v = (double)s[x];
+    bad |= isnan(v);
+    gpos[3 * n + x] += v;
+  }
+  if (bad && flag) atomicOr(flag, 1);
+}
+
+// Sum the per-block partials in block order: energy written, virial added.
+__global__ void k_finalize(const double* __restrict__ cpart, int nblk, double* __restrict__ energy,
+                           double* __restrict__ vtens, int* __restrict__ flag) {
+  double acc[kCellPart];
+#pragma unroll
+  for (int i = 0; i < kCellPart; ++i) acc[i] = 0.0;
+  for (int b = threadIdx.x; b < nblk; b += 32)
+#pragma unroll
+    for (int i = 0; i < kCellPart; ++i) acc[i] += cpart[b * kCellPart + i];
+  warp_sum<kCellPart>(acc);
+  if (threadIdx.x == 0) {
+    *energy = acc[0];
+    bool bad = isnan(acc[0]);
+    if (vtens) {
+#pragma unroll
+      for (int i = 0; i < 9; ++i) {
+        bad |= isnan(acc[1 + i]);
+        vtens[i] += acc[1 + i];
+      }
+    }
+    if (bad && flag) atomicOr(flag, 1);
+  }
+}
+
+struct MDArgs {
+  double dt;
+  double c1;            // Langevin exp(-dt / (2 timecon))
+  uint64_t seed;
+  int64_t step;         // step being finished (1-based); the next one is step+1
+  int64_t noise_step0;  // step index of noise[0]
+  int finish;           // kick + post thermostat of `step`
+  int start;            // pre thermostat + kick + drift of `step + 1`
+};
+
+// One thread per node: gather, kick, thermostat, drift, and per-step observables.
+template <typename T, bool STRUCT, int THERMO>
+__global__ void __launch_bounds__(kNodeThreads) k_md_nodes(Topo t, MDArgs p, const T* __restrict__ G,
+                                                           double* __restrict__ u, double* __restrict__ v,
+                                                           T* __restrict__ disp, const double* __restrict__ mass,
+                                                           const double* __restrict__ invm, const double* __restrict__ c2,
+                                                           const double* __restrict__ noise, double* __restrict__ npart,
+                                                           const double* __restrict__ cpart, int ncblk,
+                                                           unsigned* __restrict__ ticket, double* __restrict__ carry,
+                                                           double* __restrict__ record) {
+  __shared__ double red[kNodePart * (kNodeThreads / 32)];
+  __shared__ bool last;
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  double acc[kNodePart];
+#pragma unroll
+  for (int i = 0; i < kNodePart; ++i) acc[i] = 0.0;
+  if (n < t.N) {
+    T s[3];
+    gather_node<T, STRUCT>(t, G, n, s);
+    const double m = mass[n], im = invm[n];
+    double vv[3], a[3];
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+      vv[x] = v[x * t.N + n];
+      a[x] = -(double)s[x] * im;
+    }
+    if (p.finish) {
+#pragma unroll
+      for (int x = 0; x < 3; ++x) vv[x] += 0.5 * a[x] * p.dt;
+      acc[0] = 0.5 * m * (vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]);
+      if (THERMO == MM_THERMO_LANGEVIN) {
+        double z[3];
+        if (noise) {
+          const size_t base = ((size_t)(p.step - p.noise_step0) * 2 + 1) * (size_t)t.N * 3;
+#pragma unroll
+          for (int x = 0; x < 3; ++x) z[x] = noise[base + 3 * n + x];
+        } else {
+          float zf[3];
+          normal3(p.seed, (uint32_t)n, (uint32_t)p.step, 1u, zf);
+#pragma unroll
+          for (int x = 0; x < 3; ++x) z[x] = zf[x];
+        }
+        const double amp = c2[n];
+#pragma unroll
+        for (int x = 0; x < 3; ++x) vv[x] = p.c1 * vv[x] + amp * z[x];
+      }
+    }
+    acc[1] = 0.5 * m * (vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]);
+    acc[3] = m * vv[0] * vv[0];
+    acc[4] = m * vv[1] * vv[1];
+    acc[5] = m * vv[2] * vv[2];
+    acc[6] = m * vv[1] * vv[2];
+    acc[7] = m * vv[0] * vv[2];
+    acc[8] = m * vv[0] * vv[1];
+    if (p.start) {
+      if (THERMO == MM_THERMO_LANGEVIN) {
+        double z[3];
+        if (noise) {
+          const size_t base = ((size_t)(p.step + 1 - p.noise_step0) * 2 + 0) * (size_t)t.N * 3;
+#pragma unroll
+          for (int x = 0; x < 3; ++x) z[x] = noise[base + 3 * n + x];
+        } else {
+          float zf[3];
+          normal3(p.seed, (uint32_t)n, (uint32_t)(p.step + 1), 0u, zf);
+#pragma unroll
+          for (int x = 0; x < 3; ++x) z[x] = zf[x];
+        }
+        const double amp = c2[n];
+#pragma unroll
+        for (int x = 0; x < 3; ++x) vv[x] = p.c1 * vv[x] + amp * z[x];
+      }
+      acc[2] = 0.5 * m * (vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]);
+#pragma unroll
+      for (int x = 0; x < 3; ++x) {
+        vv[x] += 0.5 * a[x] * p.dt;
+        const double un = u[x * t.N + n] + p.dt * vv[x];
+        u[x * t.N + n] = un;
+        disp[x * t.N + n] = (T)un;
+      }
+    }
+#pragma unroll
+    for (int x = 0; x < 3; ++x) v[x * t.N + n] = vv[x];
+  }
+  block_sum<kNodePart>(acc, red);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int i = 0; i < kNodePart; ++i) npart[blockIdx.x * kNodePart + i] = acc[i];
+    __threadfence();
+    const unsigned prev = atomicAdd(ticket, 1u);
+    last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last || threadIdx.x >= 32) return;
+  __threadfence();
+  // last block: totals in block order (one warp, fixed strided split + fixed tree)
+  double tn[kNodePart], tc[kCellPart];
+#pragma unroll
+  for (int i = 0; i < kNodePart; ++i) tn[i] = 0.0;
+#pragma unroll
+  for (int i = 0; i < kCellPart; ++i) tc[i] = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += 32)
+#pragma unroll
+    for (int i = 0; i < kNodePart; ++i) tn[i] += ((volatile double*)npart)[b * kNodePart + i];
+  for (int b = threadIdx.x; b < ncblk; b += 32)
+#pragma unroll
+    for (int i = 0; i < kCellPart; ++i) tc[i] += cpart[b * kCellPart + i];
+  warp_sum<kNodePart>(tn);
+  warp_sum<kCellPart>(tc);
+  if (threadIdx.x == 0) {
+    *ticket = 0u;
+    if (record) {
+      record[MM_REC_EPOT] = tc[0];
+      record[MM_REC_EKIN] = tn[1];
+      record[MM_REC_DECONS] = (p.finish ? (tn[0] - tn[1]) : 0.0) + (p.finish ? carry[0] : 0.0);
+#pragma unroll
+      for (int i = 0; i < 9; ++i) record[MM_REC_VTENS + i] = tc[1 + i];
+      const double k[9] = {tn[3], tn[8], tn[7], tn[8], tn[4], tn[6], tn[7], tn[6], tn[5]};
+#pragma unroll
+      for (int i = 0; i < 9; ++i) record[MM_REC_KTENS + i] = k[i];
+    }
+    carry[0] = p.start ? (tn[1] - tn[2]) : 0.0;
+    carry[1] = tc[0];
+  }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ host side
+
+namespace mm {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& s) { g_last_error = s; }
+const char* last_error() { return g_last_error.c_str(); }
+
+static void topo_of(const mm_handle* h, Topo& t) {
+  t.N = h->N;
+  t.M = h->M;
+  t.structured = h->structured;
+  t.nx = h->nn[0];
+  t.ny = h->nn[1];
+  t.nz = h->nn[2];
+  t.cell_nodes = h->d_cell_nodes;
+  t.node_cells = h->d_node_cells;
+  t.node_lat = h->d_node_lat;
+  t.cell_type = h->d_cell_type;
+}
+
+static size_t cell_smem(const mm_handle* h) {
+  const size_t tp = (h->prec == MM_PREC_FP32 ? sizeof(TypeParams<float>) : sizeof(TypeParams<double>)) * h->ntypes;
+  return ((tp + 15) / 16) * 16 + sizeof(double) * kCellPart * (kCellThreads / 32);
+}
+
+template <typename T, int MODEL, bool STRUCT>
+static void launch_cells_t(mm_handle* h, cudaStream_t st, double* ecell) {
+  Topo t;
+  topo_of(h, t);
+  const int nblk = (h->M + kCellThreads - 1) / kCellThreads;
+  k_cells<T, MODEL, STRUCT><<<nblk, kCellThreads, cell_smem(h), st>>>(
+      t, h->d_tt, h->ntypes, h->d_box, (const T*)h->d_disp, (T*)h->d_G, ecell, h->d_cpart);
+}
+
+template <typename T>
+static void launch_cells_p(mm_handle* h, cudaStream_t st, double* ecell) {
+  if (h->model == MM_MODEL_ORIGINAL) {
+    if (h->structured) launch_cells_t<T, 0, true>(h, st, ecell);
+    else launch_cells_t<T, 0, false>(h, st, ecell);
+  } else {
+    if (h->structured) launch_cells_t<T, 1, true>(h, st, ecell);
+    else launch_cells_t<T, 1, false>(h, st, ecell);
+  }
+}
+
+void launch_cells(mm_handle* h, cudaStream_t st, double* ecell) {
+  if (h->prec == MM_PREC_FP32) launch_cells_p<float>(h, st, ecell);
+  else launch_cells_p<double>(h, st, ecell);
+}
+
+int cell_blocks(const mm_handle* h) { return (h->M + kCellThreads - 1) / kCellThreads; }
+int node_blocks(const mm_handle* h) { return (h->N + kNodeThreads - 1) / kNodeThreads; }
+
+void launch_pos_to_state(mm_handle* h, const double* pos, cudaStream_t st) {
+  Topo t;
+  topo_of(h, t);
+  const int nb = node_blocks(h);
+  if (h->prec == MM_PREC_FP32)
+    k_pos_to_state<float><<<nb, kNodeThreads, 0, st>>>(t, pos, h->d_box, h->d_u, (float*)h->d_disp);
+  else
+    k_pos_to_state<double><<<nb, kNodeThreads, 0, st>>>(t, pos, h->d_box, h->d_u, (double*)h->d_disp);
+}
+
+void launch_state_to_pos(mm_handle* h, double* pos, cudaStream_t st) {
+  Topo t;
+  topo_of(h, t);
+  k_state_to_pos<<<node_blocks(h), kNodeThreads, 0, st>>>(t, h->d_u, h->d_box, pos);
+}
+
+void launch_gather(mm_handle* h, double* gpos, int* flag, cudaStream_t st) {
+  Topo t;
+  topo_of(h, t);
+  const int nb = node_blocks(h);
+  if (h->prec == MM_PREC_FP32) {
+    if (h->structured) k_gather<float, true><<<nb, kNodeThreads, 0, st>>>(t, (const float*)h->d_G, gpos, flag);
+    else k_gather<float, false><<<nb, kNodeThreads, 0, st>>>(t, (const float*)h->d_G, gpos, flag);
+  } else {
+    if (h->structured) k_gather<double, true><<<nb, kNodeThreads, 0, st>>>(t, (const double*)h->d_G, gpos, flag);
+    else k_gather<double, false><<<nb, kNodeThreads, 0, st>>>(t, (const double*)h->d_G, gpos, flag);
+  }
+}
+
+void launch_finalize(mm_handle* h, double* energy, double* vtens, int* flag, cudaStream_t st) {
+  k_finalize<<<1, 32, 0, st>>>(h->d_cpart, cell_blocks(h), energy, vtens, flag);
+}
+
+void launch_aos_to_soa(int N, const double* a, double* s, cudaStream_t st) {
+  k_aos_to_soa<<<(N + kNodeThreads - 1) / kNodeThreads, kNodeThreads, 0, st>>>(N, a, s);
+}
+void launch_soa_to_aos(int N, const double* s, double* a, cudaStream_t st) {
+  k_soa_to_aos<<<(N + kNodeThreads - 1) / kNodeThreads, kNodeThreads, 0, st>>>(N, s, a);
+}
+
+template <typename T, bool STRUCT, int THERMO>
+static void launch_md_nodes_t(mm_handle* h, const MDArgs& a, const double* noise, double* record, cudaStream_t st) {
+  Topo t;
+  topo_of(h, t);
+  k_md_nodes<T, STRUCT, THERMO><<<node_blocks(h), kNodeThreads, 0, st>>>(
+      t, a, (const T*)h->d_G, h->d_u, h->d_v, (T*)h->d_disp, h->d_mass, h->d_invm, h->d_c2, noise, h->d_npart,
+      h->d_cpart, cell_blocks(h), h->d_ticket, h->d_carry, record);
+}
+
+template <typename T>
+static void launch_md_nodes_p(mm_handle* h, const MDArgs& a, int thermo, const double* noise, double* record,
+                              cudaStream_t st) {
+  if (thermo == MM_THERMO_LANGEVIN) {
+    if (h->structured) launch_md_nodes_t<T, true, MM_THERMO_LANGEVIN>(h, a, noise, record, st);
+    else launch_md_nodes_t<T, false, MM_THERMO_LANGEVIN>(h, a, noise, record, st);
+  } else {
+    if (h->structured) launch_md_nodes_t<T, true, MM_THERMO_NONE>(h, a, noise, record, st);
+    else launch_md_nodes_t<T, false, MM_THERMO_NONE>(h, a, noise, record, st);
+  }
+}
+
+void launch_md_nodes(mm_handle* h, double dt, double c1, uint64_t seed, int64_t step, int64_t noise_step0, int finish,
+                     int start, int thermo, const double* noise, double* record, cudaStream_t st) {
+  MDArgs a;
+  a.dt = dt;
+  a.c1 = c1;
+  a.seed = seed;
+  a.step = step;
+  a.noise_step0 = noise_step0;
+  a.finish = finish;
+  a.start = start;
+  if (h->prec == MM_PREC_FP32) launch_md_nodes_p<float>(h, a, thermo, noise, record, st);
+  else launch_md_nodes_p<double>(h, a, thermo, noise, record, st);
+}
+
+}  // namespace mm
