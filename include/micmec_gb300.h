@@ -20,6 +20,7 @@
 #ifndef MICMEC_GB300_H
 #define MICMEC_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -128,6 +129,42 @@ mm_status mm_cell_results(mm_handle* h, double* epot_cells, double* gpos_cells, 
 mm_status mm_md_run(mm_handle* h, double* pos, double* vel, int nsteps, double timestep, int thermo,
                     double temp, double timecon, uint64_t seed, const double* noise, double* records,
                     int64_t step0, void* stream);
+
+/*
+ * MD session for step-by-step control (what mm_md_run does in one call):
+ *  mm_md_begin   : load pos/vel (device (N,3)), evaluate the forces and start the
+ *                  first step (step0 + 1). Parameters as mm_md_run.
+ *  mm_md_advance : run nsteps steps; records as mm_md_run. With finish = 1 the last
+ *                  step is completed without starting the next one (the state is
+ *                  then a clean end-of-step state); with finish = 0 the next step is
+ *                  already started, so further mm_md_advance calls continue seamlessly.
+ *  mm_md_end     : write the end-of-step state to pos/vel (device (N,3)).
+ */
+mm_status mm_md_begin(mm_handle* h, const double* pos, const double* vel, double timestep, int thermo, double temp,
+                      double timecon, uint64_t seed, const double* noise, int64_t step0, void* stream);
+mm_status mm_md_advance(mm_handle* h, int nsteps, double* records, int finish, void* stream);
+mm_status mm_md_end(mm_handle* h, double* pos, double* vel, void* stream);
+
+/*
+ * Measurement helper: run nsteps steps of the session like mm_md_advance(finish = 0),
+ * with CUDA events around the cell kernel and the node kernel of every step, and
+ * return the summed durations (ms). If flush_buf is given, flush_bytes of it are
+ * overwritten before every step (outside the timed spans) to evict L2.
+ * No reference counterpart (measurement only).
+ */
+mm_status mm_md_time_kernels(mm_handle* h, int nsteps, void* flush_buf, size_t flush_bytes, double* ms_cells,
+                             double* ms_nodes, void* stream);
+
+/*
+ * One velocity-Verlet step with host buffers, the step of
+ * VerletIntegrator.propagate (micmec/sampling/verlet.py:140-166) with an optional
+ * Langevin thermostat before and after it (nvt.py:196-208):
+ *  pos, vel (N,3) host : in/out.   gpos (N,3) host : in = gradient at pos, out = new gradient.
+ *  record host double[MM_REC_LEN] or NULL; MM_REC_DECONS holds the "post" correction only.
+ * Copies in, runs one force evaluation and the fused updates, copies out, synchronises.
+ */
+mm_status mm_md_step_host(mm_handle* h, double* pos, double* vel, double* gpos, double* record, double timestep,
+                          int thermo, double temp, double timecon, uint64_t seed, int64_t step);
 
 /* Last CUDA error string of the calling thread's last failing call. */
 const char* mm_last_error(void);

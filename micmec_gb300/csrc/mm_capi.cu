@@ -175,7 +175,7 @@ mm_status mm_create(int nnodes, int ncells, const int32_t* node_coords, const in
             dev_alloc((char**)&h->d_disp, 3 * (size_t)N * esz) && dev_alloc((char**)&h->d_G, 24 * (size_t)M * esz) &&
             dev_alloc(&h->d_ecell, M) && dev_alloc(&h->d_cpart, (size_t)ncb * 10) &&
             dev_alloc(&h->d_npart, (size_t)nnb * 9) && dev_alloc(&h->d_ticket, 1) && dev_alloc(&h->d_carry, 4) &&
-            dev_alloc(&h->d_io, 6 * (size_t)N + 10) && dev_alloc(&h->d_flag, 1);
+            dev_alloc(&h->d_io, 9 * (size_t)N + 64) && dev_alloc(&h->d_flag, 1);
   if (ok && !structured)
     ok = dev_alloc(&h->d_cell_nodes, 8 * (size_t)M) && dev_alloc(&h->d_node_cells, 8 * (size_t)N) &&
          dev_alloc(&h->d_node_lat, 3 * (size_t)N);
@@ -316,35 +316,163 @@ mm_status mm_cell_results(mm_handle* h, double* epot_cells, double* gpos_cells, 
   return MM_OK;
 }
 
-mm_status mm_md_run(mm_handle* h, double* pos, double* vel, int nsteps, double timestep, int thermo, double temp,
-                    double timecon, uint64_t seed, const double* noise, double* records, int64_t step0,
-                    void* stream) {
-  if (!h || !pos || !vel || nsteps < 0 || !(timestep > 0.0)) return MM_ERR_ARG;
+static mm_status md_prepare(mm_handle* h, double timestep, int thermo, double temp, double timecon, uint64_t seed,
+                            cudaStream_t st) {
+  if (!(timestep > 0.0)) return MM_ERR_ARG;
   if (thermo != MM_THERMO_NONE && thermo != MM_THERMO_LANGEVIN) return MM_ERR_ARG;
-  cudaStream_t st = (cudaStream_t)stream;
-  double c1 = 1.0;
+  h->md.dt = timestep;
+  h->md.thermo = thermo;
+  h->md.temp = temp;
+  h->md.timecon = timecon;
+  h->md.seed = seed;
+  h->md.c1 = 1.0;
   if (thermo == MM_THERMO_LANGEVIN) {
     if (!(timecon > 0.0) || !(temp >= 0.0)) return MM_ERR_ARG;
-    c1 = std::exp(-timestep / timecon / 2.0);
-    std::vector<double> c2(h->N);
-    for (int i = 0; i < h->N; ++i) c2[i] = std::sqrt((1.0 - c1 * c1) * temp * kBoltzmann / h->h_mass[i]);
-    MM_CUDA(cudaMemcpyAsync(h->d_c2, c2.data(), h->N * sizeof(double), cudaMemcpyHostToDevice, st));
-    MM_CUDA(cudaStreamSynchronize(st));
+    h->md.c1 = std::exp(-timestep / timecon / 2.0);
+    if (h->md.c2_key[0] != timestep || h->md.c2_key[1] != temp || h->md.c2_key[2] != timecon) {
+      std::vector<double> c2(h->N);
+      const double c1 = h->md.c1;
+      for (int i = 0; i < h->N; ++i) c2[i] = std::sqrt((1.0 - c1 * c1) * temp * kBoltzmann / h->h_mass[i]);
+      MM_CUDA(cudaMemcpyAsync(h->d_c2, c2.data(), h->N * sizeof(double), cudaMemcpyHostToDevice, st));
+      MM_CUDA(cudaStreamSynchronize(st));
+      h->md.c2_key[0] = timestep;
+      h->md.c2_key[1] = temp;
+      h->md.c2_key[2] = timecon;
+    }
   }
+  return MM_OK;
+}
+
+mm_status mm_md_begin(mm_handle* h, const double* pos, const double* vel, double timestep, int thermo, double temp,
+                      double timecon, uint64_t seed, const double* noise, int64_t step0, void* stream) {
+  if (!h || !pos || !vel) return MM_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  mm_status s = md_prepare(h, timestep, thermo, temp, timecon, seed, st);
+  if (s != MM_OK) return s;
+  h->md.noise = noise;
+  h->md.noise_step0 = step0 + 1;
+  h->md.step = step0;
   mm::launch_pos_to_state(h, pos, st);
   mm::launch_aos_to_soa(h->N, vel, h->d_v, st);
-  const int64_t nstep0 = step0 + 1;
-  // forces at the initial positions, then the first "pre" half of step step0+1
+  // forces at the initial positions, then the first half of step step0+1
   mm::launch_cells(h, st, nullptr);
-  mm::launch_md_nodes(h, timestep, c1, seed, step0, nstep0, 0, nsteps > 0, thermo, noise, nullptr, st);
-  for (int s = 1; s <= nsteps; ++s) {
-    mm::launch_cells(h, st, nullptr);
-    mm::launch_md_nodes(h, timestep, c1, seed, step0 + s, nstep0, 1, s < nsteps, thermo, noise,
-                        records ? records + (size_t)(s - 1) * MM_REC_LEN : nullptr, st);
+  mm::launch_md_nodes(h, h->md.dt, h->md.c1, h->md.seed, h->md.step, h->md.noise_step0, 0, 1, h->md.thermo,
+                      h->md.noise, nullptr, nullptr, st);
+  h->md.mid = 1;
+  MM_CUDA(cudaGetLastError());
+  return MM_OK;
+}
+
+mm_status mm_md_advance(mm_handle* h, int nsteps, double* records, int finish, void* stream) {
+  if (!h || nsteps < 0) return MM_ERR_ARG;
+  if (!h->md.mid) {
+    mm::set_error("mm_md_advance: no step in progress (call mm_md_begin)");
+    return MM_ERR_ARG;
   }
+  cudaStream_t st = (cudaStream_t)stream;
+  for (int s = 1; s <= nsteps; ++s) {
+    const int last = finish && (s == nsteps);
+    mm::launch_cells(h, st, nullptr);
+    mm::launch_md_nodes(h, h->md.dt, h->md.c1, h->md.seed, h->md.step + 1, h->md.noise_step0, 1, !last,
+                        h->md.thermo, h->md.noise, records ? records + (size_t)(s - 1) * MM_REC_LEN : nullptr,
+                        nullptr, st);
+    h->md.step += 1;
+    if (last) h->md.mid = 0;
+  }
+  MM_CUDA(cudaGetLastError());
+  return MM_OK;
+}
+
+mm_status mm_md_end(mm_handle* h, double* pos, double* vel, void* stream) {
+  if (!h || !pos || !vel) return MM_ERR_ARG;
+  if (h->md.mid) {
+    mm::set_error("mm_md_end: a step is in progress (advance with finish=1 first)");
+    return MM_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
   mm::launch_state_to_pos(h, pos, st);
   mm::launch_soa_to_aos(h->N, h->d_v, vel, st);
   MM_CUDA(cudaGetLastError());
+  return MM_OK;
+}
+
+mm_status mm_md_run(mm_handle* h, double* pos, double* vel, int nsteps, double timestep, int thermo, double temp,
+                    double timecon, uint64_t seed, const double* noise, double* records, int64_t step0,
+                    void* stream) {
+  if (!h || !pos || !vel || nsteps < 0) return MM_ERR_ARG;
+  if (nsteps == 0) return MM_OK;
+  mm_status s = mm_md_begin(h, pos, vel, timestep, thermo, temp, timecon, seed, noise, step0, stream);
+  if (s != MM_OK) return s;
+  s = mm_md_advance(h, nsteps, records, 1, stream);
+  if (s != MM_OK) return s;
+  return mm_md_end(h, pos, vel, stream);
+}
+
+mm_status mm_md_time_kernels(mm_handle* h, int nsteps, void* flush_buf, size_t flush_bytes, double* ms_cells,
+                              double* ms_nodes, void* stream) {
+  if (!h || nsteps <= 0 || !ms_cells || !ms_nodes) return MM_ERR_ARG;
+  if (!h->md.mid) {
+    mm::set_error("mm_md_time_kernels: no step in progress (call mm_md_begin)");
+    return MM_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  std::vector<cudaEvent_t> ev(3 * (size_t)nsteps);
+  for (auto& e : ev) MM_CUDA(cudaEventCreate(&e));
+  for (int s = 0; s < nsteps; ++s) {
+    if (flush_buf && flush_bytes) MM_CUDA(cudaMemsetAsync(flush_buf, s & 0xff, flush_bytes, st));
+    MM_CUDA(cudaEventRecord(ev[3 * s], st));
+    mm::launch_cells(h, st, nullptr);
+    MM_CUDA(cudaEventRecord(ev[3 * s + 1], st));
+    mm::launch_md_nodes(h, h->md.dt, h->md.c1, h->md.seed, h->md.step + 1, h->md.noise_step0, 1, 1, h->md.thermo,
+                        h->md.noise, nullptr, nullptr, st);
+    MM_CUDA(cudaEventRecord(ev[3 * s + 2], st));
+    h->md.step += 1;
+  }
+  MM_CUDA(cudaStreamSynchronize(st));
+  double a = 0.0, b = 0.0;
+  for (int s = 0; s < nsteps; ++s) {
+    float t1 = 0.f, t2 = 0.f;
+    MM_CUDA(cudaEventElapsedTime(&t1, ev[3 * s], ev[3 * s + 1]));
+    MM_CUDA(cudaEventElapsedTime(&t2, ev[3 * s + 1], ev[3 * s + 2]));
+    a += t1;
+    b += t2;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  *ms_cells = a;
+  *ms_nodes = b;
+  return MM_OK;
+}
+
+mm_status mm_md_step_host(mm_handle* h, double* pos, double* vel, double* gpos, double* record, double timestep,
+                          int thermo, double temp, double timecon, uint64_t seed, int64_t step) {
+  if (!h || !pos || !vel || !gpos) return MM_ERR_ARG;
+  cudaStream_t st = 0;
+  mm_status s = md_prepare(h, timestep, thermo, temp, timecon, seed, st);
+  if (s != MM_OK) return s;
+  const size_t n3 = 3 * (size_t)h->N;
+  double* d_pos = h->d_io;
+  double* d_gpos = h->d_io + n3;
+  double* d_vel = h->d_io + 2 * n3;
+  double* d_rec = h->d_io + 3 * n3;
+  MM_CUDA(cudaMemcpyAsync(d_pos, pos, n3 * sizeof(double), cudaMemcpyHostToDevice, st));
+  MM_CUDA(cudaMemcpyAsync(d_vel, vel, n3 * sizeof(double), cudaMemcpyHostToDevice, st));
+  MM_CUDA(cudaMemcpyAsync(d_gpos, gpos, n3 * sizeof(double), cudaMemcpyHostToDevice, st));
+  mm::launch_pos_to_state(h, d_pos, st);
+  mm::launch_aos_to_soa(h->N, d_vel, h->d_v, st);
+  // carry (pre-thermostat correction) is produced by the begin kernel only through ekin;
+  // the host-buffer step reports the post-thermostat correction alone.
+  MM_CUDA(cudaMemsetAsync(h->d_carry, 0, sizeof(double), st));
+  mm::launch_md_begin_gpos(h, h->md.dt, h->md.c1, seed, step, thermo, d_gpos, nullptr, st);
+  mm::launch_cells(h, st, nullptr);
+  mm::launch_md_nodes(h, h->md.dt, h->md.c1, seed, step, step, 1, 0, thermo, nullptr, d_rec, d_gpos, st);
+  mm::launch_state_to_pos(h, d_pos, st);
+  mm::launch_soa_to_aos(h->N, h->d_v, d_vel, st);
+  MM_CUDA(cudaGetLastError());
+  MM_CUDA(cudaMemcpyAsync(pos, d_pos, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MM_CUDA(cudaMemcpyAsync(vel, d_vel, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MM_CUDA(cudaMemcpyAsync(gpos, d_gpos, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (record) MM_CUDA(cudaMemcpyAsync(record, d_rec, MM_REC_LEN * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MM_CUDA(cudaStreamSynchronize(st));
   return MM_OK;
 }
 

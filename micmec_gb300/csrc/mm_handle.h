@@ -45,6 +45,17 @@ struct mm_handle {
   double* d_carry = nullptr;          // values carried between MD kernels
   double* d_io = nullptr;             // staging: pos (3N), gpos (3N), energy+vtens (10)
   int* d_flag = nullptr;              // NaN flag
+  // MD session
+  struct {
+    double dt = 0.0, c1 = 1.0, temp = 0.0, timecon = 0.0;
+    int thermo = 0;
+    uint64_t seed = 0;
+    int64_t step = 0;          // last step whose first half has been applied
+    int64_t noise_step0 = 0;   // step index of noise[0]
+    const double* noise = nullptr;
+    int mid = 0;               // 1: the next step has been started (x advanced)
+    double c2_key[3] = {-1.0, -1.0, -1.0};
+  } md;
 };
 
 namespace mm {
@@ -60,5 +71,7 @@ void launch_finalize(mm_handle* h, double* energy, double* vtens, int* flag, cud
 void launch_aos_to_soa(int N, const double* a, double* s, cudaStream_t st);
 void launch_soa_to_aos(int N, const double* s, double* a, cudaStream_t st);
 void launch_md_nodes(mm_handle* h, double dt, double c1, uint64_t seed, int64_t step, int64_t noise_step0, int finish,
-                     int start, int thermo, const double* noise, double* record, cudaStream_t st);
+                     int start, int thermo, const double* noise, double* record, double* gpos_out, cudaStream_t st);
+void launch_md_begin_gpos(mm_handle* h, double dt, double c1, uint64_t seed, int64_t step, int thermo,
+                          const double* gpos, const double* noise, cudaStream_t st);
 }  // namespace mm

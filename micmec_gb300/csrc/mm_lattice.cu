@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_md_nodes(Topo t, MDArgs p, con
                                                            const double* __restrict__ noise, double* __restrict__ npart,
                                                            const double* __restrict__ cpart, int ncblk,
                                                            unsigned* __restrict__ ticket, double* __restrict__ carry,
-                                                           double* __restrict__ record) {
+                                                           double* __restrict__ record, double* __restrict__ gpos_out) {
   __shared__ double red[kNodePart * (kNodeThreads / 32)];
   __shared__ bool last;
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -322,6 +322,9 @@ __global__ void __launch_bounds__(kNodeThreads) k_md_nodes(Topo t, MDArgs p, con
       vv[x] = v[x * t.N + n];
       a[x] = -(double)s[x] * im;
     }
+    if (gpos_out)
+#pragma unroll
+      for (int x = 0; x < 3; ++x) gpos_out[3 * n + x] = (double)s[x];
     if (p.finish) {
 #pragma unroll
       for (int x = 0; x < 3; ++x) vv[x] += 0.5 * a[x] * p.dt;
@@ -418,6 +421,42 @@ __global__ void __launch_bounds__(kNodeThreads) k_md_nodes(Topo t, MDArgs p, con
     }
     carry[0] = p.start ? (tn[1] - tn[2]) : 0.0;
     carry[1] = tc[0];
+  }
+}
+
+// First half of a step from a caller-provided gradient (AoS): "pre" thermostat,
+// kick, drift. Used by the host-buffer step entry point.
+template <typename T, int THERMO>
+__global__ void k_md_begin_gpos(Topo t, MDArgs p, const double* __restrict__ gpos, double* __restrict__ u,
+                                double* __restrict__ v, T* __restrict__ disp, const double* __restrict__ invm,
+                                const double* __restrict__ c2, const double* __restrict__ noise) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= t.N) return;
+  double vv[3];
+#pragma unroll
+  for (int x = 0; x < 3; ++x) vv[x] = v[x * t.N + n];
+  if (THERMO == MM_THERMO_LANGEVIN) {
+    double z[3];
+    if (noise) {
+#pragma unroll
+      for (int x = 0; x < 3; ++x) z[x] = noise[3 * n + x];
+    } else {
+      float zf[3];
+      normal3(p.seed, (uint32_t)n, (uint32_t)p.step, 0u, zf);
+#pragma unroll
+      for (int x = 0; x < 3; ++x) z[x] = zf[x];
+    }
+#pragma unroll
+    for (int x = 0; x < 3; ++x) vv[x] = p.c1 * vv[x] + c2[n] * z[x];
+  }
+  const double im = invm[n];
+#pragma unroll
+  for (int x = 0; x < 3; ++x) {
+    vv[x] += 0.5 * (-gpos[3 * n + x] * im) * p.dt;
+    const double un = u[x * t.N + n] + p.dt * vv[x];
+    u[x * t.N + n] = un;
+    disp[x * t.N + n] = (T)un;
+    v[x * t.N + n] = vv[x];
   }
 }
 
@@ -519,28 +558,29 @@ void launch_soa_to_aos(int N, const double* s, double* a, cudaStream_t st) {
 }
 
 template <typename T, bool STRUCT, int THERMO>
-static void launch_md_nodes_t(mm_handle* h, const MDArgs& a, const double* noise, double* record, cudaStream_t st) {
+static void launch_md_nodes_t(mm_handle* h, const MDArgs& a, const double* noise, double* record, double* gpos_out,
+                              cudaStream_t st) {
   Topo t;
   topo_of(h, t);
   k_md_nodes<T, STRUCT, THERMO><<<node_blocks(h), kNodeThreads, 0, st>>>(
       t, a, (const T*)h->d_G, h->d_u, h->d_v, (T*)h->d_disp, h->d_mass, h->d_invm, h->d_c2, noise, h->d_npart,
-      h->d_cpart, cell_blocks(h), h->d_ticket, h->d_carry, record);
+      h->d_cpart, cell_blocks(h), h->d_ticket, h->d_carry, record, gpos_out);
 }
 
 template <typename T>
 static void launch_md_nodes_p(mm_handle* h, const MDArgs& a, int thermo, const double* noise, double* record,
-                              cudaStream_t st) {
+                              double* gpos_out, cudaStream_t st) {
   if (thermo == MM_THERMO_LANGEVIN) {
-    if (h->structured) launch_md_nodes_t<T, true, MM_THERMO_LANGEVIN>(h, a, noise, record, st);
-    else launch_md_nodes_t<T, false, MM_THERMO_LANGEVIN>(h, a, noise, record, st);
+    if (h->structured) launch_md_nodes_t<T, true, MM_THERMO_LANGEVIN>(h, a, noise, record, gpos_out, st);
+    else launch_md_nodes_t<T, false, MM_THERMO_LANGEVIN>(h, a, noise, record, gpos_out, st);
   } else {
-    if (h->structured) launch_md_nodes_t<T, true, MM_THERMO_NONE>(h, a, noise, record, st);
-    else launch_md_nodes_t<T, false, MM_THERMO_NONE>(h, a, noise, record, st);
+    if (h->structured) launch_md_nodes_t<T, true, MM_THERMO_NONE>(h, a, noise, record, gpos_out, st);
+    else launch_md_nodes_t<T, false, MM_THERMO_NONE>(h, a, noise, record, gpos_out, st);
   }
 }
 
 void launch_md_nodes(mm_handle* h, double dt, double c1, uint64_t seed, int64_t step, int64_t noise_step0, int finish,
-                     int start, int thermo, const double* noise, double* record, cudaStream_t st) {
+                     int start, int thermo, const double* noise, double* record, double* gpos_out, cudaStream_t st) {
   MDArgs a;
   a.dt = dt;
   a.c1 = c1;
@@ -549,8 +589,34 @@ void launch_md_nodes(mm_handle* h, double dt, double c1, uint64_t seed, int64_t 
   a.noise_step0 = noise_step0;
   a.finish = finish;
   a.start = start;
-  if (h->prec == MM_PREC_FP32) launch_md_nodes_p<float>(h, a, thermo, noise, record, st);
-  else launch_md_nodes_p<double>(h, a, thermo, noise, record, st);
+  if (h->prec == MM_PREC_FP32) launch_md_nodes_p<float>(h, a, thermo, noise, record, gpos_out, st);
+  else launch_md_nodes_p<double>(h, a, thermo, noise, record, gpos_out, st);
+}
+
+void launch_md_begin_gpos(mm_handle* h, double dt, double c1, uint64_t seed, int64_t step, int thermo,
+                          const double* gpos, const double* noise, cudaStream_t st) {
+  Topo t;
+  topo_of(h, t);
+  MDArgs a;
+  a.dt = dt;
+  a.c1 = c1;
+  a.seed = seed;
+  a.step = step;
+  a.noise_step0 = step;
+  a.finish = 0;
+  a.start = 1;
+  const int nb = node_blocks(h);
+  if (h->prec == MM_PREC_FP32) {
+    if (thermo == MM_THERMO_LANGEVIN)
+      k_md_begin_gpos<float, MM_THERMO_LANGEVIN><<<nb, kNodeThreads, 0, st>>>(t, a, gpos, h->d_u, h->d_v, (float*)h->d_disp, h->d_invm, h->d_c2, noise);
+    else
+      k_md_begin_gpos<float, MM_THERMO_NONE><<<nb, kNodeThreads, 0, st>>>(t, a, gpos, h->d_u, h->d_v, (float*)h->d_disp, h->d_invm, h->d_c2, noise);
+  } else {
+    if (thermo == MM_THERMO_LANGEVIN)
+      k_md_begin_gpos<double, MM_THERMO_LANGEVIN><<<nb, kNodeThreads, 0, st>>>(t, a, gpos, h->d_u, h->d_v, (double*)h->d_disp, h->d_invm, h->d_c2, noise);
+    else
+      k_md_begin_gpos<double, MM_THERMO_NONE><<<nb, kNodeThreads, 0, st>>>(t, a, gpos, h->d_u, h->d_v, (double*)h->d_disp, h->d_invm, h->d_c2, noise);
+  }
 }
 
 }  // namespace mm
