@@ -1,0 +1,373 @@
+"""Benchmark: nanocell-steps/s of Langevin MD on a 64^3 two-type, two-state lattice.
+
+Workload (one "step" = one velocity-Verlet step with the Langevin thermostat
+applied before and after it, over the whole lattice):
+  periodic 64 x 64 x 64 lattice, 262,144 cells and nodes; 90% fcu and 10% reo
+  cells (seeded permutation); 2 metastable states per type (h0 x (1 +/- 0.015),
+  free energies 0 and 2 kJ/mol, effective temperature 300 K); eight-corner-matrix
+  ("nanocell") energy model with FP32 per-cell arithmetic, FP64 state and
+  reductions; Langevin 300 K, timecon 100 fs, dt 1 fs.
+  Synthetic inputs: Gaussian node displacements (0.05 A) and Maxwell-Boltzmann
+  velocities at 300 K from a fixed seed.
+
+Timing: W untimed warm-up steps; then K steps, each bracketed by CUDA events
+on the launching stream, with a 256 MiB buffer overwritten before every step
+(outside the events) so that no step starts from a warm L2. ``value`` is
+cells x K / (summed event time). ``e2e`` is the same metric through the
+host-buffer C-ABI step (mm_md_step_host): per step pos, vel and gpos are copied
+in from pinned host memory and back out, plus the step record.
+
+``--impl reference`` times the CPU restatement of the reference's force
+evaluation and Langevin step (the oracle, NumPy FP64) on a bounded sample of the
+same lattice with all host cores (one process per core, spawn), reported in the
+same unit.
+
+Multi-GPU: the path is run as independent replicas, one per rank
+(torchrun); ``value`` sums the cells of all ranks over the slowest rank's time.
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "cell-steps/s"
+UNIT = "nanocell-steps/s"
+N_SIDE = 64
+DEFECT = 0.10
+SEED = 1234
+FLUSH_BYTES = 256 << 20
+
+# algorithmic figures (per cell, per evaluation / step)
+STEP_BYTES = 97          # pos r/w 24+24, vel r/w 24+24, cell type 1 (FP64 SoA state)
+CELL_KERNEL_BYTES = 109  # displacement read 12 (FP32 xyz), type 1, corner gradients written 96 (24 x FP32)
+FLOP_PER_STATE = 2400    # 8 corner matrices x ~300 flop (strain, stress, energy, gradient)
+FLOP_LSE = 20
+
+
+def config(nstates=2):
+    return {
+        "workload": "lattice64_langevin_nvt",
+        "lattice": [N_SIDE] * 3,
+        "cells": N_SIDE**3,
+        "types": {"fcu": 1 - DEFECT, "reo": DEFECT},
+        "states_per_type": nstates,
+        "model": "nanocell (8 corner matrices)",
+        "cell_precision": "fp32",
+        "state_precision": "fp64",
+        "thermostat": "langevin 300 K, timecon 100 fs",
+        "timestep_fs": 1.0,
+        "l2": "flushed before every timed step (256 MiB overwrite)",
+        "parallelism": "replicas",
+    }
+
+
+def build_workload(nstates=2):
+    from micmec_gb300 import lattices, units
+    from micmec_gb300.system import System
+
+    rng = np.random.default_rng(SEED)
+    grid = lattices.defect_grid(N_SIDE, DEFECT, rng)
+    d = lattices.make_lattice(grid, nstates=nstates)
+    d["pos"] = lattices.displace(d["pos"], 0.05 * units.angstrom, rng)
+    s = System.from_dict(d)
+    kT = units.boltzmann * 300.0
+    vel = rng.normal(0.0, 1.0, s.pos.shape) * np.sqrt(kT / s.masses)[:, None]
+    vel -= (s.masses @ vel) / s.masses.sum()
+    return s, d, vel
+
+
+def peaks():
+    fn = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(fn):
+        with open(fn) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler(object):
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.proc = None
+        self.index = index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[3:7]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {
+            "sm_mhz": float(np.median(sm)) if sm else None,
+            "sm_max_mhz": float(max(smax)) if smax else None,
+            "samples": len(sm),
+            "reasons": sorted(reasons),
+        }
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------- reference (CPU) arm
+
+
+def cpu_langevin_steps(d, vel, nsteps, nproc, model="nanocell"):
+    """Oracle Langevin steps (force evaluation split over nproc processes); returns seconds."""
+    import multiprocessing as mp
+
+    from oracle import md as omd
+
+    ctx = mp.get_context("spawn")
+    pool = ctx.Pool(nproc) if nproc > 1 else None
+    try:
+        state = omd.LangevinState(d, vel.copy(), model=model, temp=300.0, timecon_fs=100.0, dt_fs=1.0, seed=SEED,
+                                  pool=pool, nproc=nproc)
+        t0 = time.perf_counter()
+        for _ in range(nsteps):
+            state.step()
+        return time.perf_counter() - t0
+    finally:
+        if pool is not None:
+            pool.close()
+            pool.join()
+
+
+def run_reference(args):
+    """CPU arm: the oracle's Langevin step with all host cores, on bounded samples of the lattice."""
+    import multiprocessing as mp
+
+    from oracle import md as omd
+
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    s, d, vel = build_workload()
+    nproc = os.cpu_count() or 1
+    pool = mp.get_context("spawn").Pool(nproc)
+    try:
+        state = omd.LangevinState(d, vel.copy(), model="nanocell", temp=300.0, timecon_fs=100.0, dt_fs=1.0,
+                                  seed=SEED, pool=pool, nproc=nproc)
+        M = s.ncells
+        t0 = time.perf_counter()
+        state.step()  # one full-lattice step to size the samples
+        t_full = time.perf_counter() - t0
+        budget = float(os.environ.get("MICMEC_REF_BUDGET_S", "90"))
+        per_step = budget / max(1, args.steps + args.warmup)
+        ncells = int(max(nproc * 64, min(M, M * per_step / t_full)))
+        for _ in range(args.warmup):
+            state.step(ncells)
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            state.step(ncells)
+            times.append(time.perf_counter() - t0)
+    finally:
+        pool.close()
+        pool.join()
+    tot = float(np.sum(times))
+    value = ncells * args.steps / tot
+    sample = ("Langevin step of the 64^3 lattice with the force evaluation restricted to the first %d cells "
+              "(full-lattice step: %.2f s), NumPy FP64 oracle split over %d spawned processes" % (ncells, t_full, nproc))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config(),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nproc, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------- GPU arm
+
+
+def run_gpu(args):
+    import torch
+
+    from micmec_gb300 import _native as nat
+    from micmec_gb300.pes.mmff import ForcePartMechanical
+
+    rank, world, local = dist_env()
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+        pg = dist
+
+    s, d, vel = build_workload()
+    M = s.ncells
+    fp = ForcePartMechanical(s, model="nanocell", precision="fp32")
+    L = nat.lib()
+    stream = torch.cuda.current_stream().cuda_stream
+    pos_d = torch.from_numpy(np.ascontiguousarray(s.pos)).to(dev)
+    vel_d = torch.from_numpy(np.ascontiguousarray(vel)).to(dev)
+    from micmec_gb300 import units
+
+    dt, temp, tau = 1.0 * units.femtosecond, 300.0, 100.0 * units.femtosecond
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    rec = torch.empty((max(args.steps, 1), nat.MM_REC_LEN), dtype=torch.float64, device=dev)
+
+    nat.check(L.mm_md_begin(fp.handle, pos_d.data_ptr(), vel_d.data_ptr(), dt, 1, temp, tau, SEED, None, 0, stream),
+              "mm_md_begin")
+    for _ in range(args.warmup):
+        nat.check(L.mm_md_advance(fp.handle, 1, None, 0, stream), "mm_md_advance")
+    torch.cuda.synchronize()
+
+    # ---- timed region
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    if pg is not None:
+        pg.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t_wall0 = time.perf_counter()
+    for i in range(args.steps):
+        flush.fill_(i & 0xFF)
+        ev[i][0].record()
+        nat.check(L.mm_md_advance(fp.handle, 1, rec[i].data_ptr(), 0, stream), "mm_md_advance")
+        ev[i][1].record()
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    if pg is not None:
+        pg.barrier()
+    # keep sampling a moment so short regions still have clock samples
+    time.sleep(0.3)
+    clk = clocks.stop()
+    ms = float(sum(a.elapsed_time(b) for a, b in ev))
+    if pg is not None:
+        t = torch.tensor([ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+    recs = rec.cpu().numpy()
+    finite = bool(np.isfinite(recs[: args.steps, :2]).all())
+    value = world * M * args.steps / (ms * 1e-3)
+
+    # ---- per-kernel timing for the roofline (same session, same flush)
+    nk = max(20, min(200, args.steps))
+    mc, mn = nat.c_double(), nat.c_double()
+    nat.check(L.mm_md_time_kernels(fp.handle, nk, flush.data_ptr(), FLUSH_BYTES, nat.ctypes.byref(mc),
+                                   nat.ctypes.byref(mn), stream), "mm_md_time_kernels")
+    cell_ms, node_ms = mc.value / nk, mn.value / nk
+    nat.check(L.mm_md_advance(fp.handle, 1, None, 1, stream), "mm_md_advance")
+    torch.cuda.synchronize()
+
+    # ---- e2e through the host-buffer C-ABI step
+    pos_h = torch.from_numpy(np.ascontiguousarray(s.pos)).pin_memory()
+    vel_h = torch.from_numpy(np.ascontiguousarray(vel)).pin_memory()
+    gpos_h = torch.zeros((s.nnodes, 3), dtype=torch.float64).pin_memory()
+    rec_h = torch.zeros(nat.MM_REC_LEN, dtype=torch.float64).pin_memory()
+    e_steps = max(3, min(args.steps, 50))
+    fp.compute_device(pos_d.copy_(pos_h), None, None)  # warm
+    for i in range(2 + e_steps):
+        if i == 2:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+        nat.check(L.mm_md_step_host(fp.handle, pos_h.data_ptr(), vel_h.data_ptr(), gpos_h.data_ptr(),
+                                    rec_h.data_ptr(), dt, 1, temp, tau, SEED, 10**6 + i), "mm_md_step_host")
+    e2e_s = time.perf_counter() - t0
+    e2e_value = world * M * e_steps / e2e_s
+
+    # ---- roofline of the dominant kernel (cells)
+    hbm, kind = peaks()
+    achieved = CELL_KERNEL_BYTES * M / (cell_ms * 1e-3) / 1e9
+    flops = (FLOP_PER_STATE * 2 + FLOP_LSE) * M / (cell_ms * 1e-3) / 1e12
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "cells_fp32_nanocell_traffic.json")
+    if os.path.exists(tfile):
+        with open(tfile) as f:
+            traffic = json.load(f).get("bytes_per_launch_64cubed")
+    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32-cell/f64-state", "data": "synthetic", "config": config(),
+        "wall_s_timed_region": t_wall, "finite": finite,
+        "kernel_ms": {"cells": cell_ms, "nodes": node_ms},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": traffic, "peak_kind": kind,
+                     "note": "cell kernel is FP32-pipe bound; algorithmic bytes per cell %d" % CELL_KERNEL_BYTES,
+                     "compute": {"achieved_tflops_fp32": flops, "nominal_peak_tflops_fp32": fp32_peak,
+                                 "frac_of_nominal": flops / fp32_peak},
+                     "step_hbm_gbs": STEP_BYTES * M * args.steps / (ms * 1e-3) / 1e9},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 3 * 24 * s.nnodes,
+                "d2h_bytes_per_step": 3 * 24 * s.nnodes + 8 * nat.MM_REC_LEN},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        nproc = 1
+        sample_steps = 1
+        tcpu = cpu_langevin_steps(d, vel, sample_steps, nproc)
+        line["cpu_baseline"] = {"value": M * sample_steps / tcpu, "unit": UNIT, "cores": nproc, "kind": "port",
+                                "sample": "%d full 64^3 Langevin step, NumPy FP64 oracle, 1 process" % sample_steps}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

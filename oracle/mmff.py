@@ -170,15 +170,23 @@ def _state_energy_grad(mats, h0, C0, model):
     return E, GM
 
 
-def deformation(pos, rvecs, grid, surrounding_nodes, types, params, model="original", pbc=None):
-    """Per-cell energies (M,), corner gradients (M, 8, 3) and vertices (M, 8, 3)."""
+def deformation(pos, rvecs, grid, surrounding_nodes, types, params, model="original", pbc=None, cells=None,
+                shifts=None):
+    """Per-cell energies (M,), corner gradients (M, 8, 3) and vertices (M, 8, 3).
+
+    ``cells`` (optional index array) restricts the evaluation to those cells;
+    ``shifts`` (optional, from ``cell_shifts``) skips recomputing the image shifts.
+    """
     pos = np.asarray(pos, dtype=np.float64)
     rvecs = np.asarray(rvecs, dtype=np.float64).reshape(-1, 3)
     if pbc is None:
         pbc = rvecs.shape[0] == 3
     sn = np.asarray(surrounding_nodes, dtype=np.int64)
     types = np.asarray(types).astype(np.int64)
-    shifts = cell_shifts(grid, sn, pbc)
+    if shifts is None:
+        shifts = cell_shifts(grid, sn, pbc)
+    if cells is not None:
+        sn, types, shifts = sn[cells], types[cells], shifts[cells]
     r0 = pos[sn[:, 0]]
     dvec = pos[sn] - r0[:, None, :]
     if pbc:
