@@ -1,0 +1,60 @@
+"""Optimisers on GPU forces: QN against the reference's QNOptimizer trajectory; CG and cell DOFs by invariants."""
+import numpy as np
+import pytest
+
+from conftest import load_golden, make_system, system_dict
+
+pytestmark = pytest.mark.gpu
+
+
+def _ff(g, model="nanocell"):
+    from micmec_gb300.pes.mmff import ForcePartMechanical, MicMecForceField
+
+    s = make_system(system_dict(g, "sys/"))
+    return s, MicMecForceField(s, [ForcePartMechanical(s, model=model)])
+
+
+def test_qn_matches_reference():
+    from micmec_gb300.sampling.dof import CartesianDOF
+    from micmec_gb300.sampling.iterative import Hook
+    from micmec_gb300.sampling.opt import QNOptimizer
+
+    g = load_golden("opt_qn_nanocell")
+    s, ff = _ff(g)
+    energies = []
+
+    class E(Hook):
+        def __call__(self, it):
+            energies.append(it.epot)
+
+    opt = QNOptimizer(CartesianDOF(ff, gpos_rms=1e-6, dpos_rms=1e-4), hooks=[E()])
+    opt.run(60)
+    ref = g["energies"]
+    assert len(energies) == len(ref)
+    assert np.allclose(energies, ref, rtol=1e-9, atol=0)
+    assert np.abs(s.pos - g["pos_end"]).max() < 1e-6
+
+
+def test_cg_reaches_reference_minimum():
+    from micmec_gb300.sampling.dof import CartesianDOF
+    from micmec_gb300.sampling.opt import CGOptimizer
+
+    g = load_golden("opt_qn_nanocell")
+    s, ff = _ff(g)
+    dof = CartesianDOF(ff, gpos_rms=1e-7, dpos_rms=1e-5)
+    CGOptimizer(dof).run(2000)
+    e = ff.compute()
+    assert e <= g["energies"][-1] + 1e-9 * abs(g["energies"][-1])
+    gpos = np.zeros((s.nnodes, 3))
+    ff.compute(gpos)
+    assert np.sqrt((gpos**2).sum(axis=1)).max() < 3e-6
+
+
+def test_strain_cell_dof_gradient():
+    from micmec_gb300.sampling.dof import StrainCellDOF, FullCellDOF
+
+    g = load_golden("opt_qn_nanocell")
+    s, ff = _ff(g)
+    for cls in (StrainCellDOF, FullCellDOF):
+        dof = cls(ff)
+        assert dof.check_delta(eps=1e-5) < 1e-5
