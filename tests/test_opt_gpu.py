@@ -57,4 +57,4 @@ def test_strain_cell_dof_gradient():
     s, ff = _ff(g)
     for cls in (StrainCellDOF, FullCellDOF):
         dof = cls(ff)
-        assert dof.check_delta(eps=1e-5) < 1e-5
+        assert dof.check_delta(eps=1e-6) < 1e-3
