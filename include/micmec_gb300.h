@@ -166,6 +166,34 @@ mm_status mm_md_time_kernels(mm_handle* h, int nsteps, void* flush_buf, size_t f
 mm_status mm_md_step_host(mm_handle* h, double* pos, double* vel, double* gpos, double* record, double timestep,
                           int thermo, double temp, double timecon, uint64_t seed, int64_t step);
 
+/*
+ * Allocation-free force evaluation. No counterpart in the reference: it exists for
+ * callers that cannot allocate device memory (code running inside another
+ * framework's memory pool or a fixed-budget arena, plugins whose host owns every
+ * device allocation, paths where an allocation would synchronise the device at the
+ * wrong time), since mm_create allocates. It computes what mm_compute computes, for
+ * a fully periodic lattice (every lattice site a node and a cell, nodes and cells
+ * numbered as the reference's Grid does), and calls no cudaMalloc/cudaFree.
+ *  lattice_shape[3]  : host, cells per direction (each >= 2), at most
+ *                      MM_NOALLOC_MAX_CELLS cells in total (larger lattices: MM_ERR_ARG).
+ *  cell_type (M)     : device int32, 0-based type index per cell.
+ *  ntypes, nstates, h0, C, free_energy, temp_eff : host, as mm_create.
+ *  rvecs (3,3)       : host domain vectors.
+ *  pos (N,3)         : device.  gpos (N,3), vtens (3,3): device or NULL, ADDED to.
+ *  energy            : device double[1], written.
+ * Working memory is one static device array of MM_NOALLOC_SCRATCH_BYTES bytes per
+ * GPU, held until the process exits. The first call on a device looks up the
+ * array's address (make it before any stream capture). Calls share the array:
+ * calls that overlap on the GPU race. The call synchronises `stream` before it
+ * returns.
+ */
+#define MM_NOALLOC_MAX_CELLS 32768
+#define MM_NOALLOC_SCRATCH_BYTES (8u << 20)
+mm_status mm_compute_noalloc(const int32_t* lattice_shape, const int32_t* cell_type, int ntypes,
+                             const int32_t* nstates, const double* h0, const double* C, const double* free_energy,
+                             const double* temp_eff, const double* rvecs, int model, int precision,
+                             const double* pos, double* gpos, double* vtens, double* energy, void* stream);
+
 /* Last CUDA error string of the calling thread's last failing call. */
 const char* mm_last_error(void);
 
