@@ -126,6 +126,10 @@ mm_status mm_create(int nnodes, int ncells, const int32_t* node_coords, const in
   h->prec = precision;
   h->ntypes = ntypes;
   for (int d = 0; d < 3; ++d) h->nn[d] = lattice_shape[d];
+  {
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev);
+  }
 
   // parameter table
   for (int t = 0; t < ntypes; ++t) {

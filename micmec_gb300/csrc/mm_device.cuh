@@ -237,6 +237,50 @@ __device__ __forceinline__ double cell_eval(const T (&du)[8][3], const TypeParam
   return Ecell;
 }
 
+// Compensated (error-free TwoSum) FP32 accumulation: a value is the unevaluated
+// sum hi + lo. Used for warp-level sums of per-cell and per-node FP32 terms before
+// the grid-level reduction continues in FP64.
+struct F2 {
+  float hi, lo;
+};
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  const float err = (a.hi - (s - bb)) + (b.hi - bb);
+  return F2{s, err + a.lo + b.lo};
+}
+template <int NV>
+__device__ __forceinline__ void warp_sum_f2(F2 (&v)[NV]) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      F2 o{__shfl_down_sync(0xffffffffu, v[i].hi, off), __shfl_down_sync(0xffffffffu, v[i].lo, off)};
+      v[i] = f2_add(v[i], o);
+    }
+}
+
+// Block sum: compensated FP32 within each warp, FP64 across warps (fixed order).
+// Result valid in thread 0. smem must hold NV * (blockDim.x / 32) doubles.
+template <int NV>
+__device__ __forceinline__ void block_sum_f2(F2 (&v)[NV], double (&out)[NV], double* smem) {
+  warp_sum_f2<NV>(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0)
+#pragma unroll
+    for (int i = 0; i < NV; ++i) smem[i * nw + wid] = (double)v[i].hi + (double)v[i].lo;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      double acc = 0.0;
+      for (int w = 0; w < nw; ++w) acc += smem[i * nw + w];
+      out[i] = acc;
+    }
+  }
+  __syncthreads();
+}
+
 // ---------------------------------------------------------------- reductions
 
 template <int NV>

@@ -19,6 +19,7 @@ struct mm_handle {
   int model = MM_MODEL_NANOCELL;
   int prec = MM_PREC_FP64;
   int ntypes = 0;
+  int num_sms = 0;
   mm::TypeTable tt[MM_MAX_TYPES];
   double rvecs[9] = {0};
   double L[9] = {0};

@@ -25,6 +25,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/micmec_gb300.h"
@@ -217,10 +218,191 @@ __global__ void __launch_bounds__(kCellThreads) k_cells(Topo t, const TypeTable*
 #pragma unroll
     for (int i = 0; i < 9; ++i) acc[1 + i] = (double)vt[i];
   }
-  block_sum<kCellPart>(acc, red);
+  if constexpr (sizeof(T) == 8) {
+    block_sum<kCellPart>(acc, red);
+  } else {
+    F2 f[kCellPart];
+#pragma unroll
+    for (int i = 0; i < kCellPart; ++i) {
+      const float hi = (float)acc[i];
+      f[i] = F2{hi, i == 0 ? (float)(acc[i] - (double)hi) : 0.0f};
+    }
+    block_sum_f2<kCellPart>(f, acc, red);
+  }
   if (threadIdx.x == 0)
 #pragma unroll
     for (int i = 0; i < kCellPart; ++i) cpart[blockIdx.x * kCellPart + i] = acc[i];
+}
+
+// Eight lanes per cell for the eight-corner-matrix model: lane a (offset bits of
+// corner a) evaluates corner matrix a for every state. The three edges of matrix a
+// join vertex a to its neighbours a^1, a^2, a^4, whose displacements come from
+// xor-shuffles inside the 8-lane group; state energies are summed with three
+// xor-shuffles; vertex a's gradient collects, for each direction d, the row-d
+// gradient of matrix a and of matrix a^(1<<d) (the same edge). Corner gradients are
+// staged in shared memory and written as contiguous runs of the corner-major
+// layout. Energy and virial are summed per warp in compensated FP32 and per block
+// in FP64.
+constexpr int kCell8Threads = 256;
+constexpr int kCell8Cells = kCell8Threads / 8;
+
+template <typename T, bool STRUCT>
+__global__ void __launch_bounds__(kCell8Threads) k_cells8(Topo t, const TypeTable* __restrict__ tt, int ntypes,
+                                                          const double* __restrict__ box, const T* __restrict__ disp,
+                                                          T* __restrict__ G, double* __restrict__ ecell,
+                                                          double* __restrict__ cpart) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TypeParams<T>* tp = reinterpret_cast<TypeParams<T>*>(smem_raw);
+  const size_t tp_bytes = ((sizeof(TypeParams<T>) * ntypes + 15) / 16) * 16;
+  T* tile = reinterpret_cast<T*>(smem_raw + tp_bytes);  // [24][kCell8Cells]
+  double* red = reinterpret_cast<double*>(smem_raw + tp_bytes + ((sizeof(T) * 24 * kCell8Cells + 15) / 16) * 16);
+  __shared__ T Ls[9];
+  load_params<T>(tp, tt, ntypes, box);
+  if (threadIdx.x < 9) Ls[threadIdx.x] = (T)box[threadIdx.x];
+  __syncthreads();
+
+  const int lane = threadIdx.x & 31;
+  const int a = threadIdx.x & 7;
+  const int cl = threadIdx.x >> 3;
+  const int ngroups = (t.M + kCell8Cells - 1) / kCell8Cells;
+  typedef typename std::conditional<sizeof(T) == 8, double, F2>::type Acc;
+  Acc accum[kCellPart];
+#pragma unroll
+  for (int i = 0; i < kCellPart; ++i) accum[i] = Acc{};
+  for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+  const int cell = grp * kCell8Cells + cl;
+  const bool valid = cell < t.M;
+  T du[3] = {T(0), T(0), T(0)};
+  int ty = 0;
+  if (valid) {
+    int node;
+    if (STRUCT) {
+      const int nyz = t.ny * t.nz;
+      const int i = cell / nyz, r = cell - i * nyz, j = r / t.nz, k = r - j * t.nz;
+      node = struct_corner_node(t, i, j, k, a);
+    } else {
+      node = t.cell_nodes[bits_to_corner(a) * t.M + cell];
+    }
+#pragma unroll
+    for (int x = 0; x < 3; ++x) du[x] = disp[x * t.N + node];
+    ty = t.cell_type[cell];
+  }
+  // edge (vertex a -> neighbour a^(1<<d)) displacement differences, oriented lo -> hi
+  T ed[3][3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const bool hi = (a >> d) & 1;
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+      const T other = __shfl_xor_sync(0xffffffffu, du[x], 1 << d);
+      ed[d][x] = hi ? du[x] - other : other - du[x];
+    }
+  }
+  const TypeParams<T>& tpl = tp[ty];
+  const int ns_lane = valid ? tpl.nstates : 1;
+  const int ns = __reduce_max_sync(0xffffffffu, ns_lane);
+  T g[3] = {T(0), T(0), T(0)};
+  T m = T(0), wsum = T(0);
+  const T kT = tpl.kT;
+  for (int s = 0; s < ns; ++s) {
+    const bool active = s < ns_lane;
+    const StateParams<T>& p = tpl.s[active ? s : 0];
+    T W[9], GW[9];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+      for (int x = 0; x < 3; ++x) W[d * 3 + x] = p.B[d * 3 + x] + ed[d][x];
+    T Es = state_energy_grad<T>(W, p, T(0.125) * p.v0, GW);
+    Es += __shfl_xor_sync(0xffffffffu, Es, 1);
+    Es += __shfl_xor_sync(0xffffffffu, Es, 2);
+    Es += __shfl_xor_sync(0xffffffffu, Es, 4);
+    T gs[3] = {T(0), T(0), T(0)};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const T sg = ((a >> d) & 1) ? T(1) : T(-1);
+#pragma unroll
+      for (int x = 0; x < 3; ++x) {
+        const T mine = GW[d * 3 + x];
+        gs[x] += sg * (mine + __shfl_xor_sync(0xffffffffu, mine, 1 << d));
+      }
+    }
+    if (active) {
+      const T E = Es + p.df;
+      if (s == 0) {
+        m = E;
+        wsum = T(1);
+#pragma unroll
+        for (int x = 0; x < 3; ++x) g[x] = gs[x];
+      } else if (E < m) {
+        const T r = exp((E - m) / kT);
+        wsum = wsum * r + T(1);
+#pragma unroll
+        for (int x = 0; x < 3; ++x) g[x] = g[x] * r + gs[x];
+        m = E;
+      } else {
+        const T w = exp((m - E) / kT);
+        wsum += w;
+#pragma unroll
+        for (int x = 0; x < 3; ++x) g[x] += w * gs[x];
+      }
+    }
+  }
+  T Ecell = m;
+  if (ns_lane > 1) {
+    const T inv = T(1) / wsum;
+#pragma unroll
+    for (int x = 0; x < 3; ++x) g[x] *= inv;
+    Ecell = m - kT * log(wsum);
+  }
+  // stage corner gradients: tile[(corner*3 + x)][cl]
+  const int corner = bits_to_corner(a);
+#pragma unroll
+  for (int x = 0; x < 3; ++x) tile[(corner * 3 + x) * kCell8Cells + cl] = g[x];
+  if (valid && a == 0 && ecell) ecell[cell] = (double)Ecell;
+  // virial: g_a (x) (offset(a) . L + du_a - du_0)
+  const int src0 = lane & ~7;
+  T rel[3];
+#pragma unroll
+  for (int y = 0; y < 3; ++y) {
+    const T d0 = __shfl_sync(0xffffffffu, du[y], src0);
+    T r = du[y] - d0;
+    if (a & 1) r += Ls[0 * 3 + y];
+    if (a & 2) r += Ls[1 * 3 + y];
+    if (a & 4) r += Ls[2 * 3 + y];
+    rel[y] = r;
+  }
+  T vals[kCellPart];
+  vals[0] = (valid && a == 0) ? Ecell : T(0);
+#pragma unroll
+  for (int x = 0; x < 3; ++x)
+#pragma unroll
+    for (int y = 0; y < 3; ++y) vals[1 + x * 3 + y] = valid ? g[x] * rel[y] : T(0);
+  if constexpr (sizeof(T) == 8) {
+#pragma unroll
+    for (int i = 0; i < kCellPart; ++i) accum[i] += vals[i];
+  } else {
+#pragma unroll
+    for (int i = 0; i < kCellPart; ++i) accum[i] = f2_add(accum[i], F2{(float)vals[i], 0.0f});
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < 24 * kCell8Cells; idx += blockDim.x) {
+    const int row = idx / kCell8Cells, col = idx - row * kCell8Cells;
+    const int c = grp * kCell8Cells + col;
+    if (c < t.M) G[row * (size_t)t.M + c] = tile[idx];
+  }
+  __syncthreads();
+  }  // groups
+  double out[kCellPart];
+  if constexpr (sizeof(T) == 8) {
+#pragma unroll
+    for (int i = 0; i < kCellPart; ++i) out[i] = accum[i];
+    block_sum<kCellPart>(out, red);
+  } else {
+    block_sum_f2<kCellPart>(accum, out, red);
+  }
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int i = 0; i < kCellPart; ++i) cpart[blockIdx.x * kCellPart + i] = out[i];
 }
 
 template <typename T, bool STRUCT>
@@ -265,13 +447,14 @@ __global__ void k_gather(Topo t, const T* __restrict__ G, double* __restrict__ g
 // Sum the per-block partials in block order: energy written, virial added.
 __global__ void k_finalize(const double* __restrict__ cpart, int nblk, double* __restrict__ energy,
                            double* __restrict__ vtens, int* __restrict__ flag) {
+  __shared__ double red[kCellPart * 8];
   double acc[kCellPart];
 #pragma unroll
   for (int i = 0; i < kCellPart; ++i) acc[i] = 0.0;
-  for (int b = threadIdx.x; b < nblk; b += 32)
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x)
 #pragma unroll
     for (int i = 0; i < kCellPart; ++i) acc[i] += cpart[b * kCellPart + i];
-  warp_sum<kCellPart>(acc);
+  block_sum<kCellPart>(acc, red);
   if (threadIdx.x == 0) {
     *energy = acc[0];
     bool bad = isnan(acc[0]);
@@ -309,13 +492,17 @@ __global__ void __launch_bounds__(kNodeThreads) k_md_nodes(Topo t, MDArgs p, con
   __shared__ double red[kNodePart * (kNodeThreads / 32)];
   __shared__ bool last;
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  double acc[kNodePart];
+  // per-node observables: FP64 for an FP64 handle; for an FP32 handle in FP32, summed
+  // per warp with compensated FP32 and per block in FP64
+  typedef typename std::conditional<sizeof(T) == 8, double, float>::type R;
+  R obs[kNodePart];
 #pragma unroll
-  for (int i = 0; i < kNodePart; ++i) acc[i] = 0.0;
+  for (int i = 0; i < kNodePart; ++i) obs[i] = R(0);
   if (n < t.N) {
     T s[3];
     gather_node<T, STRUCT>(t, G, n, s);
     const double m = mass[n], im = invm[n];
+    const R mf = (R)m;
     double vv[3], a[3];
 #pragma unroll
     for (int x = 0; x < 3; ++x) {
@@ -328,7 +515,10 @@ __global__ void __launch_bounds__(kNodeThreads) k_md_nodes(Topo t, MDArgs p, con
     if (p.finish) {
 #pragma unroll
       for (int x = 0; x < 3; ++x) vv[x] += 0.5 * a[x] * p.dt;
-      acc[0] = 0.5 * m * (vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]);
+      {
+        const R v0 = (R)vv[0], v1 = (R)vv[1], v2 = (R)vv[2];
+        obs[0] = R(0.5) * mf * (v0 * v0 + v1 * v1 + v2 * v2);
+      }
       if (THERMO == MM_THERMO_LANGEVIN) {
         double z[3];
         if (noise) {
@@ -346,13 +536,16 @@ __global__ void __launch_bounds__(kNodeThreads) k_md_nodes(Topo t, MDArgs p, con
         for (int x = 0; x < 3; ++x) vv[x] = p.c1 * vv[x] + amp * z[x];
       }
     }
-    acc[1] = 0.5 * m * (vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]);
-    acc[3] = m * vv[0] * vv[0];
-    acc[4] = m * vv[1] * vv[1];
-    acc[5] = m * vv[2] * vv[2];
-    acc[6] = m * vv[1] * vv[2];
-    acc[7] = m * vv[0] * vv[2];
-    acc[8] = m * vv[0] * vv[1];
+    {
+      const R v0 = (R)vv[0], v1 = (R)vv[1], v2 = (R)vv[2];
+      obs[1] = R(0.5) * mf * (v0 * v0 + v1 * v1 + v2 * v2);
+      obs[3] = mf * v0 * v0;
+      obs[4] = mf * v1 * v1;
+      obs[5] = mf * v2 * v2;
+      obs[6] = mf * v1 * v2;
+      obs[7] = mf * v0 * v2;
+      obs[8] = mf * v0 * v1;
+    }
     if (p.start) {
       if (THERMO == MM_THERMO_LANGEVIN) {
         double z[3];
@@ -370,7 +563,10 @@ __global__ void __launch_bounds__(kNodeThreads) k_md_nodes(Topo t, MDArgs p, con
 #pragma unroll
         for (int x = 0; x < 3; ++x) vv[x] = p.c1 * vv[x] + amp * z[x];
       }
-      acc[2] = 0.5 * m * (vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]);
+      {
+        const R v0 = (R)vv[0], v1 = (R)vv[1], v2 = (R)vv[2];
+        obs[2] = R(0.5) * mf * (v0 * v0 + v1 * v1 + v2 * v2);
+      }
 #pragma unroll
       for (int x = 0; x < 3; ++x) {
         vv[x] += 0.5 * a[x] * p.dt;
@@ -382,31 +578,42 @@ __global__ void __launch_bounds__(kNodeThreads) k_md_nodes(Topo t, MDArgs p, con
 #pragma unroll
     for (int x = 0; x < 3; ++x) v[x * t.N + n] = vv[x];
   }
-  block_sum<kNodePart>(acc, red);
+  double tot[kNodePart];
+  if constexpr (sizeof(T) == 8) {
+#pragma unroll
+    for (int i = 0; i < kNodePart; ++i) tot[i] = obs[i];
+    block_sum<kNodePart>(tot, red);
+  } else {
+    F2 acc[kNodePart];
+#pragma unroll
+    for (int i = 0; i < kNodePart; ++i) acc[i] = F2{(float)obs[i], 0.0f};
+    block_sum_f2<kNodePart>(acc, tot, red);
+  }
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int i = 0; i < kNodePart; ++i) npart[blockIdx.x * kNodePart + i] = acc[i];
+    for (int i = 0; i < kNodePart; ++i) npart[blockIdx.x * kNodePart + i] = tot[i];
     __threadfence();
     const unsigned prev = atomicAdd(ticket, 1u);
     last = (prev == gridDim.x - 1);
   }
   __syncthreads();
-  if (!last || threadIdx.x >= 32) return;
+  if (!last) return;
   __threadfence();
-  // last block: totals in block order (one warp, fixed strided split + fixed tree)
-  double tn[kNodePart], tc[kCellPart];
+  // last block: totals of all partials; each thread takes a fixed strided subset,
+  // then a fixed-order block tree (deterministic)
+  double tt[kNodePart + kCellPart];
 #pragma unroll
-  for (int i = 0; i < kNodePart; ++i) tn[i] = 0.0;
+  for (int i = 0; i < kNodePart + kCellPart; ++i) tt[i] = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
 #pragma unroll
-  for (int i = 0; i < kCellPart; ++i) tc[i] = 0.0;
-  for (int b = threadIdx.x; b < (int)gridDim.x; b += 32)
+    for (int i = 0; i < kNodePart; ++i) tt[i] += ((volatile double*)npart)[b * kNodePart + i];
+  for (int b = threadIdx.x; b < ncblk; b += blockDim.x)
 #pragma unroll
-    for (int i = 0; i < kNodePart; ++i) tn[i] += ((volatile double*)npart)[b * kNodePart + i];
-  for (int b = threadIdx.x; b < ncblk; b += 32)
-#pragma unroll
-    for (int i = 0; i < kCellPart; ++i) tc[i] += cpart[b * kCellPart + i];
-  warp_sum<kNodePart>(tn);
-  warp_sum<kCellPart>(tc);
+    for (int i = 0; i < kCellPart; ++i) tt[kNodePart + i] += cpart[b * kCellPart + i];
+  __shared__ double red2[(kNodePart + kCellPart) * (kNodeThreads / 32)];
+  block_sum<kNodePart + kCellPart>(tt, red2);
+  double* tn = tt;
+  double* tc = tt + kNodePart;
   if (threadIdx.x == 0) {
     *ticket = 0u;
     if (record) {
@@ -485,7 +692,11 @@ static void topo_of(const mm_handle* h, Topo& t) {
 }
 
 static size_t cell_smem(const mm_handle* h) {
+  const size_t esz = h->prec == MM_PREC_FP32 ? sizeof(float) : sizeof(double);
   const size_t tp = (h->prec == MM_PREC_FP32 ? sizeof(TypeParams<float>) : sizeof(TypeParams<double>)) * h->ntypes;
+  if (h->model == MM_MODEL_NANOCELL)
+    return ((tp + 15) / 16) * 16 + ((esz * 24 * kCell8Cells + 15) / 16) * 16 +
+           sizeof(double) * kCellPart * (kCell8Threads / 32);
   return ((tp + 15) / 16) * 16 + sizeof(double) * kCellPart * (kCellThreads / 32);
 }
 
@@ -493,9 +704,14 @@ template <typename T, int MODEL, bool STRUCT>
 static void launch_cells_t(mm_handle* h, cudaStream_t st, double* ecell) {
   Topo t;
   topo_of(h, t);
-  const int nblk = (h->M + kCellThreads - 1) / kCellThreads;
-  k_cells<T, MODEL, STRUCT><<<nblk, kCellThreads, cell_smem(h), st>>>(
-      t, h->d_tt, h->ntypes, h->d_box, (const T*)h->d_disp, (T*)h->d_G, ecell, h->d_cpart);
+  const int nblk = cell_blocks(h);
+  if constexpr (MODEL == 1) {
+    k_cells8<T, STRUCT><<<nblk, kCell8Threads, cell_smem(h), st>>>(
+        t, h->d_tt, h->ntypes, h->d_box, (const T*)h->d_disp, (T*)h->d_G, ecell, h->d_cpart);
+  } else {
+    k_cells<T, MODEL, STRUCT><<<nblk, kCellThreads, cell_smem(h), st>>>(
+        t, h->d_tt, h->ntypes, h->d_box, (const T*)h->d_disp, (T*)h->d_G, ecell, h->d_cpart);
+  }
 }
 
 template <typename T>
@@ -514,7 +730,15 @@ void launch_cells(mm_handle* h, cudaStream_t st, double* ecell) {
   else launch_cells_p<double>(h, st, ecell);
 }
 
-int cell_blocks(const mm_handle* h) { return (h->M + kCellThreads - 1) / kCellThreads; }
+int cell_blocks(const mm_handle* h) {
+  if (h->model == MM_MODEL_NANOCELL) {
+    // grid-stride over groups of cells: at most 4 resident 256-thread blocks per SM
+    const int groups = (h->M + kCell8Cells - 1) / kCell8Cells;
+    const int cap = (h->num_sms > 0 ? h->num_sms : 152) * 4;
+    return groups < cap ? groups : cap;
+  }
+  return (h->M + kCellThreads - 1) / kCellThreads;
+}
 int node_blocks(const mm_handle* h) { return (h->N + kNodeThreads - 1) / kNodeThreads; }
 
 void launch_pos_to_state(mm_handle* h, const double* pos, cudaStream_t st) {
@@ -547,7 +771,7 @@ void launch_gather(mm_handle* h, double* gpos, int* flag, cudaStream_t st) {
 }
 
 void launch_finalize(mm_handle* h, double* energy, double* vtens, int* flag, cudaStream_t st) {
-  k_finalize<<<1, 32, 0, st>>>(h->d_cpart, cell_blocks(h), energy, vtens, flag);
+  k_finalize<<<1, 256, 0, st>>>(h->d_cpart, cell_blocks(h), energy, vtens, flag);
 }
 
 void launch_aos_to_soa(int N, const double* a, double* s, cudaStream_t st) {

@@ -143,6 +143,10 @@ extern "C" mm_status mm_compute_noalloc(const int32_t* lattice_shape, const int3
   h.prec = precision;
   h.ntypes = ntypes;
   for (int d = 0; d < 3; ++d) h.nn[d] = lattice_shape[d];
+  {
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&h.num_sms, cudaDevAttrMultiProcessorCount, dev);
+  }
   const size_t M = (size_t)ncells;
   const size_t esz = precision == MM_PREC_FP32 ? sizeof(float) : sizeof(double);
   size_t off = 0;

@@ -126,3 +126,79 @@ def test_mtk_matches_reference(name):
     vi.run(n)
     _compare(g, rec, n, 1e-7)
     assert np.allclose(s.domain.rvecs, g["rvecs_end"], rtol=1e-9)
+
+
+def _lattice(n, nstates, seed, sigma=0.05):
+    from micmec_gb300 import lattices, units
+    from micmec_gb300.system import System
+
+    rng = np.random.default_rng(seed)
+    d = lattices.make_lattice(lattices.defect_grid(n, 0.1, rng), nstates=nstates)
+    d["pos"] = lattices.displace(d["pos"], sigma * units.angstrom, rng)
+    s = System.from_dict(d)
+    kT = units.boltzmann * 300.0
+    vel = rng.normal(0.0, 1.0, s.pos.shape) * np.sqrt(kT / s.masses)[:, None]
+    vel -= (s.masses @ vel) / s.masses.sum()
+    return s, vel
+
+
+def test_fp32_nve_tracks_fp64_and_conserves_energy():
+    """FP32 cells / FP64 state vs the FP64 path on a 10^3 two-state lattice, 500 NVE steps."""
+    from micmec_gb300 import units
+    from micmec_gb300.pes.mmff import ForcePartMechanical, MicMecForceField
+    from micmec_gb300.sampling.verlet import VerletIntegrator
+
+    out = {}
+    for prec in ("fp64", "fp32"):
+        s, vel = _lattice(10, 2, 3)
+        ff = MicMecForceField(s, [ForcePartMechanical(s, model="nanocell", precision=prec)])
+        rec = Rec()
+        vi = VerletIntegrator(ff, 1.0 * units.femtosecond, hooks=[rec.hook], vel0=vel)
+        vi.run(500)
+        out[prec] = np.array(rec.rows)
+    a, b = out["fp64"], out["fp32"]
+    econs64, econs32 = a[:, 3], b[:, 3]
+    scale = np.abs(a[:, 2]).max()  # kinetic energy scale
+    # conserved quantity: fluctuation relative to the kinetic energy stays small in both
+    assert np.ptp(econs64) < 5e-3 * scale
+    assert np.ptp(econs32) < 5e-3 * scale
+    # short-time trajectories agree
+    assert np.abs(a[:50, 1] - b[:50, 1]).max() < 1e-5 * np.abs(a[:50, 1]).max()
+
+
+def test_langevin_generator_reaches_target_temperature():
+    """Philox noise, no replay: the kinetic temperature settles at the thermostat temperature."""
+    from micmec_gb300 import units
+    from micmec_gb300.pes.mmff import ForcePartMechanical, MicMecForceField
+    from micmec_gb300.sampling.nvt import LangevinThermostat
+    from micmec_gb300.sampling.verlet import VerletIntegrator
+
+    s, vel = _lattice(12, 2, 4)
+    ff = MicMecForceField(s, [ForcePartMechanical(s, model="nanocell", precision="fp32")])
+    rec = Rec()
+    lt = LangevinThermostat(600.0, timecon=20 * units.femtosecond, seed=7)
+    vi = VerletIntegrator(ff, 1.0 * units.femtosecond, hooks=[lt, rec.hook], vel0=vel)
+    vi.run(3000)
+    temps = np.array(rec.rows)[1000:, 4]
+    assert abs(temps.mean() - 600.0) < 0.05 * 600.0
+
+
+def test_device_and_host_langevin_paths_agree_with_replayed_noise_fp32():
+    from micmec_gb300 import units
+    from micmec_gb300.pes.mmff import ForcePartMechanical, MicMecForceField
+    from micmec_gb300.sampling.nvt import LangevinThermostat
+    from micmec_gb300.sampling.verlet import VerletIntegrator
+
+    rows = {}
+    noise = np.random.default_rng(9).normal(size=(2 * 100, 6 ** 3, 3))
+    for device in (True, False):
+        s, vel = _lattice(6, 2, 5)
+        ff = MicMecForceField(s, [ForcePartMechanical(s, model="nanocell", precision="fp32")])
+        rec = Rec()
+        lt = LangevinThermostat(300.0, timecon=100 * units.femtosecond, replay_noise=noise)
+        vi = VerletIntegrator(ff, 1.0 * units.femtosecond, hooks=[lt, rec.hook], vel0=vel, device=device)
+        vi.run(100)
+        rows[device] = np.array(rec.rows)
+    a, b = rows[True], rows[False]
+    for col in (1, 2, 3):
+        assert np.abs(a[:, col] - b[:, col]).max() <= 1e-6 * np.abs(b[:, col]).max()
