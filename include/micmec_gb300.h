@@ -194,6 +194,58 @@ mm_status mm_compute_noalloc(const int32_t* lattice_shape, const int32_t* cell_t
                              const double* temp_eff, const double* rvecs, int model, int precision,
                              const double* pos, double* gpos, double* vtens, double* energy, void* stream);
 
+/*
+ * Batched systems: nsys independent, fully periodic lattices (every lattice site a
+ * node and a cell) of uneven size, evaluated and integrated in one persistent launch
+ * (one CTA runs whole systems). No single reference function corresponds: the
+ * reference runs one System per Python process; this replaces many independent
+ * runs of VerletIntegrator (micmec/sampling/verlet.py:140-166) with
+ * TBCombination / LangevinThermostat / NHCThermostat / MTKBarostat hooks
+ * (npt.py:52-177, 513-757; nvt.py:165-218, 361-532) and of an optimiser
+ * (micmec/sampling/opt.py) over those systems.
+ *  shapes (nsys,3)   : host, cells per direction of each system (each >= 2).
+ *  cell_type (sum M) : host, 0-based type per cell, systems concatenated.
+ *  masses (sum N)    : host, node masses, concatenated.
+ *  Other parameters as mm_create.
+ */
+typedef struct mm_batch mm_batch;
+mm_status mm_batch_create(int nsys, const int32_t* shapes, const int32_t* cell_type, int ntypes,
+                          const int32_t* nstates, const double* h0, const double* C, const double* free_energy,
+                          const double* temp_eff, const double* masses, int model, int precision, mm_batch** out);
+mm_status mm_batch_destroy(mm_batch* b);
+/* Host (sum N,3) positions, velocities (or NULL: zero) and (nsys,3,3) domain vectors. */
+mm_status mm_batch_set_state(mm_batch* b, const double* pos, const double* vel, const double* rvecs);
+mm_status mm_batch_get_state(mm_batch* b, double* pos, double* vel, double* rvecs);
+/*
+ * Per-system controller block, MM_BATCH_CTL doubles per system (host; write = 1 uploads,
+ * 0 downloads): lattice matrix (0..8), domain vectors (9..17), volume (18), energy (19),
+ * kinetic energy (20), virial (21..29), kinetic tensor (30..38), barostat velocity
+ * tensor (39..47), chain positions (48..50), velocities (51..53), masses (54..56),
+ * ndof (57), barostat mass (58), barostat dof (59), thermostat / barostat
+ * conserved-energy corrections (60, 61), relaxation: largest gradient (62), iterations (63).
+ */
+#define MM_BATCH_CTL 72
+#define MM_BATCH_REC 31
+mm_status mm_batch_control(mm_batch* b, double* ctl, int write);
+/*
+ * nsteps MD steps of every system. thermo: 0 none, 1 Langevin, 2 Nose-Hoover chain of
+ * length `chain`; baro: 0 none, 1 anisotropic MTK at pressure `press`. The controller
+ * block must hold ndof, chain masses/state and barostat mass/velocity/dof (as the
+ * reference's hook init sets them). noise (device, (nsteps, 2, sum N, 3)) replays
+ * normals instead of the generator; records (device, (nsys, nsteps, MM_BATCH_REC)):
+ * energy, kinetic energy, conserved-energy correction, volume, virial(9), kinetic
+ * tensor(9), domain vectors(9). use_graph: launch through a cached CUDA graph.
+ */
+mm_status mm_batch_md(mm_batch* b, int nsteps, double timestep, int thermo, double temp, double timecon, int baro,
+                      double press, int chain, uint64_t seed, int64_t step0, const double* noise, double* records,
+                      int use_graph, void* stream);
+/* Relax node positions of every system (domain fixed) until max |gradient| < gtol. */
+mm_status mm_batch_relax(mm_batch* b, int max_iter, double gtol, void* stream);
+/* Choose CTA size and persistent CTA count by timing probe_steps MD steps (state restored). */
+mm_status mm_batch_autotune(mm_batch* b, int probe_steps, double timestep, int thermo, double temp, double timecon,
+                            int baro, double press, int chain, double* best_ms);
+mm_status mm_batch_config(mm_batch* b, int* cta_threads, int* nctas);
+
 /* Last CUDA error string of the calling thread's last failing call. */
 const char* mm_last_error(void);
 

@@ -1,0 +1,247 @@
+"""Batches of independent periodic systems on one GPU (one persistent launch).
+
+``BatchSystems`` packs hundreds of fully periodic lattices of uneven size
+(defect configurations, strain-scan points, replicas) into one device batch.
+``md`` runs velocity-Verlet steps of every system with the reference's hooks
+(none / Langevin / Nose-Hoover chain thermostat, optionally the anisotropic MTK
+barostat) in one persistent kernel (optionally replayed from a CUDA graph);
+``relax`` minimises every system's energy over node positions with nonlinear
+conjugate gradients; ``autotune`` picks the CTA size and the number of
+persistent CTAs by timing.
+
+The hook constants are set up the way the reference's hook ``init`` methods set
+them (micmec/sampling/nvt.py:393-400, 507-523; npt.py:82-97, 579-614):
+degrees of freedom, Nose-Hoover chain masses, barostat mass and the initial
+momentum removal.
+"""
+
+import ctypes
+
+import numpy as np
+
+from micmec_gb300 import _native as nat
+from micmec_gb300.units import boltzmann, femtosecond
+
+__all__ = ["BatchSystems", "CTL", "REC"]
+
+CTL = dict(L=slice(0, 9), rvecs=slice(9, 18), volume=18, epot=19, ekin=20, vtens=slice(21, 30), ktens=slice(30, 39),
+           vel_press=slice(39, 48), chain_pos=slice(48, 51), chain_vel=slice(51, 54), chain_mass=slice(54, 57),
+           ndof=57, mass_press=58, baro_ndof=59, econs_thermo=60, econs_baro=61, gmax=62, iters=63, alpha=64)
+CTL_LEN = 72
+REC = dict(epot=0, ekin=1, ecorr=2, volume=3, vtens=slice(4, 13), ktens=slice(13, 22), rvecs=slice(22, 31))
+REC_LEN = 31
+_THERMO = {None: 0, "langevin": 1, "nhc": 2}
+
+
+def _declare(L):
+    if getattr(L, "_batch_declared", False):
+        return
+    P = ctypes.c_void_p
+    L.mm_batch_create.argtypes = [ctypes.c_int, P, P, ctypes.c_int, P, P, P, P, P, P, ctypes.c_int, ctypes.c_int,
+                                  ctypes.POINTER(ctypes.c_void_p)]
+    L.mm_batch_destroy.argtypes = [P]
+    L.mm_batch_set_state.argtypes = [P, P, P, P]
+    L.mm_batch_get_state.argtypes = [P, P, P, P]
+    L.mm_batch_control.argtypes = [P, P, ctypes.c_int]
+    L.mm_batch_md.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                              ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_uint64, ctypes.c_int64, P, P,
+                              ctypes.c_int, P]
+    L.mm_batch_relax.argtypes = [P, ctypes.c_int, ctypes.c_double, P]
+    L.mm_batch_autotune.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_int, ctypes.c_double, ctypes.c_int, P]
+    L.mm_batch_config.argtypes = [P, P, P]
+    for n in ("mm_batch_create", "mm_batch_destroy", "mm_batch_set_state", "mm_batch_get_state", "mm_batch_control",
+              "mm_batch_md", "mm_batch_relax", "mm_batch_autotune", "mm_batch_config"):
+        getattr(L, n).restype = ctypes.c_int
+    L._batch_declared = True
+
+
+class BatchSystems(object):
+    """A batch of fully periodic ``System`` objects sharing one parameter table.
+
+    Every system's grid must be fully occupied (defects are other cell types) and its
+    ``surrounding_*`` tables must follow the lattice (as ``build_system`` makes them).
+    """
+
+    def __init__(self, systems, model="nanocell", precision="fp32"):
+        import torch
+
+        from micmec_gb300.pes.mmff import type_parameters
+
+        if not torch.cuda.is_available():
+            raise nat.MMError("BatchSystems needs a CUDA device")
+        self.torch = torch
+        self.systems = list(systems)
+        self.model = model
+        self.precision = precision
+        L = nat.lib()
+        _declare(L)
+        self.L = L
+        ids = sorted(set(int(t) for s in self.systems for t in np.asarray(s.types)))
+        index = {k: i for i, k in enumerate(ids)}
+        params = {}
+        for s in self.systems:
+            params.update(s.params)
+        shapes, ctype, masses = [], [], []
+        for s in self.systems:
+            grid = np.asarray(s.grid)
+            if (grid == 0).any() or np.asarray(s.domain.rvecs).shape != (3, 3):
+                raise ValueError("BatchSystems takes fully occupied, 3-D periodic lattices")
+            if s.nnodes != grid.size or s.ncells != grid.size:
+                raise ValueError("node/cell count does not match the grid")
+            shapes.append(grid.shape)
+            ctype.append([index[int(t)] for t in np.asarray(s.types)])
+            masses.append(np.asarray(s.masses, dtype=np.float64))
+        self.sizes = np.array([s.ncells for s in self.systems])
+        self.offsets = np.concatenate([[0], np.cumsum(self.sizes)])
+        nstates, h0, C, df, temp = type_parameters(params, ids)
+        self._keep = [np.ascontiguousarray(np.array(shapes, dtype=np.int32)),
+                      np.ascontiguousarray(np.concatenate(ctype).astype(np.int32)), nstates, h0, C, df, temp,
+                      np.ascontiguousarray(np.concatenate(masses))]
+        h = ctypes.c_void_p()
+        st = L.mm_batch_create(len(self.systems), *(k.ctypes.data for k in self._keep[:2]), len(ids),
+                               *(k.ctypes.data for k in self._keep[2:]), {"original": 0, "nanocell": 1}[model],
+                               {"fp64": 0, "fp32": 1}[precision], ctypes.byref(h))
+        nat.check(st, "mm_batch_create")
+        self._h = h
+        self.masses = self._keep[-1]
+        self.set_state([s.pos for s in self.systems], None, [s.domain.rvecs for s in self.systems])
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None:
+            try:
+                self.L.mm_batch_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def __len__(self):
+        return len(self.systems)
+
+    # ------------------------------------------------------------ state
+    def set_state(self, pos, vel=None, rvecs=None):
+        pos = np.ascontiguousarray(np.concatenate([np.asarray(p, dtype=np.float64) for p in pos]))
+        v = None if vel is None else np.ascontiguousarray(np.concatenate([np.asarray(x, dtype=np.float64) for x in vel]))
+        if rvecs is None:
+            rvecs = self.get_state()[2]
+        rv = np.ascontiguousarray(np.array([np.asarray(r, dtype=np.float64).reshape(3, 3) for r in rvecs]))
+        nat.check(self.L.mm_batch_set_state(self._h, pos.ctypes.data, nat.ptr(v), rv.ctypes.data), "set_state")
+
+    def get_state(self):
+        N = int(self.offsets[-1])
+        pos = np.zeros((N, 3))
+        vel = np.zeros((N, 3))
+        rv = np.zeros((len(self), 3, 3))
+        nat.check(self.L.mm_batch_get_state(self._h, pos.ctypes.data, vel.ctypes.data, rv.ctypes.data), "get_state")
+        split = lambda a: [a[self.offsets[i]:self.offsets[i + 1]] for i in range(len(self))]
+        return split(pos), split(vel), list(rv)
+
+    def control(self):
+        c = np.zeros((len(self), CTL_LEN))
+        nat.check(self.L.mm_batch_control(self._h, c.ctypes.data, 0), "control")
+        return c
+
+    def set_control(self, c):
+        c = np.ascontiguousarray(c, dtype=np.float64)
+        nat.check(self.L.mm_batch_control(self._h, c.ctypes.data, 1), "control")
+
+    # ------------------------------------------------------------ hooks set-up
+    def setup_md(self, vel=None, temp=300.0, thermostat=None, timecon=100 * femtosecond, chainlength=3,
+                 chain_vel0=None, barostat=None, baro_timecon=1000 * femtosecond, vel_press0=None, ndof=None,
+                 seed=0, clean=True):
+        """Initial velocities and hook constants for every system (as the hooks' init does)."""
+        rng = np.random.default_rng(seed)
+        pos, _, rvecs = self.get_state()
+        vels = []
+        c = self.control()
+        for i, s in enumerate(self.systems):
+            m = np.asarray(s.masses)
+            if vel is None:
+                v = rng.normal(0.0, 1.0, (s.nnodes, 3)) * np.sqrt(boltzmann * temp / m)[:, None]
+            else:
+                v = np.array(vel[i], dtype=np.float64)
+            if clean and (thermostat is not None or barostat is not None):
+                v -= (m @ v) / m.sum()
+            vels.append(v)
+            n3 = 3 * s.nnodes
+            nd = ndof
+            if nd is None:
+                nd = n3 if (thermostat in (None, "langevin") and barostat is None) else n3 - 3
+            mtk_ndof = nd
+            if barostat == "mtk":
+                angfreq = 2 * np.pi / baro_timecon
+                c[i, CTL["mass_press"]] = (mtk_ndof + 9) * boltzmann * temp / angfreq**2
+                c[i, CTL["baro_ndof"]] = 6
+                vp = np.zeros((3, 3)) if vel_press0 is None else np.asarray(vel_press0[i] if np.ndim(vel_press0) == 3
+                                                                             else vel_press0)
+                c[i, CTL["vel_press"]] = vp.ravel()
+                if thermostat == "langevin" and ndof is None:
+                    nd = n3  # TBCombination: Langevin thermostat lets the centre of mass fluctuate
+            if thermostat == "nhc":
+                afreq = 2 * np.pi / timecon
+                cm = np.ones(3) * (boltzmann * temp / afreq**2)
+                cm[0] *= nd
+                c[i, CTL["chain_mass"]] = cm
+                cv = np.zeros(3) if chain_vel0 is None else np.asarray(chain_vel0[i] if np.ndim(chain_vel0) == 2
+                                                                        else chain_vel0)
+                c[i, CTL["chain_vel"]] = cv
+                c[i, CTL["chain_pos"]] = 0.0
+            c[i, CTL["ndof"]] = nd
+            c[i, CTL["econs_thermo"]] = 0.0
+            c[i, CTL["econs_baro"]] = 0.0
+        self.set_state(pos, vels, rvecs)
+        # set_state rewrote the lattice part; merge the hook constants back in
+        c2 = self.control()
+        keep = [CTL["L"], CTL["rvecs"], CTL["volume"]]
+        for sl in keep:
+            c[:, sl] = c2[:, sl]
+        self.set_control(c)
+        self.hooks = dict(thermostat=thermostat, barostat=barostat, temp=temp, timecon=timecon, chain=chainlength)
+
+    # ------------------------------------------------------------ kernels
+    def md(self, nsteps, timestep=1.0 * femtosecond, thermostat=None, temp=300.0, timecon=100 * femtosecond,
+           barostat=None, press=0.0, chainlength=3, seed=1, step0=0, noise=None, record=False, use_graph=True):
+        torch = self.torch
+        dev = torch.device("cuda", torch.cuda.current_device())
+        rec = None
+        if record:
+            rec = torch.zeros((len(self), nsteps, REC_LEN), dtype=torch.float64, device=dev)
+        nz = None
+        if noise is not None:
+            nz = torch.from_numpy(np.ascontiguousarray(noise, dtype=np.float64)).to(dev)
+        st = self.L.mm_batch_md(self._h, int(nsteps), float(timestep), _THERMO[thermostat], float(temp),
+                                float(timecon), 1 if barostat == "mtk" else 0, float(press), int(chainlength),
+                                int(seed), int(step0), nat.ptr(nz), nat.ptr(rec), int(bool(use_graph)),
+                                torch.cuda.current_stream().cuda_stream)
+        nat.check(st, "mm_batch_md")
+        if record:
+            return rec.cpu().numpy()
+        return None
+
+    def relax(self, max_iter=2000, gtol=1e-6):
+        """CG relaxation of node positions; returns (largest gradient norm, iterations) per system."""
+        torch = self.torch
+        nat.check(self.L.mm_batch_relax(self._h, int(max_iter), float(gtol), torch.cuda.current_stream().cuda_stream),
+                  "mm_batch_relax")
+        c = self.control()
+        return c[:, CTL["gmax"]], c[:, CTL["iters"]]
+
+    def autotune(self, probe_steps=5, timestep=1.0 * femtosecond, thermostat=None, temp=300.0,
+                 timecon=100 * femtosecond, barostat=None, press=0.0, chainlength=3):
+        best = ctypes.c_double()
+        nat.check(self.L.mm_batch_autotune(self._h, int(probe_steps), float(timestep), _THERMO[thermostat], float(temp),
+                                           float(timecon), 1 if barostat == "mtk" else 0, float(press),
+                                           int(chainlength), ctypes.byref(best)), "mm_batch_autotune")
+        bt, nc = ctypes.c_int(), ctypes.c_int()
+        nat.check(self.L.mm_batch_config(self._h, ctypes.byref(bt), ctypes.byref(nc)), "mm_batch_config")
+        return {"cta_threads": bt.value, "ctas": nc.value, "probe_ms": best.value}
+
+    # ------------------------------------------------------------ observables
+    def energies(self):
+        return self.control()[:, CTL["epot"]]
+
+    def stress(self):
+        """Static stress -vtens / V per system (3x3), from the last force evaluation."""
+        c = self.control()
+        return np.array([-c[i, CTL["vtens"]].reshape(3, 3) / c[i, CTL["volume"]] for i in range(len(self))])

@@ -287,73 +287,8 @@ __global__ void __launch_bounds__(kCell8Threads) k_cells8(Topo t, const TypeTabl
     for (int x = 0; x < 3; ++x) du[x] = disp[x * t.N + node];
     ty = t.cell_type[cell];
   }
-  // edge (vertex a -> neighbour a^(1<<d)) displacement differences, oriented lo -> hi
-  T ed[3][3];
-#pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    const bool hi = (a >> d) & 1;
-#pragma unroll
-    for (int x = 0; x < 3; ++x) {
-      const T other = __shfl_xor_sync(0xffffffffu, du[x], 1 << d);
-      ed[d][x] = hi ? du[x] - other : other - du[x];
-    }
-  }
-  const TypeParams<T>& tpl = tp[ty];
-  const int ns_lane = valid ? tpl.nstates : 1;
-  const int ns = __reduce_max_sync(0xffffffffu, ns_lane);
-  T g[3] = {T(0), T(0), T(0)};
-  T m = T(0), wsum = T(0);
-  const T kT = tpl.kT;
-  for (int s = 0; s < ns; ++s) {
-    const bool active = s < ns_lane;
-    const StateParams<T>& p = tpl.s[active ? s : 0];
-    T W[9], GW[9];
-#pragma unroll
-    for (int d = 0; d < 3; ++d)
-#pragma unroll
-      for (int x = 0; x < 3; ++x) W[d * 3 + x] = p.B[d * 3 + x] + ed[d][x];
-    T Es = state_energy_grad<T>(W, p, T(0.125) * p.v0, GW);
-    Es += __shfl_xor_sync(0xffffffffu, Es, 1);
-    Es += __shfl_xor_sync(0xffffffffu, Es, 2);
-    Es += __shfl_xor_sync(0xffffffffu, Es, 4);
-    T gs[3] = {T(0), T(0), T(0)};
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const T sg = ((a >> d) & 1) ? T(1) : T(-1);
-#pragma unroll
-      for (int x = 0; x < 3; ++x) {
-        const T mine = GW[d * 3 + x];
-        gs[x] += sg * (mine + __shfl_xor_sync(0xffffffffu, mine, 1 << d));
-      }
-    }
-    if (active) {
-      const T E = Es + p.df;
-      if (s == 0) {
-        m = E;
-        wsum = T(1);
-#pragma unroll
-        for (int x = 0; x < 3; ++x) g[x] = gs[x];
-      } else if (E < m) {
-        const T r = exp((E - m) / kT);
-        wsum = wsum * r + T(1);
-#pragma unroll
-        for (int x = 0; x < 3; ++x) g[x] = g[x] * r + gs[x];
-        m = E;
-      } else {
-        const T w = exp((m - E) / kT);
-        wsum += w;
-#pragma unroll
-        for (int x = 0; x < 3; ++x) g[x] += w * gs[x];
-      }
-    }
-  }
-  T Ecell = m;
-  if (ns_lane > 1) {
-    const T inv = T(1) / wsum;
-#pragma unroll
-    for (int x = 0; x < 3; ++x) g[x] *= inv;
-    Ecell = m - kT * log(wsum);
-  }
+  T g[3];
+  const T Ecell = cell8_eval<T>(du, a, tp[ty], valid, g);
   // stage corner gradients: tile[(corner*3 + x)][cl]
   const int corner = bits_to_corner(a);
 #pragma unroll

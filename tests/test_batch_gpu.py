@@ -1,0 +1,150 @@
+"""Batched persistent kernel: reference trajectories, relaxation, precision, autotuning, graphs."""
+import numpy as np
+import pytest
+
+from conftest import load_golden, make_system, system_dict
+
+pytestmark = pytest.mark.gpu
+
+
+def _golden_batch(name, copies=1, precision="fp64"):
+    from micmec_gb300.batch import BatchSystems
+
+    g = load_golden(name)
+    systems = [make_system(system_dict(g, "sys/")) for _ in range(copies)]
+    return g, BatchSystems(systems, model=str(g["model"]), precision=precision)
+
+
+def _check(g, rec, n, rtol):
+    from micmec_gb300.batch import REC
+
+    ref = g["records"][1: n + 1]
+    econs = rec[:, REC["epot"]] + rec[:, REC["ekin"]] + rec[:, REC["ecorr"]]
+    for got, col in ((rec[:, REC["epot"]], 1), (rec[:, REC["ekin"]], 2), (econs, 3)):
+        assert np.abs(got - ref[:, col]).max() <= rtol * np.abs(ref[:, col]).max(), col
+    vt = rec[:, REC["vtens"]]
+    assert np.abs(vt - ref[:, 6:15]).max() <= rtol * np.abs(ref[:, 6:15]).max()
+    vol = rec[:, REC["volume"]]
+    assert np.abs(vol - ref[:, -1]).max() <= rtol * ref[:, -1].max()
+
+
+def test_batch_nve_matches_reference_in_every_copy():
+    g, b = _golden_batch("md_nve_nanocell", copies=3)
+    b.setup_md(vel=[g["vel0"]] * 3, thermostat=None)
+    rec = b.md(1000, timestep=float(g["timestep"]), record=True, use_graph=False)
+    for i in range(3):
+        _check(g, rec[i], 1000, 1e-8)
+    pos, vel, _ = b.get_state()
+    assert np.abs(pos[1] - g["pos_1000"]).max() < 1e-6
+
+
+def test_batch_langevin_replay_matches_reference():
+    g, b = _golden_batch("md_langevin_nanocell")
+    b.setup_md(vel=[g["vel0"]], thermostat="langevin", temp=float(g["meta/temp"]))
+    noise = g["noise"].reshape(200, 2, -1, 3)
+    rec = b.md(200, timestep=float(g["timestep"]), thermostat="langevin", temp=float(g["meta/temp"]),
+               timecon=float(g["meta/timecon"]), noise=noise, record=True)
+    _check(g, rec[0], 200, 1e-8)
+
+
+def test_batch_nhc_matches_reference():
+    g, b = _golden_batch("md_nhc_nanocell")
+    T, tau = float(g["meta/temp"]), float(g["meta/timecon"])
+    b.setup_md(vel=[g["vel0"]], thermostat="nhc", temp=T, timecon=tau, chain_vel0=[g["meta/chain_vel0"]])
+    rec = b.md(200, timestep=float(g["timestep"]), thermostat="nhc", temp=T, timecon=tau, record=True)
+    _check(g, rec[0], 200, 1e-8)
+    from micmec_gb300.batch import CTL
+
+    assert np.allclose(b.control()[0, CTL["chain_pos"]], g["chain_pos_end"], rtol=1e-7, atol=1e-12)
+
+
+@pytest.mark.parametrize("name", ["md_mtk_nanocell", "md_nhc_mtk_nanocell", "md_langevin_mtk_nanocell"])
+def test_batch_mtk_matches_reference(name):
+    g, b = _golden_batch(name)
+    T, P = float(g["meta/temp"]), float(g["meta/press"])
+    n = len(g["records"]) - 1
+    if name == "md_mtk_nanocell":
+        thermo, tt, tb = None, 100.0, float(g["meta/timecon"])
+    else:
+        thermo = "nhc" if "nhc" in name else "langevin"
+        tt, tb = float(g["meta/timecon_thermo"]), float(g["meta/timecon_baro"])
+    chain0 = [g["meta/chain_vel0"]] if thermo == "nhc" else None
+    b.setup_md(vel=[g["vel0"]], thermostat=thermo, temp=T, timecon=tt, chain_vel0=chain0, barostat="mtk",
+               baro_timecon=tb, vel_press0=[g["meta/vel_press0"]])
+    noise = g["noise"].reshape(n, 2, -1, 3) if thermo == "langevin" else None
+    rec = b.md(n, timestep=float(g["timestep"]), thermostat=thermo, temp=T, timecon=tt, barostat="mtk", press=P,
+               noise=noise, record=True)
+    _check(g, rec[0], n, 1e-7)
+    _, _, rv = b.get_state()
+    assert np.allclose(rv[0], g["rvecs_end"], rtol=1e-9)
+
+
+def _mixed_batch(ns, precision, seed=0, sigma=0.1, strains=None):
+    from micmec_gb300 import lattices, units
+    from micmec_gb300.batch import BatchSystems
+    from micmec_gb300.system import System
+
+    rng = np.random.default_rng(seed)
+    systems = []
+    for i, n in enumerate(ns):
+        d = lattices.make_lattice(lattices.defect_grid(n, 0.2, rng), nstates=2)
+        if strains is not None:
+            F = np.eye(3)
+            F[0, 0] += strains[i]
+            d["pos"] = d["pos"] @ F
+            d["rvecs"] = d["rvecs"] @ F
+        d["pos"] = lattices.displace(d["pos"], sigma * units.angstrom, rng)
+        systems.append(System.from_dict(d))
+    return systems, BatchSystems(systems, model="nanocell", precision=precision)
+
+
+def test_batch_relax_reaches_tolerance_and_matches_single_system_forces():
+    from micmec_gb300.pes.mmff import ForcePartMechanical, MicMecForceField
+
+    systems, b = _mixed_batch([3, 4, 5, 6], "fp64", strains=[0.0, 0.01, 0.02, 0.03])
+    e0 = [MicMecForceField(s, [ForcePartMechanical(s)]).compute() for s in systems]
+    gmax, iters = b.relax(max_iter=3000, gtol=1e-7)
+    assert (gmax < 1e-7).all(), (gmax, iters)
+    pos, _, rv = b.get_state()
+    e_batch = b.energies()
+    for i, s in enumerate(systems):
+        s.pos[:] = pos[i]
+        ff = MicMecForceField(s, [ForcePartMechanical(s)])
+        gp = np.zeros((s.nnodes, 3))
+        e = ff.compute(gp)
+        assert e < e0[i]
+        assert abs(e - e_batch[i]) <= 1e-10 * abs(e)
+        assert np.sqrt((gp**2).sum(axis=1)).max() < 1e-7
+
+
+def test_batch_fp32_tracks_fp64_with_replayed_noise():
+    from micmec_gb300.batch import REC
+
+    recs = {}
+    ns = [3, 5, 7, 4]
+    for prec in ("fp64", "fp32"):
+        systems, b = _mixed_batch(ns, prec, seed=3)
+        N = int(b.offsets[-1])
+        noise = np.random.default_rng(5).normal(size=(50, 2, N, 3))
+        b.setup_md(temp=300.0, thermostat="langevin", seed=11)
+        recs[prec] = b.md(50, thermostat="langevin", temp=300.0, noise=noise, record=True)
+    a, f = recs["fp64"], recs["fp32"]
+    for i in range(len(ns)):
+        for col in (REC["epot"], REC["ekin"]):
+            assert np.abs(a[i, :, col] - f[i, :, col]).max() <= 1e-5 * np.abs(a[i, :, col]).max()
+
+
+def test_autotune_and_graph_replay_keep_results():
+    from micmec_gb300.batch import REC
+
+    systems, b = _mixed_batch([3, 6, 4, 8, 5, 3, 7], "fp32", seed=4)
+    b.setup_md(temp=300.0, thermostat=None, seed=2)
+    pos0, vel0, rv0 = b.get_state()
+    ref = b.md(20, record=True, use_graph=False)
+    cfg = b.autotune(probe_steps=3)
+    assert cfg["cta_threads"] in (128, 256) and cfg["ctas"] >= 1
+    for use_graph in (True, True, False):
+        b.set_state(pos0, vel0, rv0)
+        got = b.md(20, record=True, use_graph=use_graph)
+        for col in (REC["epot"], REC["ekin"]):
+            assert np.abs(got[:, :, col] - ref[:, :, col]).max() <= 1e-6 * np.abs(ref[:, :, col]).max()
