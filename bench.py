@@ -223,6 +223,159 @@ def run_reference(args):
 # ---------------------------------------------------------------- GPU arm
 
 
+def measure_fp64_lattice(s, vel, nsteps, flush):
+    """The plain FP64 GPU path on the same lattice: same session API, FP64 cells."""
+    import torch
+
+    from micmec_gb300 import _native as nat, units
+    from micmec_gb300.pes.mmff import ForcePartMechanical
+
+    L = nat.lib()
+    dev = flush.device
+    fp = ForcePartMechanical(s, model="nanocell", precision="fp64")
+    stream = torch.cuda.current_stream().cuda_stream
+    pos_d = torch.from_numpy(np.ascontiguousarray(s.pos)).to(dev)
+    vel_d = torch.from_numpy(np.ascontiguousarray(vel)).to(dev)
+    dt, tau = 1.0 * units.femtosecond, 100.0 * units.femtosecond
+    nat.check(L.mm_md_begin(fp.handle, pos_d.data_ptr(), vel_d.data_ptr(), dt, 1, 300.0, tau, SEED, None, 0, stream),
+              "mm_md_begin")
+    for _ in range(3):
+        nat.check(L.mm_md_advance(fp.handle, 1, None, 0, stream), "mm_md_advance")
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nsteps)]
+    for i in range(nsteps):
+        flush.fill_(i & 0xFF)
+        ev[i][0].record()
+        nat.check(L.mm_md_advance(fp.handle, 1, None, 0, stream), "mm_md_advance")
+        ev[i][1].record()
+    torch.cuda.synchronize()
+    ms = float(sum(a.elapsed_time(b) for a, b in ev))
+    nat.check(L.mm_md_advance(fp.handle, 1, None, 1, stream), "mm_md_advance")
+    torch.cuda.synchronize()
+    return s.ncells * nsteps / (ms * 1e-3), ms / nsteps
+
+
+def batch_workload(nsys=512, seed=77, nstates=2):
+    """512 periodic systems, n ~ U{3..12}, defect fraction ~ U[0, 0.3], uniaxial strain 0..5% in 0.25% steps."""
+    from micmec_gb300 import lattices, units
+    from micmec_gb300.system import System
+
+    rng = np.random.default_rng(seed)
+    systems, strains = [], []
+    for i in range(nsys):
+        n = int(rng.integers(3, 13))
+        frac = float(rng.uniform(0.0, 0.3))
+        strain = 0.0025 * (i % 21)
+        d = lattices.make_lattice(lattices.defect_grid(n, frac, rng), nstates=nstates)
+        F = np.eye(3)
+        F[0, 0] += strain
+        d["pos"] = d["pos"] @ F
+        d["rvecs"] = d["rvecs"] @ F
+        d["pos"] = lattices.displace(d["pos"], 0.02 * units.angstrom, rng)
+        systems.append(System.from_dict(d))
+        strains.append(strain)
+    return systems, np.array(strains)
+
+
+def measure_batch(systems, strains, precision, md_steps, relax_iters):
+    import torch
+
+    from micmec_gb300 import units
+    from micmec_gb300.batch import BatchSystems
+
+    fs = units.femtosecond
+    b = BatchSystems(systems, model="nanocell", precision=precision)
+    gtol = 1e-4 * units.electronvolt / units.angstrom
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    gmax, iters = b.relax(max_iter=relax_iters, gtol=gtol)
+    torch.cuda.synchronize()
+    t_relax = time.perf_counter() - t0
+    stress = b.stress()[:, 0, 0] / units.gigapascal
+    b.setup_md(temp=300.0, thermostat="nhc", barostat="mtk", timecon=100 * fs, baro_timecon=1000 * fs, seed=5)
+    cfg = b.autotune(probe_steps=3, thermostat="nhc", temp=300.0, barostat="mtk", press=0.0)
+    b.md(1, thermostat="nhc", temp=300.0, barostat="mtk", press=0.0, use_graph=True)  # capture
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    b.md(md_steps, thermostat="nhc", temp=300.0, barostat="mtk", press=0.0, use_graph=True, step0=1)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    cells = float(np.sum(b.sizes))
+    return {
+        "systems": len(systems), "cells": int(cells), "precision": precision, "md_steps": md_steps,
+        "md_ms": ms, "systems_steps_per_s": len(systems) * md_steps / (ms * 1e-3),
+        "cell_steps_per_s": cells * md_steps / (ms * 1e-3),
+        "force_evals_per_step": 3, "relax_s": t_relax, "relax_converged": int(np.sum(gmax < gtol)),
+        "relax_max_iters": int(np.max(iters)), "autotune": cfg,
+        "stress_xx_gpa_by_strain": {f"{s:.4f}": float(np.mean(stress[np.isclose(strains, s)])) for s in
+                                     np.unique(strains)[:: 5]},
+    }
+
+
+def measure_plain_per_system(systems, nsteps):
+    """The plain FP64 GPU path for the same hooks: one System at a time through VerletIntegrator
+    (MTK barostat + NHC thermostat on the host, every force evaluation on the GPU)."""
+    import torch
+
+    from micmec_gb300 import units
+    from micmec_gb300.pes.mmff import ForcePartMechanical, MicMecForceField
+    from micmec_gb300.sampling.npt import MTKBarostat
+    from micmec_gb300.sampling.nvt import NHCThermostat
+    from micmec_gb300.sampling.verlet import VerletIntegrator
+
+    fs = units.femtosecond
+    t = 0.0
+    steps = 0
+    for s in systems:
+        ff = MicMecForceField(s, [ForcePartMechanical(s, model="nanocell", precision="fp64")])
+        hooks = [NHCThermostat(300.0, timecon=100 * fs), MTKBarostat(ff, 300.0, 0.0, timecon=1000 * fs)]
+        vi = VerletIntegrator(ff, 1.0 * fs, hooks=hooks, temp0=300.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        vi.run(nsteps)
+        torch.cuda.synchronize()
+        t += time.perf_counter() - t0
+        steps += nsteps
+    return {"systems": len(systems), "steps_each": nsteps, "systems_steps_per_s": steps / t,
+            "cell_steps_per_s": sum(s.ncells for s in systems) * nsteps / t}
+
+
+def measure_grad_over_fwd(n=16, reps=5):
+    """Cost of the adjoint (backward of a force loss) relative to the forward force evaluation, 16^3 FP64."""
+    import torch
+
+    from micmec_gb300 import lattices, units
+    from micmec_gb300.autograd import MicMecParameters, energy_and_gradient
+    from micmec_gb300.pes.mmff import ForcePartMechanical
+    from micmec_gb300.system import System
+
+    rng = np.random.default_rng(3)
+    d = lattices.make_lattice(lattices.defect_grid(n, 0.2, rng), nstates=2)
+    d["pos"] = lattices.displace(d["pos"], 0.05 * units.angstrom, rng)
+    s = System.from_dict(d)
+    part = ForcePartMechanical(s, model="nanocell", precision="fp64")
+    params = MicMecParameters(part)
+    pos = torch.tensor(s.pos, dtype=torch.float64, device="cuda")
+    w = torch.tensor(rng.normal(size=(s.nnodes, 3)), dtype=torch.float64, device="cuda")
+    fwd, bwd = [], []
+    for _ in range(reps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        E, g = energy_and_gradient(pos, params)
+        loss = (w * g).sum()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        torch.autograd.grad(loss, [params.c21, params.h0, params.free_energy])
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        fwd.append(t1 - t0)
+        bwd.append(t2 - t1)
+    f, b = float(np.median(fwd[1:])), float(np.median(bwd[1:]))
+    return {"lattice": [n] * 3, "forward_ms": 1e3 * f, "backward_ms": 1e3 * b, "grad_over_fwd": b / f}
+
+
 def run_gpu(args):
     import torch
 
@@ -341,6 +494,21 @@ def run_gpu(args):
         "gpu_launches": 2 * args.steps,
         "clocks": clk,
     }
+    if rank == 0 and not args.no_extra:
+        try:
+            v64, ms64 = measure_fp64_lattice(s, vel, max(5, min(args.steps, 30)), flush)
+            line["fp64_lattice"] = {"value": v64, "unit": UNIT, "ms_per_step": ms64,
+                                    "fp32_over_fp64": value / world / v64}
+            systems, strains = batch_workload()
+            bf = measure_batch(systems, strains, "fp32", 200, 400)
+            bd = measure_batch(systems, strains, "fp64", 20, 100)
+            plain = measure_plain_per_system(systems[:6], 10)
+            line["batched"] = {"fp32": bf, "fp64": bd, "plain_fp64_per_system": plain,
+                               "batched_fp32_over_plain_fp64_systems_per_s":
+                                   bf["systems_steps_per_s"] / plain["systems_steps_per_s"]}
+            line["adjoint"] = measure_grad_over_fwd()
+        except Exception as exc:  # extra measurements never block the main line
+            line["extra_error"] = repr(exc)[:300]
     if rank == 0 and not args.no_cpu_baseline:
         nproc = 1
         sample_steps = 1
@@ -361,6 +529,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the FP64 / batched / adjoint side measurements")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -246,6 +246,31 @@ mm_status mm_batch_autotune(mm_batch* b, int probe_steps, double timestep, int t
                             int baro, double press, int chain, double* best_ms);
 mm_status mm_batch_config(mm_batch* b, int* cta_threads, int* nctas);
 
+/*
+ * Replace the parameters of a handle (same layout as mm_create): used by
+ * differentiable parameter fits. No reference counterpart (the reference builds a
+ * new ForcePartMechanical for new parameters, mmff.py:207-245).
+ */
+mm_status mm_set_params(mm_handle* h, const double* h0, const double* C, const double* free_energy,
+                        const double* temp_eff);
+
+/*
+ * Adjoint evaluation in FP64 (forward-mode tangent along a node displacement field
+ * lam and a lattice-matrix tangent dlattice, on top of the energy, gradient and
+ * parameter gradient). Derivatives of the reference's energy model
+ * (micmec/pes/nanocell.py:40-132, nanocell_original.py:46-132, mmff.py:377-398).
+ *  pos (N,3) device; lam (N,3) device or NULL (zero); dlattice (3,3) host or NULL.
+ *  energy  device double[2] : E, dE/dt along (lam, dlattice).
+ *  gpos    device (N,3) or NULL : dE/dx.
+ *  hvp     device (N,3) or NULL : d(dE/dx)/dt = H lam (+ lattice coupling).
+ *  vtens   device double[18] or NULL : virial and its tangent.
+ *  pgrad   device double[ntypes*4*46*2] or NULL : per (type, state) slot, 46 values
+ *          [dE/dA (36, the 6x6 stress map of mm_create), dE/dh0 (9), dE/d(free energy)],
+ *          each as (value, tangent): the tangent is d/dtheta (lam . dE/dx).
+ */
+mm_status mm_adjoint(mm_handle* h, const double* pos, const double* lam, const double* dlattice, double* energy,
+                     double* gpos, double* hvp, double* vtens, double* pgrad, void* stream);
+
 /* Last CUDA error string of the calling thread's last failing call. */
 const char* mm_last_error(void);
 

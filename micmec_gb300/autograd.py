@@ -1,0 +1,188 @@
+"""Differentiation: gradients with respect to the model parameters, through forces and trajectories.
+
+``MicMecParameters`` holds differentiable per-(type, state) parameters as torch
+tensors: the 21 independent Voigt components of each elasticity tensor, the 3x3
+rest matrix h0 and the state free energy. ``energy_and_gradient(pos, params)`` is
+a ``torch.autograd.Function``: forward runs the GPU force evaluation, backward runs
+the hand-written FP64 adjoint kernel (``mm_adjoint``) once, with the incoming
+gradient of the forces as tangent direction. That gives, in one pass,
+dL/dpos = gE dE/dx + H lam and dL/dtheta = gE dE/dtheta + d/dtheta (lam . dE/dx),
+with lam = dL/d(dE/dx), so losses on energies, forces and trajectories built from
+them differentiate exactly (to FP64 rounding).
+
+``verlet_trajectory`` integrates velocity Verlet with torch operations on top of
+that Function, recomputing segments of ``checkpoint_every`` steps in the backward
+pass (torch.utils.checkpoint) instead of storing every step.
+
+Elasticity in Voigt notation C_v (6x6, symmetric, order 00,11,22,12,02,01, as
+micmec/analysis/tensor.py:96-149 with mode="elasticity"); the kernel's stress map is
+A = C_v diag(1,1,1,2,2,2).
+"""
+
+import numpy as np
+import torch
+
+from micmec_gb300 import _native as nat
+
+__all__ = ["MicMecParameters", "energy_and_gradient", "verlet_trajectory", "voigt21_to_tensor"]
+
+_IU = np.triu_indices(6)
+_VPAIRS = [(0, 0), (1, 1), (2, 2), (1, 2), (0, 2), (0, 1)]
+
+
+def _voigt_index():
+    idx = np.zeros((3, 3), dtype=np.int64)
+    for p, (i, j) in enumerate(_VPAIRS):
+        idx[i, j] = idx[j, i] = p
+    return idx
+
+
+_VIDX = _voigt_index()
+
+
+def voigt21_to_matrix(c21):
+    """(..., 21) upper-triangle Voigt components -> (..., 6, 6) symmetric matrix."""
+    shape = c21.shape[:-1]
+    m = torch.zeros(shape + (6, 6), dtype=c21.dtype, device=c21.device)
+    iu = torch.as_tensor(_IU[0]), torch.as_tensor(_IU[1])
+    m[..., iu[0], iu[1]] = c21
+    m[..., iu[1], iu[0]] = c21
+    return m
+
+
+def voigt21_to_tensor(c21):
+    """(..., 21) -> (..., 3, 3, 3, 3) elasticity tensor (voigt_inv, mode="elasticity")."""
+    m = voigt21_to_matrix(c21)
+    v = torch.as_tensor(_VIDX)
+    return m[..., v[:, :, None, None], v[None, None, :, :]]
+
+
+class MicMecParameters(object):
+    """Differentiable parameters of the cell types of one ``ForcePartMechanical``."""
+
+    def __init__(self, part):
+        from micmec_gb300.pes.mmff import type_parameters
+
+        self.part = part
+        nstates, h0, C, df, temp = type_parameters(part.system.params, part.type_ids)
+        self.nstates = nstates
+        self.temp = np.ascontiguousarray(temp)
+        T = len(part.type_ids)
+        c21 = np.zeros((T, 4, 21))
+        for t in range(T):
+            for s in range(nstates[t]):
+                Ct = C[4 * t + s].reshape(3, 3, 3, 3)
+                M = np.array([[Ct[_VPAIRS[p] + _VPAIRS[q]] for q in range(6)] for p in range(6)])
+                c21[t, s] = M[_IU]
+        self.c21 = torch.tensor(c21, dtype=torch.float64, requires_grad=True)
+        self.h0 = torch.tensor(h0.reshape(T, 4, 3, 3), dtype=torch.float64, requires_grad=True)
+        self.free_energy = torch.tensor(df.reshape(T, 4), dtype=torch.float64, requires_grad=True)
+
+    def tensors(self):
+        return self.c21, self.h0, self.free_energy
+
+    def upload(self, c21, h0, df):
+        """Push parameter values into the native handle (unused state slots repeat state 0)."""
+        T = c21.shape[0]
+        C = voigt21_to_tensor(c21.detach()).cpu().numpy().reshape(T * 4, 81).copy()
+        H = h0.detach().cpu().numpy().reshape(T * 4, 9).copy()
+        D = df.detach().cpu().numpy().reshape(T * 4).copy()
+        for t in range(T):
+            for s in range(self.nstates[t], 4):
+                C[4 * t + s] = C[4 * t]
+                H[4 * t + s] = H[4 * t]
+                D[4 * t + s] = D[4 * t]
+        C, H, D = (np.ascontiguousarray(a) for a in (C, H, D))
+        nat.check(nat.lib().mm_set_params(self.part.handle, H.ctypes.data, C.ctypes.data, D.ctypes.data,
+                                          self.temp.ctypes.data), "mm_set_params")
+
+
+def _adjoint(part, pos, lam):
+    dev = pos.device
+    N = pos.shape[0]
+    T = len(part.type_ids)
+    energy = torch.zeros(2, dtype=torch.float64, device=dev)
+    gpos = torch.zeros((N, 3), dtype=torch.float64, device=dev)
+    hvp = torch.zeros((N, 3), dtype=torch.float64, device=dev) if lam is not None else None
+    vt = torch.zeros(18, dtype=torch.float64, device=dev)
+    pg = torch.zeros((T, 4, 46, 2), dtype=torch.float64, device=dev)
+    st = nat.lib().mm_adjoint(part.handle, pos.contiguous().data_ptr(), nat.ptr(None if lam is None else lam.contiguous()),
+                              None, energy.data_ptr(), gpos.data_ptr(), nat.ptr(hvp), vt.data_ptr(), pg.data_ptr(),
+                              torch.cuda.current_stream().cuda_stream)
+    nat.check(st, "mm_adjoint")
+    return energy, gpos, hvp, pg
+
+
+class _EnergyGrad(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, pos, c21, h0, df, params):
+        params.upload(c21, h0, df)
+        energy, gpos, _, _ = _adjoint(params.part, pos.detach(), None)
+        ctx.params = params
+        ctx.save_for_backward(pos.detach(), c21.detach(), h0.detach(), df.detach())
+        return energy[0].clone(), gpos
+
+    @staticmethod
+    def backward(ctx, gE, gG):
+        pos, c21, h0, df = ctx.saved_tensors
+        params = ctx.params
+        params.upload(c21, h0, df)
+        lam = gG if gG is not None else torch.zeros_like(pos)
+        gE = gE if gE is not None else torch.zeros((), dtype=torch.float64, device=pos.device)
+        energy, gpos, hvp, pg = _adjoint(params.part, pos, lam)
+        grad_pos = gE * gpos + hvp
+        # dL/dtheta per slot: gE * value + tangent
+        slot = gE * pg[..., 0] + pg[..., 1]  # (T, 4, 46)
+        dA = slot[..., :36].reshape(slot.shape[:2] + (6, 6))
+        w = torch.tensor([1.0, 1.0, 1.0, 2.0, 2.0, 2.0], dtype=torch.float64, device=dA.device)
+        dCv = dA * w  # A = C_v diag(w)  ->  dL/dC_v[p, q] = dL/dA[p, q] w_q
+        iu = torch.as_tensor(_IU[0]), torch.as_tensor(_IU[1])
+        dC21 = dCv[..., iu[0], iu[1]] + torch.where(iu[0] != iu[1], dCv[..., iu[1], iu[0]], torch.zeros_like(dCv[..., iu[0], iu[1]]))
+        dh0 = slot[..., 36:45].reshape(slot.shape[:2] + (3, 3))
+        ddf = slot[..., 45]
+        mask = torch.zeros(slot.shape[:2], dtype=torch.float64, device=dA.device)
+        for t, n in enumerate(params.nstates):
+            mask[t, :n] = 1.0
+        return (grad_pos, (dC21 * mask[..., None]).to(c21.device), (dh0 * mask[..., None, None]).to(h0.device),
+                (ddf * mask).to(df.device), None)
+
+
+def energy_and_gradient(pos, params):
+    """(E, dE/dx) at device positions ``pos`` (N,3) for ``params`` (differentiable in both)."""
+    c21, h0, df = params.tensors()
+    return _EnergyGrad.apply(pos, c21, h0, df, params)
+
+
+def verlet_trajectory(pos0, vel0, masses, params, timestep, nsteps, checkpoint_every=20):
+    """Velocity-Verlet trajectory (micmec/sampling/verlet.py:140-166) as torch operations.
+
+    Returns the list of gradients dE/dx at every step (index 0 = initial positions) and
+    the final (pos, vel). Segments of ``checkpoint_every`` steps are recomputed in the
+    backward pass.
+    """
+    from torch.utils.checkpoint import checkpoint
+
+    inv_m = (1.0 / masses).reshape(-1, 1)
+    dt = float(timestep)
+
+    def segment(x, v, g, k):
+        grads = []
+        for _ in range(k):
+            v = v - 0.5 * dt * g * inv_m
+            x = x + dt * v
+            _, g = energy_and_gradient(x, params)
+            v = v - 0.5 * dt * g * inv_m
+            grads.append(g)
+        return (x, v, g) + tuple(grads)
+
+    _, g = energy_and_gradient(pos0, params)
+    x, v = pos0, vel0
+    out = [g]
+    done = 0
+    while done < nsteps:
+        k = min(checkpoint_every, nsteps - done)
+        res = checkpoint(segment, x, v, g, k, use_reentrant=False)
+        x, v, g = res[0], res[1], res[2]
+        out.extend(res[3:])
+        done += k
+    return out, x, v

@@ -513,7 +513,7 @@ __global__ void __launch_bounds__(BT) k_batch_md(BArgs a, BMD p) {
     double* c = sh.ctl;
     load_tables<T>(sh, a.tt, a.ntypes, c + C_L);
     __syncthreads();
-    const double kT = 3.1668154051341965e-06 * p.temp;  // boltzmann (Hartree / K) x T
+    const double kT = (1.3806505e-23 / 4.35974381e-18) * p.temp;  // boltzmann (Hartree / K) x T
     write_disp<T>(a, sy);
     __syncthreads();
     forces<T, MODEL>(a, sh, sy);
@@ -678,8 +678,8 @@ __global__ void __launch_bounds__(BT) k_batch_relax(BArgs a, int max_iter, doubl
           const double s1 = s1v[0], e1 = c[C_EPOT];
           double anew;
           int acc_flag = 0;
-          if (s0 - s1 > 0.0) {
-            anew = alpha * s0 / (s0 - s1);
+          if (s1 - s0 > 0.0) {  // phi'(alpha) grew from s0 < 0: secant root of phi'
+            anew = alpha * (-s0) / (s1 - s0);
             anew = fmin(fmax(anew, 0.05 * alpha), 20.0 * alpha);
             acc_flag = (e1 <= e0) ? 1 : 0;
           } else {

@@ -46,6 +46,8 @@ struct mm_handle {
   double* d_carry = nullptr;          // values carried between MD kernels
   double* d_io = nullptr;             // staging: pos (3N), gpos (3N), energy+vtens (10)
   int* d_flag = nullptr;              // NaN flag
+  double* d_adj = nullptr;            // adjoint scratch (allocated on first mm_adjoint call)
+  size_t adj_len = 0;
   // MD session
   struct {
     double dt = 0.0, c1 = 1.0, temp = 0.0, timecon = 0.0;

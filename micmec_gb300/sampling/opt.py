@@ -101,9 +101,9 @@ class CGOptimizer(BaseOptimizer):
             s1 = float(np.dot(g1, d))
             if f1 <= self.f + 1e-4 * alpha * s0 and (best is None or f1 < best[1]):
                 best = (x1, f1, g1, alpha)
-            denom = s0 - s1
-            if denom > 0:
-                a_new = alpha * s0 / denom
+            denom = s1 - s0
+            if denom > 0:  # the directional derivative grew: secant root of phi'
+                a_new = alpha * (-s0) / denom
                 if best is not None and abs(s1) <= 0.1 * abs(s0):
                     break
                 alpha = min(max(a_new, 0.1 * alpha), 10.0 * alpha)

@@ -1,0 +1,123 @@
+"""Adjoint kernel behind torch.autograd: parameter and position gradients of energy, force and
+trajectory losses, against an FP64 autograd reference and central finite differences."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(n=4, model="nanocell", seed=0):
+    import torch
+
+    from micmec_gb300 import lattices, units
+    from micmec_gb300.autograd import MicMecParameters
+    from micmec_gb300.pes.mmff import ForcePartMechanical
+    from micmec_gb300.system import System
+
+    rng = np.random.default_rng(seed)
+    d = lattices.make_lattice(lattices.defect_grid(n, 0.25, rng), nstates=2)
+    d["pos"] = lattices.displace(d["pos"], 0.1 * units.angstrom, rng)
+    s = System.from_dict(d)
+    part = ForcePartMechanical(s, model=model, precision="fp64")
+    params = MicMecParameters(part)
+    pos = torch.tensor(s.pos, dtype=torch.float64, device="cuda")
+    return s, part, params, pos, rng
+
+
+def _ref_energy(s, part, params, pos_t, c21, h0, df, model):
+    from oracle import torch_mmff
+
+    return torch_mmff.energy(pos_t, s.domain.rvecs, s.grid, s.surrounding_nodes, s.types, part.type_ids,
+                             params.nstates, c21, h0, df, params.temp, model=model)
+
+
+@pytest.mark.parametrize("model", ["nanocell", "original"])
+def test_force_loss_gradients_match_fp64_autograd_reference(model):
+    import torch
+
+    from micmec_gb300.autograd import energy_and_gradient
+
+    s, part, params, pos, rng = _setup(model=model)
+    w = torch.tensor(rng.normal(size=(s.nnodes, 3)), dtype=torch.float64, device="cuda")
+    pos.requires_grad_(True)
+    E, g = energy_and_gradient(pos, params)
+    loss = 1e3 * E + (w * g).sum() * 10.0
+    gp, gc, gh, gd = torch.autograd.grad(loss, [pos, params.c21, params.h0, params.free_energy])
+    # FP64 autograd reference on the CPU
+    c21 = params.c21.detach().clone().requires_grad_(True)
+    h0 = params.h0.detach().clone().requires_grad_(True)
+    df = params.free_energy.detach().clone().requires_grad_(True)
+    pt = torch.tensor(s.pos, dtype=torch.float64, requires_grad=True)
+    Er = _ref_energy(s, part, params, pt, c21, h0, df, model)
+    gr, = torch.autograd.grad(Er, pt, create_graph=True)
+    lr = 1e3 * Er + (w.cpu() * gr).sum() * 10.0
+    rp, rc, rh, rd = torch.autograd.grad(lr, [pt, c21, h0, df])
+    assert abs(E.item() - Er.item()) <= 1e-10 * abs(Er.item())
+    assert (g.detach().cpu() - gr.detach()).abs().max() <= 1e-10 * gr.abs().max()
+    for a, b in ((gp.cpu(), rp), (gc.cpu(), rc), (gh.cpu(), rh), (gd.cpu(), rd)):
+        assert (a - b).abs().max() <= 1e-8 * b.abs().max() + 1e-300, (a - b).abs().max()
+
+
+def test_force_loss_gradient_matches_central_differences():
+    import torch
+
+    from micmec_gb300.autograd import energy_and_gradient
+
+    s, part, params, pos, rng = _setup(n=3)
+    w = torch.tensor(rng.normal(size=(s.nnodes, 3)), dtype=torch.float64, device="cuda")
+
+    def loss():
+        E, g = energy_and_gradient(pos, params)
+        return (w * g).sum()
+
+    l0 = loss()
+    gc, gh, gd = torch.autograd.grad(l0, [params.c21, params.h0, params.free_energy])
+    checks = [(params.c21, gc, (0, 1, 0)), (params.c21, gc, (1, 0, 3)), (params.h0, gh, (0, 0, 0, 0)),
+              (params.h0, gh, (1, 1, 2, 1)), (params.free_energy, gd, (0, 1))]
+    for tensor, grad, idx in checks:
+        base = tensor.detach()[idx].item()
+        h = 1e-4 * max(abs(base), 1e-12)
+        vals = []
+        for sgn in (1, -1):
+            with torch.no_grad():
+                tensor[idx] = base + sgn * h
+            vals.append(loss().item())
+        with torch.no_grad():
+            tensor[idx] = base
+        fd = (vals[0] - vals[1]) / (2 * h)
+        assert abs(fd - grad[idx].item()) <= 1e-6 * max(abs(fd), 1e-3 * grad.abs().max().item()), (idx, fd, grad[idx])
+
+
+def test_trajectory_gradient_with_checkpointing():
+    import torch
+
+    from micmec_gb300 import units
+    from micmec_gb300.autograd import verlet_trajectory
+
+    s, part, params, pos, rng = _setup(n=3, seed=2)
+    masses = torch.tensor(s.masses, dtype=torch.float64, device="cuda")
+    vel = torch.tensor(rng.normal(size=(s.nnodes, 3)) * np.sqrt(units.boltzmann * 300.0 / s.masses)[:, None],
+                       dtype=torch.float64, device="cuda")
+    target = torch.tensor(rng.normal(size=(s.nnodes, 3)) * 1e-3, dtype=torch.float64, device="cuda")
+    dt = 1.0 * units.femtosecond
+
+    def loss():
+        grads, _, _ = verlet_trajectory(pos, vel, masses, params, dt, 12, checkpoint_every=5)
+        mean_force = -torch.stack(grads).mean(dim=0)
+        return ((mean_force - target) ** 2).mean()
+
+    l0 = loss()
+    gc, gh, gd = torch.autograd.grad(l0, [params.c21, params.h0, params.free_energy])
+    for tensor, grad, idx in ((params.c21, gc, (0, 0, 0)), (params.h0, gh, (0, 1, 1, 1)),
+                              (params.free_energy, gd, (1, 0))):
+        base = tensor.detach()[idx].item()
+        h = 1e-4 * max(abs(base), 1e-12)
+        vals = []
+        for sgn in (1, -1):
+            with torch.no_grad():
+                tensor[idx] = base + sgn * h
+            vals.append(loss().item())
+        with torch.no_grad():
+            tensor[idx] = base
+        fd = (vals[0] - vals[1]) / (2 * h)
+        assert abs(fd - grad[idx].item()) <= 1e-6 * max(abs(fd), 1e-3 * grad.abs().max().item()), (idx, fd, grad[idx])

@@ -70,3 +70,29 @@ def test_virial_is_homogeneous_strain_derivative():
                 es.append(om.compute(p, "nanocell")[0])
             fd[k, l] = (es[0] - es[1]) / (2 * h)
     assert np.abs(fd - vtens).max() <= 1e-6 * np.abs(vtens).max()
+
+
+def test_torch_oracle_matches_numpy_oracle():
+    torch = pytest.importorskip("torch")
+    from oracle import torch_mmff
+    from micmec_gb300.pes.mmff import type_parameters
+
+    sysd = system_dict(G, "synth_4x4x4_2types_2states/sys/")
+    ids = sorted(set(int(t) for t in sysd["types"]))
+    nstates, h0, C, df, temp = type_parameters(sysd["params"], ids)
+    iu = np.triu_indices(6)
+    pairs = [(0, 0), (1, 1), (2, 2), (1, 2), (0, 2), (0, 1)]
+    c21 = np.zeros((len(ids), 4, 21))
+    for t in range(len(ids)):
+        for s in range(nstates[t]):
+            Ct = C[4 * t + s].reshape(3, 3, 3, 3)
+            c21[t, s] = np.array([[Ct[pairs[p] + pairs[q]] for q in range(6)] for p in range(6)])[iu]
+    pos = torch.tensor(sysd["pos"], requires_grad=True)
+    for model in ("nanocell", "original"):
+        E = torch_mmff.energy(pos, sysd["rvecs"], sysd["grid"], sysd["surrounding_nodes"], sysd["types"], ids,
+                              nstates, torch.tensor(c21), torch.tensor(h0.reshape(-1, 4, 3, 3)),
+                              torch.tensor(df.reshape(-1, 4)), temp, model=model)
+        g, = torch.autograd.grad(E, pos)
+        e_ref, g_ref, _ = om.compute(sysd, model)
+        assert abs(E.item() - e_ref) <= 1e-12 * abs(e_ref)
+        assert np.abs(g.numpy() - g_ref).max() <= 1e-11 * np.abs(g_ref).max()
