@@ -131,16 +131,17 @@ class _EnergyGrad(torch.autograd.Function):
         gE = gE if gE is not None else torch.zeros((), dtype=torch.float64, device=pos.device)
         energy, gpos, hvp, pg = _adjoint(params.part, pos, lam)
         grad_pos = gE * gpos + hvp
-        # dL/dtheta per slot: gE * value + tangent
-        slot = gE * pg[..., 0] + pg[..., 1]  # (T, 4, 46)
+        # dL/dtheta per slot: gE * value + tangent (small: on the host)
+        pg = pg.cpu()
+        slot = float(gE) * pg[..., 0] + pg[..., 1]  # (T, 4, 46)
         dA = slot[..., :36].reshape(slot.shape[:2] + (6, 6))
-        w = torch.tensor([1.0, 1.0, 1.0, 2.0, 2.0, 2.0], dtype=torch.float64, device=dA.device)
+        w = torch.tensor([1.0, 1.0, 1.0, 2.0, 2.0, 2.0], dtype=torch.float64)
         dCv = dA * w  # A = C_v diag(w)  ->  dL/dC_v[p, q] = dL/dA[p, q] w_q
-        iu = torch.as_tensor(_IU[0]), torch.as_tensor(_IU[1])
-        dC21 = dCv[..., iu[0], iu[1]] + torch.where(iu[0] != iu[1], dCv[..., iu[1], iu[0]], torch.zeros_like(dCv[..., iu[0], iu[1]]))
+        i0, i1 = torch.as_tensor(_IU[0]), torch.as_tensor(_IU[1])
+        dC21 = dCv[..., i0, i1] + torch.where(i0 != i1, dCv[..., i1, i0], torch.zeros_like(dCv[..., i0, i1]))
         dh0 = slot[..., 36:45].reshape(slot.shape[:2] + (3, 3))
         ddf = slot[..., 45]
-        mask = torch.zeros(slot.shape[:2], dtype=torch.float64, device=dA.device)
+        mask = torch.zeros(slot.shape[:2], dtype=torch.float64)
         for t, n in enumerate(params.nstates):
             mask[t, :n] = 1.0
         return (grad_pos, (dC21 * mask[..., None]).to(c21.device), (dh0 * mask[..., None, None]).to(h0.device),
