@@ -242,6 +242,7 @@ class BatchSystems(object):
         return self.control()[:, CTL["epot"]]
 
     def stress(self):
-        """Static stress -vtens / V per system (3x3), from the last force evaluation."""
+        """Static stress vtens / V per system (3x3), from the last force evaluation
+        (the convention of the reference's stress-strain script, simulations/stress_strain.py:88-90)."""
         c = self.control()
-        return np.array([-c[i, CTL["vtens"]].reshape(3, 3) / c[i, CTL["volume"]] for i in range(len(self))])
+        return np.array([c[i, CTL["vtens"]].reshape(3, 3) / c[i, CTL["volume"]] for i in range(len(self))])

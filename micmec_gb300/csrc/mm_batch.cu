@@ -657,10 +657,15 @@ __global__ void __launch_bounds__(BT) k_batch_relax(BArgs a, int max_iter, doubl
           a.cgg[g] = a.gpos[g];
         }
       __syncthreads();
-      // secant line search: trial step alpha, then the secant minimiser along d
+      // line search on phi'(alpha) = g(x + alpha d) . d (gradient-based, so that it also
+      // works when energy differences are below the cell precision's resolution):
+      // bracketed (phi' >= 0) -> secant root; enough slope decrease -> accept; still
+      // steep -> extrapolate; energy above e0 + noise -> backtrack.
+      const double noise = (sizeof(T) == 4 ? 1e-6 : 1e-12) * fabs(e0);
       double alpha = c[C_ALPHA];
       bool accepted = false;
-      for (int ls = 0; ls < 12 && !accepted; ++ls) {
+      __shared__ int s_mode;
+      for (int ls = 0; ls < 16 && !accepted; ++ls) {
         for (int n = threadIdx.x; n < sy.M; n += blockDim.x)
           for (int x = 0; x < 3; ++x) {
             const long long g = x * N3 + sy.off + n;
@@ -676,23 +681,26 @@ __global__ void __launch_bounds__(BT) k_batch_relax(BArgs a, int max_iter, doubl
         block_sum<1>(s1v, sh.red);
         if (threadIdx.x == 0) {
           const double s1 = s1v[0], e1 = c[C_EPOT];
-          double anew;
-          int acc_flag = 0;
-          if (s1 - s0 > 0.0) {  // phi'(alpha) grew from s0 < 0: secant root of phi'
-            anew = alpha * (-s0) / (s1 - s0);
-            anew = fmin(fmax(anew, 0.05 * alpha), 20.0 * alpha);
-            acc_flag = (e1 <= e0) ? 1 : 0;
+          int mode = 0;
+          double anew = alpha;
+          if (e1 > e0 + noise && s1 < 0.0) {
+            anew = 0.25 * alpha;
+          } else if (s1 >= 0.0) {
+            anew = alpha * (-s0) / (s1 - s0);  // root of the secant through (0, s0), (alpha, s1)
+            mode = 2;
+          } else if (fabs(s1) <= 0.5 * fabs(s0)) {
+            mode = 1;
           } else {
-            anew = (e1 > e0) ? 0.25 * alpha : 4.0 * alpha;
-            acc_flag = 0;
+            anew = (s1 > s0) ? fmin(alpha * (-s0) / (s1 - s0), 8.0 * alpha) : 4.0 * alpha;
           }
           s_alpha = anew;
-          sh.scal[2] = acc_flag;
-          sh.scal[3] = e1;
+          s_mode = mode;
         }
         __syncthreads();
-        if (sh.scal[2] != 0.0) {
-          // move to the secant point
+        if (s_mode == 1) {
+          accepted = true;
+          if (threadIdx.x == 0) c[C_ALPHA] = alpha;
+        } else if (s_mode == 2) {
           const double as = s_alpha;
           for (int n = threadIdx.x; n < sy.M; n += blockDim.x)
             for (int x = 0; x < 3; ++x) {
@@ -703,23 +711,8 @@ __global__ void __launch_bounds__(BT) k_batch_relax(BArgs a, int max_iter, doubl
           write_disp<T>(a, sy);
           __syncthreads();
           forces<T, MODEL>(a, sh, sy);
-          if (c[C_EPOT] <= e0) {
-            accepted = true;
-            if (threadIdx.x == 0) c[C_ALPHA] = as;
-          } else {  // secant point worse: keep the trial point if it improved
-            for (int n = threadIdx.x; n < sy.M; n += blockDim.x)
-              for (int x = 0; x < 3; ++x) {
-                const long long g = x * N3 + sy.off + n;
-                a.u[g] = a.cgu[g] + alpha * a.cgd[g];
-              }
-            __syncthreads();
-            write_disp<T>(a, sy);
-            __syncthreads();
-            forces<T, MODEL>(a, sh, sy);
-            accepted = true;
-            if (threadIdx.x == 0) c[C_ALPHA] = alpha;
-          }
-          __syncthreads();
+          accepted = true;
+          if (threadIdx.x == 0) c[C_ALPHA] = as;
         } else {
           alpha = s_alpha;
         }

@@ -69,7 +69,7 @@ void free_handle(mm_handle* h) {
   if (!h) return;
   void* bufs[] = {h->d_tt, h->d_box, h->d_cell_nodes, h->d_node_cells, h->d_node_lat, h->d_cell_type,
                   h->d_mass, h->d_invm, h->d_c2, h->d_u, h->d_v, h->d_disp, h->d_G, h->d_ecell,
-                  h->d_cpart, h->d_npart, h->d_ticket, h->d_carry, h->d_io, h->d_flag, h->d_adj};
+                  h->d_cpart, h->d_npart, h->d_ticket, h->d_carry, h->d_io, h->d_flag, h->d_adj, h->d_nodef};
   for (void* b : bufs)
     if (b) cudaFree(b);
   delete h;
@@ -179,7 +179,7 @@ mm_status mm_create(int nnodes, int ncells, const int32_t* node_coords, const in
             dev_alloc((char**)&h->d_disp, 3 * (size_t)N * esz) && dev_alloc((char**)&h->d_G, 24 * (size_t)M * esz) &&
             dev_alloc(&h->d_ecell, M) && dev_alloc(&h->d_cpart, (size_t)ncb * 10) &&
             dev_alloc(&h->d_npart, (size_t)nnb * 9) && dev_alloc(&h->d_ticket, 1) && dev_alloc(&h->d_carry, 4) &&
-            dev_alloc(&h->d_io, 9 * (size_t)N + 64) && dev_alloc(&h->d_flag, 1);
+            dev_alloc(&h->d_io, 9 * (size_t)N + 64) && dev_alloc(&h->d_flag, 1) && dev_alloc(&h->d_nodef, N);
   if (ok && !structured)
     ok = dev_alloc(&h->d_cell_nodes, 8 * (size_t)M) && dev_alloc(&h->d_node_cells, 8 * (size_t)N) &&
          dev_alloc(&h->d_node_lat, 3 * (size_t)N);
@@ -193,10 +193,13 @@ mm_status mm_create(int nnodes, int ncells, const int32_t* node_coords, const in
   h->h_mass.assign(masses, masses + N);
   std::vector<double> invm(N);
   for (int i = 0; i < N; ++i) invm[i] = 1.0 / masses[i];
+  std::vector<float4> nodef(N);
+  for (int i = 0; i < N; ++i) nodef[i] = make_float4((float)masses[i], (float)invm[i], 0.0f, 0.0f);
   bool up = cuda_ok(cudaMemcpy(h->d_tt, h->tt, sizeof(h->tt), cudaMemcpyHostToDevice), "upload tt") &&
             cuda_ok(cudaMemcpy(h->d_cell_type, ty.data(), M, cudaMemcpyHostToDevice), "upload types") &&
             cuda_ok(cudaMemcpy(h->d_mass, masses, N * sizeof(double), cudaMemcpyHostToDevice), "upload mass") &&
             cuda_ok(cudaMemcpy(h->d_invm, invm.data(), N * sizeof(double), cudaMemcpyHostToDevice), "upload invm") &&
+            cuda_ok(cudaMemcpy(h->d_nodef, nodef.data(), N * sizeof(float4), cudaMemcpyHostToDevice), "upload nodef") &&
             cuda_ok(cudaMemset(h->d_ticket, 0, sizeof(unsigned)), "memset") &&
             cuda_ok(cudaMemset(h->d_carry, 0, 4 * sizeof(double)), "memset") &&
             cuda_ok(cudaMemset(h->d_v, 0, 3 * (size_t)N * sizeof(double)), "memset") &&
@@ -335,9 +338,14 @@ static mm_status md_prepare(mm_handle* h, double timestep, int thermo, double te
     h->md.c1 = std::exp(-timestep / timecon / 2.0);
     if (h->md.c2_key[0] != timestep || h->md.c2_key[1] != temp || h->md.c2_key[2] != timecon) {
       std::vector<double> c2(h->N);
+      std::vector<float4> nodef(h->N);
       const double c1 = h->md.c1;
-      for (int i = 0; i < h->N; ++i) c2[i] = std::sqrt((1.0 - c1 * c1) * temp * kBoltzmann / h->h_mass[i]);
+      for (int i = 0; i < h->N; ++i) {
+        c2[i] = std::sqrt((1.0 - c1 * c1) * temp * kBoltzmann / h->h_mass[i]);
+        nodef[i] = make_float4((float)h->h_mass[i], (float)(1.0 / h->h_mass[i]), (float)c2[i], 0.0f);
+      }
       MM_CUDA(cudaMemcpyAsync(h->d_c2, c2.data(), h->N * sizeof(double), cudaMemcpyHostToDevice, st));
+      MM_CUDA(cudaMemcpyAsync(h->d_nodef, nodef.data(), h->N * sizeof(float4), cudaMemcpyHostToDevice, st));
       MM_CUDA(cudaStreamSynchronize(st));
       h->md.c2_key[0] = timestep;
       h->md.c2_key[1] = temp;

@@ -32,12 +32,13 @@ __host__ __device__ constexpr int corner_to_bits(int k) { return k == 3 ? 4 : (k
 
 // Per (type, state) parameters in the precision T of the cell arithmetic.
 template <typename T>
-struct StateParams {
+struct __align__(16) StateParams {
+  T A[36];     // 6x6: symmetric stress (Voigt 00,11,22,12,02,01) = A . strain (first: 16-byte aligned rows)
   T hinv[9];   // h0^-1, row-major
   T B[9];      // L - h0 (rows), for the current lattice matrix L
-  T A[36];     // 6x6: symmetric stress (Voigt 00,11,22,12,02,01) = A . strain
   T v0;        // det(h0)
   T df;        // state free energy
+  T pad[2];
 };
 
 template <typename T>

@@ -35,6 +35,7 @@ struct mm_handle {
   double* d_mass = nullptr;           // [N]
   double* d_invm = nullptr;           // [N]
   double* d_c2 = nullptr;             // [N] Langevin noise amplitude
+  float4* d_nodef = nullptr;          // [N] FP32 copies: mass, 1/mass, Langevin amplitude
   double* d_u = nullptr;              // [3][N] displacement from lattice sites (FP64)
   double* d_v = nullptr;              // [3][N] velocities (FP64)
   void* d_disp = nullptr;             // [3][N] displacement in the cell precision

@@ -247,7 +247,7 @@ constexpr int kCell8Threads = 256;
 constexpr int kCell8Cells = kCell8Threads / 8;
 
 template <typename T, bool STRUCT>
-__global__ void __launch_bounds__(kCell8Threads) k_cells8(Topo t, const TypeTable* __restrict__ tt, int ntypes,
+__global__ void __launch_bounds__(kCell8Threads, sizeof(T) == 4 ? 3 : 1) k_cells8(Topo t, const TypeTable* __restrict__ tt, int ntypes,
                                                           const double* __restrict__ box, const T* __restrict__ disp,
                                                           T* __restrict__ G, double* __restrict__ ecell,
                                                           double* __restrict__ cpart) {
@@ -423,7 +423,8 @@ __global__ void __launch_bounds__(kNodeThreads) k_md_nodes(Topo t, MDArgs p, con
                                                            const double* __restrict__ noise, double* __restrict__ npart,
                                                            const double* __restrict__ cpart, int ncblk,
                                                            unsigned* __restrict__ ticket, double* __restrict__ carry,
-                                                           double* __restrict__ record, double* __restrict__ gpos_out) {
+                                                           double* __restrict__ record, double* __restrict__ gpos_out,
+                                                           const float4* __restrict__ nodef) {
   __shared__ double red[kNodePart * (kNodeThreads / 32)];
   __shared__ bool last;
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -433,7 +434,110 @@ __global__ void __launch_bounds__(kNodeThreads) k_md_nodes(Topo t, MDArgs p, con
   R obs[kNodePart];
 #pragma unroll
   for (int i = 0; i < kNodePart; ++i) obs[i] = R(0);
-  if (n < t.N) {
+  if (sizeof(T) == 4 && n < t.N) {
+    // FP32 cells: the velocity and position increments of the whole step are formed in
+    // FP32, the state update itself is FP64:
+    //   v' = cv v + q,  u' = u + dt v'
+    // with (finish and start) cv = c1^2, q = (c1^2 + 1) h a + c1 n1 + n2; (finish only)
+    // cv = c1, q = c1 h a + n1; (start only) cv = c1, q = h a + n2; h = dt/2, a = -g/m,
+    // n1/n2 the post/pre thermostat noise terms (c1 = 1, n = 0 without a thermostat).
+    // The observables come from an FP32 copy of the same velocity sequence.
+    T s[3];
+    gather_node<T, STRUCT>(t, G, n, s);
+    const float4 nf = nodef[n];  // mass, 1/mass, Langevin amplitude
+    const float hf = (float)(0.5 * p.dt), c1f = (float)p.c1;
+    float af[3], n1[3] = {0.f, 0.f, 0.f}, n2[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int x = 0; x < 3; ++x) af[x] = -(float)s[x] * nf.y;
+    if (gpos_out)
+#pragma unroll
+      for (int x = 0; x < 3; ++x) gpos_out[3 * n + x] = (double)s[x];
+    if (THERMO == MM_THERMO_LANGEVIN) {
+      if (p.finish) {
+        if (noise) {
+          const size_t base = ((size_t)(p.step - p.noise_step0) * 2 + 1) * (size_t)t.N * 3;
+#pragma unroll
+          for (int x = 0; x < 3; ++x) n1[x] = nf.z * (float)noise[base + 3 * n + x];
+        } else {
+          float zf[3];
+          normal3(p.seed, (uint32_t)n, (uint32_t)p.step, 1u, zf);
+#pragma unroll
+          for (int x = 0; x < 3; ++x) n1[x] = nf.z * zf[x];
+        }
+      }
+      if (p.start) {
+        if (noise) {
+          const size_t base = ((size_t)(p.step + 1 - p.noise_step0) * 2 + 0) * (size_t)t.N * 3;
+#pragma unroll
+          for (int x = 0; x < 3; ++x) n2[x] = nf.z * (float)noise[base + 3 * n + x];
+        } else {
+          float zf[3];
+          normal3(p.seed, (uint32_t)n, (uint32_t)(p.step + 1), 0u, zf);
+#pragma unroll
+          for (int x = 0; x < 3; ++x) n2[x] = nf.z * zf[x];
+        }
+      }
+    }
+    const float c1 = (THERMO == MM_THERMO_LANGEVIN) ? c1f : 1.0f;
+    double vv[3];
+    float vf[3];
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+      vv[x] = v[x * t.N + n];
+      vf[x] = (float)vv[x];
+    }
+    const float mf = nf.x;
+    if (p.finish) {
+#pragma unroll
+      for (int x = 0; x < 3; ++x) vf[x] += hf * af[x];
+      obs[0] = 0.5f * mf * (vf[0] * vf[0] + vf[1] * vf[1] + vf[2] * vf[2]);
+#pragma unroll
+      for (int x = 0; x < 3; ++x) vf[x] = c1 * vf[x] + n1[x];
+    }
+    obs[1] = 0.5f * mf * (vf[0] * vf[0] + vf[1] * vf[1] + vf[2] * vf[2]);
+    obs[3] = mf * vf[0] * vf[0];
+    obs[4] = mf * vf[1] * vf[1];
+    obs[5] = mf * vf[2] * vf[2];
+    obs[6] = mf * vf[1] * vf[2];
+    obs[7] = mf * vf[0] * vf[2];
+    obs[8] = mf * vf[0] * vf[1];
+    if (p.start) {
+#pragma unroll
+      for (int x = 0; x < 3; ++x) vf[x] = c1 * vf[x] + n2[x];
+      obs[2] = 0.5f * mf * (vf[0] * vf[0] + vf[1] * vf[1] + vf[2] * vf[2]);
+    }
+    if (p.finish || p.start) {
+      double cv;
+      float q[3];
+      if (p.finish && p.start) {
+        cv = p.c1 * p.c1;
+        if (THERMO != MM_THERMO_LANGEVIN) cv = 1.0;
+        const float cc = c1 * c1;
+#pragma unroll
+        for (int x = 0; x < 3; ++x) q[x] = (cc + 1.0f) * hf * af[x] + c1 * n1[x] + n2[x];
+      } else if (p.finish) {
+        cv = (THERMO == MM_THERMO_LANGEVIN) ? p.c1 : 1.0;
+#pragma unroll
+        for (int x = 0; x < 3; ++x) q[x] = c1 * hf * af[x] + n1[x];
+      } else {
+        cv = (THERMO == MM_THERMO_LANGEVIN) ? p.c1 : 1.0;
+#pragma unroll
+        for (int x = 0; x < 3; ++x) q[x] = hf * af[x] + n2[x];
+      }
+#pragma unroll
+      for (int x = 0; x < 3; ++x) {
+        vv[x] = cv * vv[x] + (double)q[x];
+        v[x * t.N + n] = vv[x];
+      }
+      if (p.start)
+#pragma unroll
+        for (int x = 0; x < 3; ++x) {
+          const double un = u[x * t.N + n] + p.dt * vv[x];
+          u[x * t.N + n] = un;
+          disp[x * t.N + n] = (T)un;
+        }
+    }
+  } else if (sizeof(T) == 8 && n < t.N) {
     T s[3];
     gather_node<T, STRUCT>(t, G, n, s);
     const double m = mass[n], im = invm[n];
@@ -723,7 +827,7 @@ static void launch_md_nodes_t(mm_handle* h, const MDArgs& a, const double* noise
   topo_of(h, t);
   k_md_nodes<T, STRUCT, THERMO><<<node_blocks(h), kNodeThreads, 0, st>>>(
       t, a, (const T*)h->d_G, h->d_u, h->d_v, (T*)h->d_disp, h->d_mass, h->d_invm, h->d_c2, noise, h->d_npart,
-      h->d_cpart, cell_blocks(h), h->d_ticket, h->d_carry, record, gpos_out);
+      h->d_cpart, cell_blocks(h), h->d_ticket, h->d_carry, record, gpos_out, h->d_nodef);
 }
 
 template <typename T>

@@ -170,13 +170,142 @@ class VerletIntegrator(Iterative):
             return None
         if len(vhooks) == 1 and type(vhooks[0]) is LangevinThermostat and vhooks[0].start == 0 and vhooks[0].step == 1:
             return vhooks[0]
+        spec = self._batch_spec(vhooks, parts[0])
+        if spec is not None:
+            return ("batch", spec)
         return False
+
+    # systems up to this many cells run NHC / MTK hooks in the one-CTA batch kernel
+    batch_max_cells = 32768
+
+    def _batch_spec(self, vhooks, part):
+        """Hook set the persistent batch kernel runs: NHC and/or MTK (with NHC, Langevin or no thermostat)."""
+        from micmec_gb300.sampling.npt import MTKBarostat, TBCombination
+        from micmec_gb300.sampling.nvt import LangevinThermostat, NHCThermostat
+
+        s = self.mmf.system
+        grid = np.asarray(s.grid)
+        if len(vhooks) != 1 or grid is None or (grid == 0).any() or s.ncells > self.batch_max_cells:
+            return None
+        if not part.pbc or not part.handle or s.nnodes != grid.size:
+            return None
+        h = vhooks[0]
+        if h.start != 0 or h.step != 1:
+            return None
+        thermo, baro = None, None
+        if isinstance(h, TBCombination):
+            thermo, baro = h.thermostat, h.barostat
+            if thermo.step != 1 or baro.step != 1:
+                return None
+        elif type(h) is NHCThermostat:
+            thermo = h
+        elif type(h) is MTKBarostat:
+            baro = h
+        else:
+            return None
+        if thermo is not None and type(thermo) not in (NHCThermostat, LangevinThermostat):
+            return None
+        if baro is not None and (type(baro) is not MTKBarostat or not baro.anisotropic or baro.vol_constraint
+                                 or baro.baro_thermo is not None):
+            return None
+        if type(thermo) is NHCThermostat and thermo.chain.length != 3:
+            return None
+        return dict(hook=h, thermo=thermo, baro=baro)
+
+    def _run_batch(self, nsteps, spec):
+        """NHC / MTK hooks on the device: the system as a one-element batch (one persistent CTA)."""
+        from micmec_gb300.batch import BatchSystems, CTL, REC
+        from micmec_gb300.sampling.nvt import LangevinThermostat, NHCThermostat
+
+        part = self.mmf.parts[0]
+        thermo, baro, hook = spec["thermo"], spec["baro"], spec["hook"]
+        b = getattr(self, "_batch", None)
+        if b is None:
+            b = self._batch = BatchSystems([self.mmf.system], model=part.model, precision=part.precision)
+        b.set_state([self.pos], [self.vel], [self.mmf.system.domain.rvecs])
+        c = b.control()
+        c[0, CTL["ndof"]] = self.ndof
+        kind, temp, timecon, noise = None, 0.0, 1.0, None
+        if type(thermo) is NHCThermostat:
+            kind, temp, timecon = "nhc", thermo.temp, thermo.chain.timecon
+            c[0, CTL["chain_pos"]] = thermo.chain.pos
+            c[0, CTL["chain_vel"]] = thermo.chain.vel
+            c[0, CTL["chain_mass"]] = thermo.chain.masses
+            c[0, CTL["econs_thermo"]] = thermo.econs_correction
+        elif type(thermo) is LangevinThermostat:
+            kind, temp, timecon = "langevin", thermo.temp, thermo.timecon
+            c[0, CTL["econs_thermo"]] = thermo.econs_correction
+        if baro is not None:
+            c[0, CTL["vel_press"]] = np.asarray(baro.vel_press).ravel()
+            c[0, CTL["mass_press"]] = baro.mass_press
+            c[0, CTL["baro_ndof"]] = baro.baro_ndof
+            c[0, CTL["econs_baro"]] = baro.econs_correction
+            temp = temp if thermo is not None else baro.temp
+        c[0, CTL["epot"]] = self.epot
+        c[0, CTL["vtens"]] = self.vtens.ravel()
+        b.set_control(c)
+        seed = 0
+        if type(thermo) is LangevinThermostat:
+            seed = thermo.seed
+            if thermo.replay_noise is not None:
+                i0 = 2 * (self.counter - thermo.replay_offset)
+                noise = np.asarray(thermo.replay_noise[i0:i0 + 2 * nsteps]).reshape(nsteps, 2, -1, 3)
+        rec = b.md(nsteps, timestep=self.timestep, thermostat=kind, temp=temp, timecon=timecon,
+                   barostat="mtk" if baro is not None else None, press=0.0 if baro is None else baro.press,
+                   seed=seed, step0=self.counter, noise=noise, record=True, use_graph=False)[0]
+        if not np.isfinite(rec[:, :3]).all():
+            raise ValueError("The energy is not-a-number (``nan``).")
+        pos, vel, rv = b.get_state()
+        c = b.control()
+        if type(thermo) is NHCThermostat:
+            thermo.chain.pos[:] = c[0, CTL["chain_pos"]]
+            thermo.chain.vel[:] = c[0, CTL["chain_vel"]]
+        if baro is not None:
+            baro.vel_press = c[0, CTL["vel_press"]].reshape(3, 3).copy()
+        return rec, pos[0], vel[0], rv[0], c[0], (thermo, baro, hook)
+
+    def _finish_batch_chunk(self, rec, pos, vel, rv, ctl, hooks):
+        from micmec_gb300.batch import CTL, REC
+
+        thermo, baro, hook = hooks
+        for r in rec:
+            self.counter += 1
+            self.time += self.timestep
+            self.epot = r[REC["epot"]]
+            self.ekin = r[REC["ekin"]]
+            hook.econs_correction = r[REC["ecorr"]]
+            self.vtens = r[REC["vtens"]].reshape(3, 3).copy()
+            if baro is not None:
+                self.mmf.system.domain.update_rvecs(r[REC["rvecs"]].reshape(3, 3))
+            self._finish_properties(ktens=r[REC["ktens"]].reshape(3, 3))
+        if thermo is not None and thermo is not hook:
+            thermo.econs_correction = ctl[CTL["econs_thermo"]]
+        if baro is not None and baro is not hook:
+            baro.econs_correction = ctl[CTL["econs_baro"]]
+        self.pos[:] = pos
+        self.vel[:] = vel
+        if baro is not None:
+            self.rvecs[:] = rv
+            self.mmf.update_rvecs(rv)
+        self.mmf.update_pos(self.pos)
+        self.delta[:] = self.pos - self.posold
+        self.posold[:] = self.pos
+        self.rmsd_delta = np.sqrt(np.mean(self.delta**2))
 
     def run(self, nsteps=None):
         plan = self._device_plan() if nsteps is not None else False
         if plan is False:
             return Iterative.run(self, nsteps)
-        self._run_device(int(nsteps), plan)
+        if isinstance(plan, tuple) and plan[0] == "batch":
+            remaining = int(nsteps)
+            while remaining > 0:
+                k = self._next_hook_gap(remaining)
+                out = self._run_batch(k, plan[1])
+                self._finish_batch_chunk(*out)
+                remaining -= k
+                self.call_hooks()
+        else:
+            self._run_device(int(nsteps), plan)
         self.finalize()
 
     def _next_hook_gap(self, remaining):

@@ -76,7 +76,7 @@ def test_force_loss_gradient_matches_central_differences():
               (params.h0, gh, (1, 1, 2, 1)), (params.free_energy, gd, (0, 1))]
     for tensor, grad, idx in checks:
         base = tensor.detach()[idx].item()
-        h = 1e-4 * max(abs(base), 1e-12)
+        h = 1e-4 * max(abs(base), 1e-2 * tensor.detach().abs().max().item())
         vals = []
         for sgn in (1, -1):
             with torch.no_grad():
@@ -111,7 +111,7 @@ def test_trajectory_gradient_with_checkpointing():
     for tensor, grad, idx in ((params.c21, gc, (0, 0, 0)), (params.h0, gh, (0, 1, 1, 1)),
                               (params.free_energy, gd, (1, 0))):
         base = tensor.detach()[idx].item()
-        h = 1e-4 * max(abs(base), 1e-12)
+        h = 1e-4 * max(abs(base), 1e-2 * tensor.detach().abs().max().item())
         vals = []
         for sgn in (1, -1):
             with torch.no_grad():
