@@ -146,6 +146,23 @@ mm_status mm_md_advance(mm_handle* h, int nsteps, double* records, int finish, v
 mm_status mm_md_end(mm_handle* h, double* pos, double* vel, void* stream);
 
 /*
+ * MD with the Nose-Hoover chain (thermo 2, chain length 3), Langevin (thermo 1) or no
+ * thermostat, optionally with the anisotropic MTK barostat (baro 1), for a system of any
+ * size spread over the whole GPU: the step of VerletIntegrator.propagate
+ * (micmec/sampling/verlet.py:140-166) with TBCombination / NHCThermostat / MTKBarostat
+ * (micmec/sampling/npt.py:99-148, 513-757; nvt.py:361-532) as grid-wide kernels and
+ * one-thread controller kernels.
+ *  pos, vel (N,3) device: in/out.   ctl_host double[MM_BATCH_CTL] host: hook constants
+ *  and state in the layout of mm_batch_control (ndof, chain masses/positions/velocities,
+ *  barostat mass/velocity/dof, conserved-energy corrections); returned updated. The
+ *  lattice/domain part is taken from the handle and returned after the barostat moved it.
+ *  records device (nsteps, MM_BATCH_REC) or NULL.  noise: as mm_md_run, or NULL.
+ */
+mm_status mm_md_engine(mm_handle* h, double* pos, double* vel, int nsteps, double timestep, int thermo, double temp,
+                       double timecon, int baro, double press, int chain, uint64_t seed, const double* noise,
+                       double* ctl_host, double* records, int64_t step0, void* stream);
+
+/*
  * Measurement helper: run nsteps steps of the session like mm_md_advance(finish = 0),
  * with CUDA events around the cell kernel and the node kernel of every step, and
  * return the summed durations (ms). If flush_buf is given, flush_bytes of it are

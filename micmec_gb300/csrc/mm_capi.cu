@@ -69,7 +69,7 @@ void free_handle(mm_handle* h) {
   if (!h) return;
   void* bufs[] = {h->d_tt, h->d_box, h->d_cell_nodes, h->d_node_cells, h->d_node_lat, h->d_cell_type,
                   h->d_mass, h->d_invm, h->d_c2, h->d_u, h->d_v, h->d_disp, h->d_G, h->d_ecell,
-                  h->d_cpart, h->d_npart, h->d_ticket, h->d_carry, h->d_io, h->d_flag, h->d_adj, h->d_nodef};
+                  h->d_cpart, h->d_npart, h->d_ticket, h->d_carry, h->d_io, h->d_flag, h->d_adj, h->d_nodef, h->d_eng};
   for (void* b : bufs)
     if (b) cudaFree(b);
   delete h;

@@ -49,6 +49,8 @@ struct mm_handle {
   int* d_flag = nullptr;              // NaN flag
   double* d_adj = nullptr;            // adjoint scratch (allocated on first mm_adjoint call)
   size_t adj_len = 0;
+  double* d_eng = nullptr;            // NHC/MTK engine scratch (allocated on first mm_md_engine call)
+  size_t eng_len = 0;
   // MD session
   struct {
     double dt = 0.0, c1 = 1.0, temp = 0.0, timecon = 0.0;

@@ -247,7 +247,7 @@ constexpr int kCell8Threads = 256;
 constexpr int kCell8Cells = kCell8Threads / 8;
 
 template <typename T, bool STRUCT>
-__global__ void __launch_bounds__(kCell8Threads, sizeof(T) == 4 ? 3 : 1) k_cells8(Topo t, const TypeTable* __restrict__ tt, int ntypes,
+__global__ void __launch_bounds__(kCell8Threads) k_cells8(Topo t, const TypeTable* __restrict__ tt, int ntypes,
                                                           const double* __restrict__ box, const T* __restrict__ disp,
                                                           T* __restrict__ G, double* __restrict__ ecell,
                                                           double* __restrict__ cpart) {

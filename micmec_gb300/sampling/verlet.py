@@ -183,11 +183,7 @@ class VerletIntegrator(Iterative):
         from micmec_gb300.sampling.npt import MTKBarostat, TBCombination
         from micmec_gb300.sampling.nvt import LangevinThermostat, NHCThermostat
 
-        s = self.mmf.system
-        grid = np.asarray(s.grid)
-        if len(vhooks) != 1 or grid is None or (grid == 0).any() or s.ncells > self.batch_max_cells:
-            return None
-        if not part.pbc or not part.handle or s.nnodes != grid.size:
+        if len(vhooks) != 1 or not part.handle:
             return None
         h = vhooks[0]
         if h.start != 0 or h.step != 1:
@@ -210,7 +206,12 @@ class VerletIntegrator(Iterative):
             return None
         if type(thermo) is NHCThermostat and thermo.chain.length != 3:
             return None
-        return dict(hook=h, thermo=thermo, baro=baro)
+        if baro is not None and not part.pbc:
+            return None
+        s = self.mmf.system
+        grid = np.asarray(s.grid)
+        small = (part.pbc and not (grid == 0).any() and s.nnodes == grid.size and s.ncells <= self.batch_max_cells)
+        return dict(hook=h, thermo=thermo, baro=baro, engine="batch" if small else "lattice")
 
     def _run_batch(self, nsteps, spec):
         """NHC / MTK hooks on the device: the system as a one-element batch (one persistent CTA)."""
@@ -264,6 +265,69 @@ class VerletIntegrator(Iterative):
             baro.vel_press = c[0, CTL["vel_press"]].reshape(3, 3).copy()
         return rec, pos[0], vel[0], rv[0], c[0], (thermo, baro, hook)
 
+    def _hook_control(self, thermo, baro):
+        """Control block (layout of the batch/engine kernels) from the initialised hooks."""
+        from micmec_gb300.batch import CTL, CTL_LEN
+        from micmec_gb300.sampling.nvt import LangevinThermostat, NHCThermostat
+
+        c = np.zeros(CTL_LEN)
+        c[CTL["ndof"]] = self.ndof
+        kind, temp, timecon = None, 0.0, 1.0
+        if type(thermo) is NHCThermostat:
+            kind, temp, timecon = "nhc", thermo.temp, thermo.chain.timecon
+            c[CTL["chain_pos"]] = thermo.chain.pos
+            c[CTL["chain_vel"]] = thermo.chain.vel
+            c[CTL["chain_mass"]] = thermo.chain.masses
+            c[CTL["econs_thermo"]] = thermo.econs_correction
+        elif type(thermo) is LangevinThermostat:
+            kind, temp, timecon = "langevin", thermo.temp, thermo.timecon
+            c[CTL["econs_thermo"]] = thermo.econs_correction
+        if baro is not None:
+            c[CTL["vel_press"]] = np.asarray(baro.vel_press).ravel()
+            c[CTL["mass_press"]] = baro.mass_press
+            c[CTL["baro_ndof"]] = baro.baro_ndof
+            c[CTL["econs_baro"]] = baro.econs_correction
+            temp = temp if thermo is not None else baro.temp
+        return c, kind, temp, timecon
+
+    def _run_engine(self, nsteps, spec):
+        """NHC / MTK hooks on the device for a system spread over the whole GPU (mm_md_engine)."""
+        import torch
+
+        from micmec_gb300 import _native as nat
+        from micmec_gb300.batch import CTL, REC_LEN
+        from micmec_gb300.sampling.nvt import LangevinThermostat, NHCThermostat
+
+        part = self.mmf.parts[0]
+        thermo, baro, hook = spec["thermo"], spec["baro"], spec["hook"]
+        c, kind, temp, timecon = self._hook_control(thermo, baro)
+        dev = part.device
+        pos_d = torch.from_numpy(np.ascontiguousarray(self.pos)).to(dev)
+        vel_d = torch.from_numpy(np.ascontiguousarray(self.vel)).to(dev)
+        rec = torch.zeros((nsteps, REC_LEN), dtype=torch.float64, device=dev)
+        noise, seed = None, 0
+        if type(thermo) is LangevinThermostat:
+            seed = thermo.seed
+            if thermo.replay_noise is not None:
+                i0 = 2 * (self.counter - thermo.replay_offset)
+                noise = torch.from_numpy(np.ascontiguousarray(thermo.replay_noise[i0:i0 + 2 * nsteps])).to(dev)
+        st = nat.lib().mm_md_engine(part.handle, pos_d.data_ptr(), vel_d.data_ptr(), int(nsteps), float(self.timestep),
+                                    {None: 0, "langevin": 1, "nhc": 2}[kind], float(temp), float(timecon),
+                                    1 if baro is not None else 0, 0.0 if baro is None else float(baro.press), 3,
+                                    int(seed), nat.ptr(noise), c.ctypes.data, rec.data_ptr(), int(self.counter),
+                                    torch.cuda.current_stream().cuda_stream)
+        nat.check(st, "mm_md_engine")
+        rec = rec.cpu().numpy()
+        if not np.isfinite(rec[:, :3]).all():
+            raise ValueError("The energy is not-a-number (``nan``).")
+        if type(thermo) is NHCThermostat:
+            thermo.chain.pos[:] = c[CTL["chain_pos"]]
+            thermo.chain.vel[:] = c[CTL["chain_vel"]]
+        if baro is not None:
+            baro.vel_press = c[CTL["vel_press"]].reshape(3, 3).copy()
+        rv = c[CTL["rvecs"]].reshape(3, 3).copy()
+        return rec, pos_d.cpu().numpy(), vel_d.cpu().numpy(), rv, c, (thermo, baro, hook)
+
     def _finish_batch_chunk(self, rec, pos, vel, rv, ctl, hooks):
         from micmec_gb300.batch import CTL, REC
 
@@ -300,7 +364,10 @@ class VerletIntegrator(Iterative):
             remaining = int(nsteps)
             while remaining > 0:
                 k = self._next_hook_gap(remaining)
-                out = self._run_batch(k, plan[1])
+                if plan[1]["engine"] == "batch":
+                    out = self._run_batch(k, plan[1])
+                else:
+                    out = self._run_engine(k, plan[1])
                 self._finish_batch_chunk(*out)
                 remaining -= k
                 self.call_hooks()

@@ -72,8 +72,11 @@ def test_force_loss_gradient_matches_central_differences():
 
     l0 = loss()
     gc, gh, gd = torch.autograd.grad(l0, [params.c21, params.h0, params.free_energy])
+    # the free-energy slot with the largest effect (in a lattice built on state 0's rest cell the
+    # other states carry weights ~exp(-E/kT) far below rounding)
+    fe = tuple(int(i) for i in np.unravel_index(int(gd.abs().argmax()), gd.shape))
     checks = [(params.c21, gc, (0, 1, 0)), (params.c21, gc, (1, 0, 3)), (params.h0, gh, (0, 0, 0, 0)),
-              (params.h0, gh, (1, 1, 2, 1)), (params.free_energy, gd, (0, 1))]
+              (params.h0, gh, (1, 1, 2, 1)), (params.free_energy, gd, fe)]
     for tensor, grad, idx in checks:
         base = tensor.detach()[idx].item()
         h = 1e-4 * max(abs(base), 1e-2 * tensor.detach().abs().max().item())
@@ -85,7 +88,9 @@ def test_force_loss_gradient_matches_central_differences():
         with torch.no_grad():
             tensor[idx] = base
         fd = (vals[0] - vals[1]) / (2 * h)
-        assert abs(fd - grad[idx].item()) <= 1e-6 * max(abs(fd), 1e-3 * grad.abs().max().item()), (idx, fd, grad[idx])
+        floor = 1e-13 * abs(l0.item()) / h  # rounding of the central difference
+        assert abs(fd - grad[idx].item()) <= 1e-6 * max(abs(fd), 1e-3 * grad.abs().max().item()) + floor, \
+            (idx, fd, grad[idx])
 
 
 def test_trajectory_gradient_with_checkpointing():
@@ -108,8 +113,9 @@ def test_trajectory_gradient_with_checkpointing():
 
     l0 = loss()
     gc, gh, gd = torch.autograd.grad(l0, [params.c21, params.h0, params.free_energy])
+    fe = tuple(int(i) for i in np.unravel_index(int(gd.abs().argmax()), gd.shape))
     for tensor, grad, idx in ((params.c21, gc, (0, 0, 0)), (params.h0, gh, (0, 1, 1, 1)),
-                              (params.free_energy, gd, (1, 0))):
+                              (params.free_energy, gd, fe)):
         base = tensor.detach()[idx].item()
         h = 1e-4 * max(abs(base), 1e-2 * tensor.detach().abs().max().item())
         vals = []
@@ -120,4 +126,6 @@ def test_trajectory_gradient_with_checkpointing():
         with torch.no_grad():
             tensor[idx] = base
         fd = (vals[0] - vals[1]) / (2 * h)
-        assert abs(fd - grad[idx].item()) <= 1e-6 * max(abs(fd), 1e-3 * grad.abs().max().item()), (idx, fd, grad[idx])
+        floor = 1e-13 * abs(l0.item()) / h
+        assert abs(fd - grad[idx].item()) <= 1e-6 * max(abs(fd), 1e-3 * grad.abs().max().item()) + floor, \
+            (idx, fd, grad[idx])

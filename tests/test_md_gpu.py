@@ -85,7 +85,7 @@ def test_langevin_replay_matches_reference(device):
     _compare(g, rec, 200, 1e-8)
 
 
-@pytest.mark.parametrize("device", [True, False])
+@pytest.mark.parametrize("device", ["batch", "engine", "host"])
 def test_nhc_matches_reference(device):
     from micmec_gb300.sampling.nvt import NHCThermostat
     from micmec_gb300.sampling.verlet import VerletIntegrator
@@ -94,13 +94,16 @@ def test_nhc_matches_reference(device):
     rec = Rec()
     t = NHCThermostat(float(g["meta/temp"]), timecon=float(g["meta/timecon"]), chainlength=3,
                       chain_vel0=g["meta/chain_vel0"].copy())
-    vi = VerletIntegrator(ff, float(g["timestep"]), hooks=[t, rec.hook], vel0=g["vel0"].copy(), device=device)
+    vi = VerletIntegrator(ff, float(g["timestep"]), hooks=[t, rec.hook], vel0=g["vel0"].copy(),
+                          device=device != "host")
+    if device == "engine":
+        vi.batch_max_cells = 0
     vi.run(200)
     _compare(g, rec, 200, 1e-8)
     assert np.allclose(t.chain.pos, g["chain_pos_end"], rtol=1e-7, atol=1e-12)
 
 
-@pytest.mark.parametrize("device", [True, False])
+@pytest.mark.parametrize("device", ["batch", "engine", "host"])
 @pytest.mark.parametrize("name", ["md_mtk_nanocell", "md_nhc_mtk_nanocell", "md_langevin_mtk_nanocell"])
 def test_mtk_matches_reference(name, device):
     from micmec_gb300.sampling.npt import MTKBarostat
@@ -124,7 +127,10 @@ def test_mtk_matches_reference(name, device):
         hooks.append(MTKBarostat(ff, T, float(g["meta/press"]), timecon=float(g["meta/timecon_baro"]),
                                  vel_press0=g["meta/vel_press0"].copy()))
     n = len(g["records"]) - 1
-    vi = VerletIntegrator(ff, float(g["timestep"]), hooks=hooks + [rec.hook], vel0=g["vel0"].copy(), device=device)
+    vi = VerletIntegrator(ff, float(g["timestep"]), hooks=hooks + [rec.hook], vel0=g["vel0"].copy(),
+                          device=device != "host")
+    if device == "engine":
+        vi.batch_max_cells = 0
     vi.run(n)
     _compare(g, rec, n, 1e-7)
     assert np.allclose(s.domain.rvecs, g["rvecs_end"], rtol=1e-9)
