@@ -49,7 +49,8 @@ FLUSH_BYTES = 256 << 20
 # algorithmic figures (per cell, per evaluation / step)
 STEP_BYTES = 97          # pos r/w 24+24, vel r/w 24+24, cell type 1 (FP64 SoA state)
 CELL_KERNEL_BYTES = 109  # displacement read 12 (FP32 xyz), type 1, corner gradients written 96 (24 x FP32)
-FLOP_PER_STATE = 2400    # 8 corner matrices x ~300 flop (strain, stress, energy, gradient)
+FLOP_PER_STATE = 2400    # 8 corner matrices x ~300 flop (strain, stress, energy, gradient), general h0 / C
+FLOP_PER_STATE_CUBIC = 1450  # the same with diagonal h0 and cubic C (reduced 3x3 / 6x6 products)
 FLOP_LSE = 20
 
 
@@ -223,8 +224,29 @@ def run_reference(args):
 # ---------------------------------------------------------------- GPU arm
 
 
-def measure_fp64_lattice(s, vel, nsteps, flush):
-    """The plain FP64 GPU path on the same lattice: same session API, FP64 cells."""
+def general_form(d):
+    """Copy of a system dict whose types have a slightly anisotropic C and sheared h0.
+
+    The standard fcu/reo types have diagonal rest matrices and cubic elasticity, for
+    which the cell kernel uses reduced strain/stress products; this variant takes the
+    general 3x3 / 6x6 products and is timed beside the main line.
+    """
+    g = dict(d)
+    for k in list(d):
+        if k.endswith("/elasticity"):
+            C = np.array(d[k], dtype=float)
+            C[..., 0, 0, 0, 0] *= 1.001
+            g[k] = C
+        elif k.endswith("/cell"):
+            h = np.array(d[k], dtype=float)
+            h[..., 0, 1] += 1e-4 * h[..., 0, 0]
+            h[..., 1, 0] += 1e-4 * h[..., 0, 0]
+            g[k] = h
+    return g
+
+
+def measure_lattice(s, vel, nsteps, flush, precision="fp64"):
+    """The same session API on the same lattice at another cell precision."""
     import torch
 
     from micmec_gb300 import _native as nat, units
@@ -232,7 +254,7 @@ def measure_fp64_lattice(s, vel, nsteps, flush):
 
     L = nat.lib()
     dev = flush.device
-    fp = ForcePartMechanical(s, model="nanocell", precision="fp64")
+    fp = ForcePartMechanical(s, model="nanocell", precision=precision)
     stream = torch.cuda.current_stream().cuda_stream
     pos_d = torch.from_numpy(np.ascontiguousarray(s.pos)).to(dev)
     vel_d = torch.from_numpy(np.ascontiguousarray(vel)).to(dev)
@@ -470,7 +492,8 @@ def run_gpu(args):
     # ---- roofline of the dominant kernel (cells)
     hbm, kind = peaks()
     achieved = CELL_KERNEL_BYTES * M / (cell_ms * 1e-3) / 1e9
-    flops = (FLOP_PER_STATE * 2 + FLOP_LSE) * M / (cell_ms * 1e-3) / 1e12
+    # the standard fcu/reo types have diagonal h0 and cubic C: the kernel runs the reduced products
+    flops = (FLOP_PER_STATE_CUBIC * 2 + FLOP_LSE) * M / (cell_ms * 1e-3) / 1e12
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "cells_fp32_nanocell_traffic.json")
     if os.path.exists(tfile):
@@ -496,9 +519,15 @@ def run_gpu(args):
     }
     if rank == 0 and not args.no_extra:
         try:
-            v64, ms64 = measure_fp64_lattice(s, vel, max(5, min(args.steps, 30)), flush)
+            v64, ms64 = measure_lattice(s, vel, max(5, min(args.steps, 30)), flush, "fp64")
             line["fp64_lattice"] = {"value": v64, "unit": UNIT, "ms_per_step": ms64,
                                     "fp32_over_fp64": value / world / v64}
+            from micmec_gb300.system import System
+
+            sg = System.from_dict(general_form(d))
+            vg, msg = measure_lattice(sg, vel, max(5, min(args.steps, 30)), flush, "fp32")
+            line["general_params_fp32"] = {"value": vg, "unit": UNIT, "ms_per_step": msg,
+                                           "note": "anisotropic C, sheared h0: full 3x3/6x6 products"}
             systems, strains = batch_workload()
             bf = measure_batch(systems, strains, "fp32", 200, 400)
             bd = measure_batch(systems, strains, "fp64", 20, 100)

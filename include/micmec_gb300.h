@@ -294,6 +294,13 @@ const char* mm_last_error(void);
 /* Library version string. */
 const char* mm_version(void);
 
+/*
+ * Self-test of the device-side FP64 <-> FP32 conversions the FP32 node update uses
+ * (integer-pipe restatements of IEEE 754 round-to-nearest-even and exact widening):
+ * dout[i] = (float)din[i], fout[i] = (double)fin[i] for i < n. All pointers device.
+ */
+mm_status mm_selftest_convert(const double* din, float* dout, const float* fin, double* fout, int n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -377,6 +377,7 @@ mm_status mm_set_params(mm_handle* h, const double* h0, const double* C, const d
       st.df = free_energy[slot];
     }
   }
+  h->simple = mm::tables_are_simple(h->tt, h->ntypes);
   const cudaError_t e = cudaMemcpy(h->d_tt, h->tt, sizeof(h->tt), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     mm::set_error(std::string("mm_set_params: ") + cudaGetErrorString(e));

@@ -87,6 +87,20 @@ extern "C" {
 const char* mm_last_error(void) { return mm::last_error(); }
 const char* mm_version(void) { return MM_VERSION; }
 
+mm_status mm_selftest_convert(const double* din, float* dout, const float* fin, double* fout, int n, void* stream) {
+  if (n < 0 || (n > 0 && (!din || !dout || !fin || !fout))) {
+    mm::set_error("mm_selftest_convert: bad arguments");
+    return MM_ERR_ARG;
+  }
+  mm::launch_selftest_convert(din, dout, fin, fout, n, (cudaStream_t)stream);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    mm::set_error(std::string("mm_selftest_convert: ") + cudaGetErrorString(e));
+    return MM_ERR_CUDA;
+  }
+  return MM_OK;
+}
+
 mm_status mm_create(int nnodes, int ncells, const int32_t* node_coords, const int32_t* cell_nodes,
                     const int32_t* node_cells, const int32_t* cell_type, const int32_t* lattice_shape, int pbc,
                     int ntypes, const int32_t* nstates, const double* h0, const double* C,
@@ -151,6 +165,8 @@ mm_status mm_create(int nnodes, int ncells, const int32_t* node_coords, const in
       st.df = free_energy[slot];
     }
   }
+
+  h->simple = mm::tables_are_simple(h->tt, ntypes);
 
   // structured lattice detection: periodic, every lattice site a node and a cell,
   // tables identical to the implicit ones

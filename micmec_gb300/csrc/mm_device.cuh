@@ -70,15 +70,26 @@ struct TypeTable {
 // This is the energy of nanocell_original.py:46-82 / nanocell.py:40-77 and the
 // gradient form of nanocell.py:98-132 (stress C_ijkl eps_kl against the
 // symmetric strain derivative).
-template <typename T>
+// SIMPLE: every rest matrix is diagonal and every stress map has cubic form
+// (A00 = A11 = A22, A01 = A02 = A12 and symmetric, A33 = A44 = A55, all else 0); the
+// products with h0^-1 and A then reduce to scalings (detected exactly on the host).
+template <typename T, bool SIMPLE = false>
 __device__ __forceinline__ T state_energy_grad(const T* __restrict__ W, const StateParams<T>& p, T scale,
                                                T* __restrict__ GW) {
   T D[9];
+  if (SIMPLE) {
+    const T h[3] = {p.hinv[0], p.hinv[4], p.hinv[8]};
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) D[i * 3 + k] = W[k * 3 + i] * h[k];
+  } else {
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int k = 0; k < 3; ++k)
       D[i * 3 + k] = W[0 * 3 + i] * p.hinv[k * 3 + 0] + W[1 * 3 + i] * p.hinv[k * 3 + 1] + W[2 * 3 + i] * p.hinv[k * 3 + 2];
+  }
   const T h = T(0.5);
   T e[6];
   e[0] = D[0] + h * (D[0] * D[0] + D[3] * D[3] + D[6] * D[6]);
@@ -88,12 +99,23 @@ __device__ __forceinline__ T state_energy_grad(const T* __restrict__ W, const St
   e[4] = h * (D[2] + D[6] + D[0] * D[2] + D[3] * D[5] + D[6] * D[8]);
   e[5] = h * (D[1] + D[3] + D[0] * D[1] + D[3] * D[4] + D[6] * D[7]);
   T s[6];
+  if (SIMPLE) {
+    const T a = p.A[0], b = p.A[1], c = p.A[21];
+    const T tr = e[0] + e[1] + e[2];
+    s[0] = (a - b) * e[0] + b * tr;
+    s[1] = (a - b) * e[1] + b * tr;
+    s[2] = (a - b) * e[2] + b * tr;
+    s[3] = c * e[3];
+    s[4] = c * e[4];
+    s[5] = c * e[5];
+  } else {
 #pragma unroll
   for (int q = 0; q < 6; ++q) {
     T acc = T(0);
 #pragma unroll
     for (int r = 0; r < 6; ++r) acc += p.A[q * 6 + r] * e[r];
     s[q] = acc;
+  }
   }
   T dens = e[0] * s[0] + e[1] * s[1] + e[2] * s[2] + T(2) * (e[3] * s[3] + e[4] * s[4] + e[5] * s[5]);
   // S symmetric 3x3 from s
@@ -106,11 +128,20 @@ __device__ __forceinline__ T state_energy_grad(const T* __restrict__ W, const St
     for (int l = 0; l < 3; ++l)
       GF[i * 3 + l] = S[i * 3 + l] + D[i * 3 + 0] * S[0 * 3 + l] + D[i * 3 + 1] * S[1 * 3 + l] + D[i * 3 + 2] * S[2 * 3 + l];
   // GW[j][i] = scale * sum_k GF[i][k] hinv[k][j]
+  if (SIMPLE) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const T sj = scale * p.hinv[j * 4];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) GW[j * 3 + i] = sj * GF[i * 3 + j];
+    }
+  } else {
 #pragma unroll
   for (int j = 0; j < 3; ++j)
 #pragma unroll
     for (int i = 0; i < 3; ++i)
       GW[j * 3 + i] = scale * (GF[i * 3 + 0] * p.hinv[0 * 3 + j] + GF[i * 3 + 1] * p.hinv[1 * 3 + j] + GF[i * 3 + 2] * p.hinv[2 * 3 + j]);
+  }
   return h * scale * dens;
 }
 
@@ -261,25 +292,83 @@ __device__ __forceinline__ void warp_sum_f2(F2 (&v)[NV]) {
     }
 }
 
-// Block sum: compensated FP32 within each warp, FP64 across warps (fixed order).
-// Result valid in thread 0. smem must hold NV * (blockDim.x / 32) doubles.
+// Block sum: compensated FP32 within each warp and across the warps (warp 0 adds the
+// warps' (hi, lo) pairs in fixed order); one FP64 conversion per value per block.
+// Result valid in thread 0. smem must hold NV * (blockDim.x / 32) doubles. Ends
+// without a barrier: a caller that reuses smem afterwards synchronises first.
 template <int NV>
 __device__ __forceinline__ void block_sum_f2(F2 (&v)[NV], double (&out)[NV], double* smem) {
   warp_sum_f2<NV>(v);
+  F2* s2 = reinterpret_cast<F2*>(smem);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   if (lane == 0)
 #pragma unroll
-    for (int i = 0; i < NV; ++i) smem[i * nw + wid] = (double)v[i].hi + (double)v[i].lo;
+    for (int i = 0; i < NV; ++i) s2[i * nw + wid] = v[i];
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (wid == 0) {
 #pragma unroll
-    for (int i = 0; i < NV; ++i) {
-      double acc = 0.0;
-      for (int w = 0; w < nw; ++w) acc += smem[i * nw + w];
-      out[i] = acc;
+    for (int i = 0; i < NV; ++i) v[i] = (lane < nw) ? s2[i * nw + lane] : F2{0.0f, 0.0f};
+    for (int off = 16; off > 0; off >>= 1) {
+      if (off >= nw) continue;
+#pragma unroll
+      for (int i = 0; i < NV; ++i) {
+        F2 o{__shfl_down_sync(0xffffffffu, v[i].hi, off), __shfl_down_sync(0xffffffffu, v[i].lo, off)};
+        v[i] = f2_add(v[i], o);
+      }
     }
+    if (lane == 0)
+#pragma unroll
+      for (int i = 0; i < NV; ++i) out[i] = (double)v[i].hi + (double)v[i].lo;
   }
-  __syncthreads();
+}
+
+// IEEE 754 binary64 <-> binary32 conversions built from the bit layouts with integer
+// operations only (the FP64 pipe of this part is narrow and hardware conversions queue
+// there). d2f_rn rounds to nearest, ties to even, including subnormal results and
+// overflow to infinity; every NaN becomes the canonical NaN 0x7fffffff. f2d is exact.
+__device__ __forceinline__ float d2f_rn(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const unsigned sign = hi & 0x80000000u;
+  const unsigned e = (hi >> 20) & 0x7FFu;  // binary32 exponent field = e - 896
+  unsigned f;
+  if (e - 897u <= 253u) {  // normal binary32 result (before rounding)
+    f = ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const unsigned rem = lo & 0x1FFFFFFFu, halfway = 0x10000000u;
+    f += (unsigned)(rem > halfway) | ((unsigned)(rem == halfway) & (f & 1u));  // a carry bumps the exponent
+  } else if (e >= 1151u) {  // too large, infinity or NaN
+    f = (e == 2047u && (((hi & 0xFFFFFu) | lo) != 0u)) ? 0x7FFFFFFFu : 0x7F800000u;
+    if (f == 0x7FFFFFFFu) return __uint_as_float(f);
+  } else if (e < 873u) {  // below half the smallest subnormal: zero
+    f = 0u;
+  } else {  // subnormal binary32: value = m * 2^(e - 1075), bits = round(m >> (926 - e))
+    const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const unsigned sh = 926u - e;  // 30 .. 53
+    const unsigned long long q = m >> sh, rem = m & ((1ull << sh) - 1ull), halfway = 1ull << (sh - 1u);
+    f = (unsigned)q + ((unsigned)(rem > halfway) | ((unsigned)(rem == halfway) & ((unsigned)q & 1u)));
+  }
+  return __uint_as_float(sign | f);
+}
+__device__ __forceinline__ double f2d(float x) {
+  const unsigned f = __float_as_uint(x);
+  const unsigned sign = f & 0x80000000u, e = (f >> 23) & 0xFFu, m = f & 0x7FFFFFu;
+  unsigned hi, lo;
+  if (e - 1u <= 253u) {  // normal
+    hi = sign | ((e + 896u) << 20) | (m >> 3);
+    lo = m << 29;
+  } else if (e == 255u) {  // infinity, NaN (payload kept)
+    hi = sign | 0x7FF00000u | (m >> 3);
+    lo = m << 29;
+  } else if (m == 0u) {  // zero
+    hi = sign;
+    lo = 0u;
+  } else {  // subnormal: m * 2^-149 with the leading bit at position p
+    const int p = 31 - __clz((int)m);
+    const unsigned long long frac = ((unsigned long long)m << (52 - p)) & 0xFFFFFFFFFFFFFull;
+    hi = sign | ((unsigned)(p + 874) << 20) | (unsigned)(frac >> 32);
+    lo = (unsigned)frac;
+  }
+  return __hiloint2double((int)hi, (int)lo);
 }
 
 // Eight lanes per cell (eight-corner-matrix model). Lane a (corner offset bits) of an
@@ -290,7 +379,7 @@ __device__ __forceinline__ void block_sum_f2(F2 (&v)[NV], double (&out)[NV], dou
 // All 32 lanes of the warp must call this together (the state loop runs to the
 // warp's largest state count). Returns the cell energy (same in the 8 lanes) and
 // the gradient g of vertex a.
-template <typename T>
+template <typename T, bool SIMPLE = false>
 __device__ __forceinline__ T cell8_eval(const T (&du)[3], int a, const TypeParams<T>& tpl, bool valid, T (&g)[3]) {
   // edge (vertex a -> neighbour a^(1<<d)) displacement differences, oriented lo -> hi
   T ed[3][3];
@@ -316,7 +405,7 @@ __device__ __forceinline__ T cell8_eval(const T (&du)[3], int a, const TypeParam
     for (int d = 0; d < 3; ++d)
 #pragma unroll
       for (int x = 0; x < 3; ++x) W[d * 3 + x] = p.B[d * 3 + x] + ed[d][x];
-    T Es = state_energy_grad<T>(W, p, T(0.125) * p.v0, GW);
+    T Es = state_energy_grad<T, SIMPLE>(W, p, T(0.125) * p.v0, GW);
     Es += __shfl_xor_sync(0xffffffffu, Es, 1);
     Es += __shfl_xor_sync(0xffffffffu, Es, 2);
     Es += __shfl_xor_sync(0xffffffffu, Es, 4);

@@ -303,7 +303,7 @@ struct Engine {
       if (h->structured) k_eng_gather<double, true><<<nb, kET, 0, st>>>(t, (const double*)h->d_G, gs);
       else k_eng_gather<double, false><<<nb, kET, 0, st>>>(t, (const double*)h->d_G, gs);
     }
-    k_eng_energy<<<1, kET, 0, st>>>(h->d_cpart, cell_blocks(h), ctl);
+    k_eng_energy<<<1, kET, 0, st>>>(h->d_cpart, cell_grid(h), ctl);
   }
   void baro_half() {
     ctlop(CT_BARO_VEL);

@@ -20,6 +20,9 @@ struct mm_handle {
   int prec = MM_PREC_FP64;
   int ntypes = 0;
   int num_sms = 0;
+  int simple = 0;  // all rest matrices diagonal and all stress maps cubic (exactly)
+  int cell_occ[2] = {0, 0};  // resident cell-kernel blocks per SM (general, simple); 0 = not queried
+  int node_occ[2] = {0, 0};  // resident node-kernel blocks per SM (no thermostat, Langevin)
   mm::TypeTable tt[MM_MAX_TYPES];
   double rvecs[9] = {0};
   double L[9] = {0};
@@ -65,16 +68,38 @@ struct mm_handle {
 };
 
 namespace mm {
+// 1 if every (type, state) has a diagonal h0 and a cubic-form stress map A.
+inline int tables_are_simple(const TypeTable* tt, int ntypes) {
+  for (int t = 0; t < ntypes; ++t)
+    for (int s = 0; s < MM_MAX_STATES; ++s) {
+      const StateTable& st = tt[t].s[s];
+      const double* h = st.h0;
+      if (h[1] != 0.0 || h[2] != 0.0 || h[3] != 0.0 || h[5] != 0.0 || h[6] != 0.0 || h[7] != 0.0) return 0;
+      const double* A = st.A;
+      const double a = A[0], b = A[1], c = A[21];
+      for (int p = 0; p < 6; ++p)
+        for (int q = 0; q < 6; ++q) {
+          double want = 0.0;
+          if (p < 3 && q < 3) want = (p == q) ? a : b;
+          else if (p == q) want = c;
+          if (A[p * 6 + q] != want) return 0;
+        }
+    }
+  return 1;
+}
 void set_error(const std::string& s);
 const char* last_error();
-int cell_blocks(const mm_handle* h);
-int node_blocks(const mm_handle* h);
+int cell_blocks(const mm_handle* h);  // upper bound of the cell grid (partials buffer size)
+int node_blocks(const mm_handle* h);  // upper bound of the node grid (partials buffer size)
+int cell_grid(mm_handle* h);          // cell grid of a launch: resident blocks x SMs, capped
+int node_grid(mm_handle* h, int thermo);
 void launch_cells(mm_handle* h, cudaStream_t st, double* ecell);
 void launch_pos_to_state(mm_handle* h, const double* pos, cudaStream_t st);
 void launch_state_to_pos(mm_handle* h, double* pos, cudaStream_t st);
 void launch_gather(mm_handle* h, double* gpos, int* flag, cudaStream_t st);
 void launch_finalize(mm_handle* h, double* energy, double* vtens, int* flag, cudaStream_t st);
 void launch_aos_to_soa(int N, const double* a, double* s, cudaStream_t st);
+void launch_selftest_convert(const double* din, float* dout, const float* fin, double* fout, int n, cudaStream_t st);
 void launch_soa_to_aos(int N, const double* s, double* a, cudaStream_t st);
 void launch_md_nodes(mm_handle* h, double dt, double c1, uint64_t seed, int64_t step, int64_t noise_step0, int finish,
                      int start, int thermo, const double* noise, double* record, double* gpos_out, cudaStream_t st);

@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(kCellThreads) k_cells(Topo t, const TypeTable*
 constexpr int kCell8Threads = 256;
 constexpr int kCell8Cells = kCell8Threads / 8;
 
-template <typename T, bool STRUCT>
+template <typename T, bool STRUCT, bool SIMPLE>
 __global__ void __launch_bounds__(kCell8Threads) k_cells8(Topo t, const TypeTable* __restrict__ tt, int ntypes,
                                                           const double* __restrict__ box, const T* __restrict__ disp,
                                                           T* __restrict__ G, double* __restrict__ ecell,
@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(kCell8Threads) k_cells8(Topo t, const TypeTabl
     ty = t.cell_type[cell];
   }
   T g[3];
-  const T Ecell = cell8_eval<T>(du, a, tp[ty], valid, g);
+  const T Ecell = cell8_eval<T, SIMPLE>(du, a, tp[ty], valid, g);
   // stage corner gradients: tile[(corner*3 + x)][cl]
   const int corner = bits_to_corner(a);
 #pragma unroll
@@ -407,6 +407,8 @@ __global__ void k_finalize(const double* __restrict__ cpart, int nblk, double* _
 struct MDArgs {
   double dt;
   double c1;            // Langevin exp(-dt / (2 timecon))
+  double cv;            // velocity factor of the step part run (FP32-cell path): c1^2, c1 or 1
+  float hf, c1f;        // dt / 2 and the thermostat factor (1 without one) in FP32
   uint64_t seed;
   int64_t step;         // step being finished (1-based); the next one is step+1
   int64_t noise_step0;  // step index of noise[0]
@@ -416,7 +418,7 @@ struct MDArgs {
 
 // One thread per node: gather, kick, thermostat, drift, and per-step observables.
 template <typename T, bool STRUCT, int THERMO>
-__global__ void __launch_bounds__(kNodeThreads) k_md_nodes(Topo t, MDArgs p, const T* __restrict__ G,
+__global__ void __launch_bounds__(kNodeThreads, 4) k_md_nodes(Topo t, MDArgs p, const T* __restrict__ G,
                                                            double* __restrict__ u, double* __restrict__ v,
                                                            T* __restrict__ disp, const double* __restrict__ mass,
                                                            const double* __restrict__ invm, const double* __restrict__ c2,
@@ -427,14 +429,19 @@ __global__ void __launch_bounds__(kNodeThreads) k_md_nodes(Topo t, MDArgs p, con
                                                            const float4* __restrict__ nodef) {
   __shared__ double red[kNodePart * (kNodeThreads / 32)];
   __shared__ bool last;
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
   // per-node observables: FP64 for an FP64 handle; for an FP32 handle in FP32, summed
   // per warp with compensated FP32 and per block in FP64
   typedef typename std::conditional<sizeof(T) == 8, double, float>::type R;
+  typedef typename std::conditional<sizeof(T) == 8, double, F2>::type Acc;
+  Acc accum[kNodePart];
+#pragma unroll
+  for (int i = 0; i < kNodePart; ++i) accum[i] = Acc{};
+  // grid-stride over the nodes (the grid holds as many blocks as are resident at once)
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < t.N; n += gridDim.x * blockDim.x) {
   R obs[kNodePart];
 #pragma unroll
   for (int i = 0; i < kNodePart; ++i) obs[i] = R(0);
-  if (sizeof(T) == 4 && n < t.N) {
+  if (sizeof(T) == 4) {
     // FP32 cells: the velocity and position increments of the whole step are formed in
     // FP32, the state update itself is FP64:
     //   v' = cv v + q,  u' = u + dt v'
@@ -445,19 +452,19 @@ __global__ void __launch_bounds__(kNodeThreads) k_md_nodes(Topo t, MDArgs p, con
     T s[3];
     gather_node<T, STRUCT>(t, G, n, s);
     const float4 nf = nodef[n];  // mass, 1/mass, Langevin amplitude
-    const float hf = (float)(0.5 * p.dt), c1f = (float)p.c1;
+    const float hf = p.hf;
     float af[3], n1[3] = {0.f, 0.f, 0.f}, n2[3] = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int x = 0; x < 3; ++x) af[x] = -(float)s[x] * nf.y;
     if (gpos_out)
 #pragma unroll
-      for (int x = 0; x < 3; ++x) gpos_out[3 * n + x] = (double)s[x];
+      for (int x = 0; x < 3; ++x) gpos_out[3 * n + x] = f2d(s[x]);
     if (THERMO == MM_THERMO_LANGEVIN) {
       if (p.finish) {
         if (noise) {
           const size_t base = ((size_t)(p.step - p.noise_step0) * 2 + 1) * (size_t)t.N * 3;
 #pragma unroll
-          for (int x = 0; x < 3; ++x) n1[x] = nf.z * (float)noise[base + 3 * n + x];
+          for (int x = 0; x < 3; ++x) n1[x] = nf.z * d2f_rn(noise[base + 3 * n + x]);
         } else {
           float zf[3];
           normal3(p.seed, (uint32_t)n, (uint32_t)p.step, 1u, zf);
@@ -469,7 +476,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_md_nodes(Topo t, MDArgs p, con
         if (noise) {
           const size_t base = ((size_t)(p.step + 1 - p.noise_step0) * 2 + 0) * (size_t)t.N * 3;
 #pragma unroll
-          for (int x = 0; x < 3; ++x) n2[x] = nf.z * (float)noise[base + 3 * n + x];
+          for (int x = 0; x < 3; ++x) n2[x] = nf.z * d2f_rn(noise[base + 3 * n + x]);
         } else {
           float zf[3];
           normal3(p.seed, (uint32_t)n, (uint32_t)(p.step + 1), 0u, zf);
@@ -478,13 +485,13 @@ __global__ void __launch_bounds__(kNodeThreads) k_md_nodes(Topo t, MDArgs p, con
         }
       }
     }
-    const float c1 = (THERMO == MM_THERMO_LANGEVIN) ? c1f : 1.0f;
+    const float c1 = (THERMO == MM_THERMO_LANGEVIN) ? p.c1f : 1.0f;
     double vv[3];
     float vf[3];
 #pragma unroll
     for (int x = 0; x < 3; ++x) {
       vv[x] = v[x * t.N + n];
-      vf[x] = (float)vv[x];
+      vf[x] = d2f_rn(vv[x]);
     }
     const float mf = nf.x;
     if (p.finish) {
@@ -494,7 +501,8 @@ __global__ void __launch_bounds__(kNodeThreads) k_md_nodes(Topo t, MDArgs p, con
 #pragma unroll
       for (int x = 0; x < 3; ++x) vf[x] = c1 * vf[x] + n1[x];
     }
-    obs[1] = 0.5f * mf * (vf[0] * vf[0] + vf[1] * vf[1] + vf[2] * vf[2]);
+    // obs[1] (kinetic energy between the two halves) is 0.5 * (obs[3] + obs[4] + obs[5])
+    // and is formed from those totals in the block sum below
     obs[3] = mf * vf[0] * vf[0];
     obs[4] = mf * vf[1] * vf[1];
     obs[5] = mf * vf[2] * vf[2];
@@ -507,37 +515,33 @@ __global__ void __launch_bounds__(kNodeThreads) k_md_nodes(Topo t, MDArgs p, con
       obs[2] = 0.5f * mf * (vf[0] * vf[0] + vf[1] * vf[1] + vf[2] * vf[2]);
     }
     if (p.finish || p.start) {
-      double cv;
+      const double cv = p.cv;
       float q[3];
       if (p.finish && p.start) {
-        cv = p.c1 * p.c1;
-        if (THERMO != MM_THERMO_LANGEVIN) cv = 1.0;
         const float cc = c1 * c1;
 #pragma unroll
         for (int x = 0; x < 3; ++x) q[x] = (cc + 1.0f) * hf * af[x] + c1 * n1[x] + n2[x];
       } else if (p.finish) {
-        cv = (THERMO == MM_THERMO_LANGEVIN) ? p.c1 : 1.0;
 #pragma unroll
         for (int x = 0; x < 3; ++x) q[x] = c1 * hf * af[x] + n1[x];
       } else {
-        cv = (THERMO == MM_THERMO_LANGEVIN) ? p.c1 : 1.0;
 #pragma unroll
         for (int x = 0; x < 3; ++x) q[x] = hf * af[x] + n2[x];
       }
 #pragma unroll
       for (int x = 0; x < 3; ++x) {
-        vv[x] = cv * vv[x] + (double)q[x];
+        vv[x] = fma(cv, vv[x], f2d(q[x]));
         v[x * t.N + n] = vv[x];
       }
       if (p.start)
 #pragma unroll
         for (int x = 0; x < 3; ++x) {
-          const double un = u[x * t.N + n] + p.dt * vv[x];
+          const double un = fma(p.dt, vv[x], u[x * t.N + n]);
           u[x * t.N + n] = un;
-          disp[x * t.N + n] = (T)un;
+          disp[x * t.N + n] = d2f_rn(un);
         }
     }
-  } else if (sizeof(T) == 8 && n < t.N) {
+  } else {
     T s[3];
     gather_node<T, STRUCT>(t, G, n, s);
     const double m = mass[n], im = invm[n];
@@ -617,16 +621,33 @@ __global__ void __launch_bounds__(kNodeThreads) k_md_nodes(Topo t, MDArgs p, con
 #pragma unroll
     for (int x = 0; x < 3; ++x) v[x * t.N + n] = vv[x];
   }
+  if constexpr (sizeof(T) == 8) {
+#pragma unroll
+    for (int i = 0; i < kNodePart; ++i) accum[i] += obs[i];
+  } else {
+#pragma unroll
+    for (int i = 0; i < kNodePart; ++i) accum[i] = f2_add(accum[i], F2{(float)obs[i], 0.0f});
+  }
+  }  // nodes
   double tot[kNodePart];
   if constexpr (sizeof(T) == 8) {
 #pragma unroll
-    for (int i = 0; i < kNodePart; ++i) tot[i] = obs[i];
+    for (int i = 0; i < kNodePart; ++i) tot[i] = accum[i];
     block_sum<kNodePart>(tot, red);
   } else {
-    F2 acc[kNodePart];
+    // accum[1] is not summed: thread 0 forms it from the kinetic tensor's diagonal
+    F2 acc[kNodePart - 1];
+    acc[0] = accum[0];
 #pragma unroll
-    for (int i = 0; i < kNodePart; ++i) acc[i] = F2{(float)obs[i], 0.0f};
-    block_sum_f2<kNodePart>(acc, tot, red);
+    for (int i = 2; i < kNodePart; ++i) acc[i - 1] = accum[i];
+    double t8[kNodePart - 1];
+    block_sum_f2<kNodePart - 1>(acc, t8, red);
+    if (threadIdx.x == 0) {
+      tot[0] = t8[0];
+#pragma unroll
+      for (int i = 2; i < kNodePart; ++i) tot[i] = t8[i - 1];
+      tot[1] = 0.5 * (tot[3] + tot[4] + tot[5]);
+    }
   }
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -739,14 +760,34 @@ static size_t cell_smem(const mm_handle* h) {
   return ((tp + 15) / 16) * 16 + sizeof(double) * kCellPart * (kCellThreads / 32);
 }
 
+template <typename K>
+static int occupancy_of(K kern, int threads, size_t smem) {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads, smem) != cudaSuccess || nb < 1) {
+    (void)cudaGetLastError();
+    nb = 1;
+  }
+  return nb;
+}
+
+template <typename T, bool STRUCT>
+static int cell8_occupancy(const mm_handle* h) {
+  return h->simple ? occupancy_of(k_cells8<T, STRUCT, true>, kCell8Threads, cell_smem(h))
+                   : occupancy_of(k_cells8<T, STRUCT, false>, kCell8Threads, cell_smem(h));
+}
+
 template <typename T, int MODEL, bool STRUCT>
 static void launch_cells_t(mm_handle* h, cudaStream_t st, double* ecell) {
   Topo t;
   topo_of(h, t);
-  const int nblk = cell_blocks(h);
+  const int nblk = cell_grid(h);
   if constexpr (MODEL == 1) {
-    k_cells8<T, STRUCT><<<nblk, kCell8Threads, cell_smem(h), st>>>(
-        t, h->d_tt, h->ntypes, h->d_box, (const T*)h->d_disp, (T*)h->d_G, ecell, h->d_cpart);
+    if (h->simple)
+      k_cells8<T, STRUCT, true><<<nblk, kCell8Threads, cell_smem(h), st>>>(
+          t, h->d_tt, h->ntypes, h->d_box, (const T*)h->d_disp, (T*)h->d_G, ecell, h->d_cpart);
+    else
+      k_cells8<T, STRUCT, false><<<nblk, kCell8Threads, cell_smem(h), st>>>(
+          t, h->d_tt, h->ntypes, h->d_box, (const T*)h->d_disp, (T*)h->d_G, ecell, h->d_cpart);
   } else {
     k_cells<T, MODEL, STRUCT><<<nblk, kCellThreads, cell_smem(h), st>>>(
         t, h->d_tt, h->ntypes, h->d_box, (const T*)h->d_disp, (T*)h->d_G, ecell, h->d_cpart);
@@ -780,6 +821,20 @@ int cell_blocks(const mm_handle* h) {
 }
 int node_blocks(const mm_handle* h) { return (h->N + kNodeThreads - 1) / kNodeThreads; }
 
+// The nanocell kernel grid-strides over groups of cells with exactly as many blocks
+// as fit on the GPU at once (so no partial second wave), at most 4 per SM.
+int cell_grid(mm_handle* h) {
+  if (h->model != MM_MODEL_NANOCELL) return cell_blocks(h);
+  int& occ = h->cell_occ[h->simple ? 1 : 0];
+  if (occ == 0) {
+    if (h->prec == MM_PREC_FP32) occ = h->structured ? cell8_occupancy<float, true>(h) : cell8_occupancy<float, false>(h);
+    else occ = h->structured ? cell8_occupancy<double, true>(h) : cell8_occupancy<double, false>(h);
+  }
+  const int groups = (h->M + kCell8Cells - 1) / kCell8Cells;
+  const int cap = (h->num_sms > 0 ? h->num_sms : 152) * (occ < 4 ? occ : 4);
+  return groups < cap ? groups : cap;
+}
+
 void launch_pos_to_state(mm_handle* h, const double* pos, cudaStream_t st) {
   Topo t;
   topo_of(h, t);
@@ -810,7 +865,17 @@ void launch_gather(mm_handle* h, double* gpos, int* flag, cudaStream_t st) {
 }
 
 void launch_finalize(mm_handle* h, double* energy, double* vtens, int* flag, cudaStream_t st) {
-  k_finalize<<<1, 256, 0, st>>>(h->d_cpart, cell_blocks(h), energy, vtens, flag);
+  k_finalize<<<1, 256, 0, st>>>(h->d_cpart, cell_grid(h), energy, vtens, flag);
+}
+
+__global__ void k_selftest_convert(const double* din, float* dout, const float* fin, double* fout, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  dout[i] = d2f_rn(din[i]);
+  fout[i] = f2d(fin[i]);
+}
+void launch_selftest_convert(const double* din, float* dout, const float* fin, double* fout, int n, cudaStream_t st) {
+  if (n > 0) k_selftest_convert<<<(n + 255) / 256, 256, 0, st>>>(din, dout, fin, fout, n);
 }
 
 void launch_aos_to_soa(int N, const double* a, double* s, cudaStream_t st) {
@@ -825,9 +890,21 @@ static void launch_md_nodes_t(mm_handle* h, const MDArgs& a, const double* noise
                               cudaStream_t st) {
   Topo t;
   topo_of(h, t);
-  k_md_nodes<T, STRUCT, THERMO><<<node_blocks(h), kNodeThreads, 0, st>>>(
+  int& occ = h->node_occ[THERMO == MM_THERMO_LANGEVIN ? 1 : 0];
+  if (occ == 0) occ = occupancy_of(k_md_nodes<T, STRUCT, THERMO>, kNodeThreads, 0);
+  k_md_nodes<T, STRUCT, THERMO><<<node_grid(h, THERMO), kNodeThreads, 0, st>>>(
       t, a, (const T*)h->d_G, h->d_u, h->d_v, (T*)h->d_disp, h->d_mass, h->d_invm, h->d_c2, noise, h->d_npart,
-      h->d_cpart, cell_blocks(h), h->d_ticket, h->d_carry, record, gpos_out, h->d_nodef);
+      h->d_cpart, cell_grid(h), h->d_ticket, h->d_carry, record, gpos_out, h->d_nodef);
+}
+
+// Node grid: as many blocks as fit at once (grid-stride over the nodes), at most one
+// block per 256 nodes.
+int node_grid(mm_handle* h, int thermo) {
+  const int occ = h->node_occ[thermo == MM_THERMO_LANGEVIN ? 1 : 0];
+  const int nb = node_blocks(h);
+  if (occ <= 0) return nb;
+  const int cap = (h->num_sms > 0 ? h->num_sms : 152) * occ;
+  return nb < cap ? nb : cap;
 }
 
 template <typename T>
@@ -852,6 +929,10 @@ void launch_md_nodes(mm_handle* h, double dt, double c1, uint64_t seed, int64_t 
   a.noise_step0 = noise_step0;
   a.finish = finish;
   a.start = start;
+  const bool lang = thermo == MM_THERMO_LANGEVIN;
+  a.cv = lang ? ((finish && start) ? c1 * c1 : c1) : 1.0;
+  a.hf = (float)(0.5 * dt);
+  a.c1f = lang ? (float)c1 : 1.0f;
   if (h->prec == MM_PREC_FP32) launch_md_nodes_p<float>(h, a, thermo, noise, record, gpos_out, st);
   else launch_md_nodes_p<double>(h, a, thermo, noise, record, gpos_out, st);
 }

@@ -182,6 +182,7 @@ extern "C" mm_status mm_compute_noalloc(const int32_t* lattice_shape, const int3
       tt[t].s[st].df = free_energy[slot];
     }
   }
+  h.simple = mm::tables_are_simple(tt, ntypes);
   double L[9];
   for (int d = 0; d < 3; ++d)
     for (int x = 0; x < 3; ++x) L[3 * d + x] = rvecs[3 * d + x] / lattice_shape[d];
