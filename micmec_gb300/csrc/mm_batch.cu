@@ -77,19 +77,8 @@ template <typename T>
 __device__ void load_tables(Shared<T>& sh, const TypeTable* tt, int ntypes, const double* L) {
   for (int idx = threadIdx.x; idx < ntypes * MM_MAX_STATES; idx += blockDim.x) {
     const int ty = idx / MM_MAX_STATES, s = idx % MM_MAX_STATES;
-    const StateTable& src = tt[ty].s[s];
-    StateParams<T>& dst = sh.tp[ty].s[s];
-    for (int i = 0; i < 9; ++i) {
-      dst.hinv[i] = (T)src.hinv[i];
-      dst.B[i] = (T)(L[i] - src.h0[i]);
-    }
-    for (int i = 0; i < 36; ++i) dst.A[i] = (T)src.A[i];
-    dst.v0 = (T)src.v0;
-    dst.df = (T)src.df;
-    if (s == 0) {
-      sh.tp[ty].kT = (T)tt[ty].kT;
-      sh.tp[ty].nstates = tt[ty].nstates;
-    }
+    fill_state_params<T>(sh.tp[ty].s[s], tt[ty].s[s], L);
+    if (s == 0) fill_type_scalars<T>(sh.tp[ty], tt[ty]);
   }
   if (threadIdx.x < 9) sh.L[threadIdx.x] = (T)L[threadIdx.x];
 }
@@ -131,7 +120,7 @@ __device__ void forces(const BArgs& a, Shared<T>& sh, const BSys& sy) {
   const int M = sy.M;
   double acc[10];
   for (int i = 0; i < 10; ++i) acc[i] = 0.0;
-  if (MODEL == 1) {
+  if (MODEL >= 1) {  // eight corner matrices; MODEL 2: diagonal h0 and cubic stress maps
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, av = threadIdx.x & 7;
     const int ngroups = (M + 3) / 4;
     const int nw = blockDim.x >> 5;
@@ -147,7 +136,7 @@ __device__ void forces(const BArgs& a, Shared<T>& sh, const BSys& sy) {
         ty = a.ctype[sy.off + cell];
       }
       T g[3];
-      const T E = cell8_eval<T>(du, av, sh.tp[ty], valid, g);
+      const T E = cell8_eval<T, MODEL == 2>(du, av, sh.tp[ty], valid, g);
       T d0[3];
       for (int y = 0; y < 3; ++y) d0[y] = __shfl_sync(0xffffffffu, du[y], lane & ~7);  // all lanes
       if (valid) {
@@ -656,6 +645,7 @@ void bstress_map(const double* C, double* A) {
 
 struct mm_batch {
   int nsys = 0, model = 1, prec = 0, ntypes = 0, num_sms = 0;
+  int simple = 0;  // every rest matrix diagonal and every stress map cubic (exactly)
   long long Ntot = 0;
   int bt = 256;        // CTA size
   int nctas = 0;       // persistent CTAs
@@ -750,7 +740,8 @@ void launch_md_t(mm_batch* b, const BMD& p, cudaStream_t st) {
 
 void launch_md(mm_batch* b, const BMD& p, cudaStream_t st) {
   if (b->prec == MM_PREC_FP32) {
-    if (b->model == MM_MODEL_NANOCELL) launch_md_t<float, 1>(b, p, st);
+    if (b->model == MM_MODEL_NANOCELL && b->simple) launch_md_t<float, 2>(b, p, st);
+    else if (b->model == MM_MODEL_NANOCELL) launch_md_t<float, 1>(b, p, st);
     else launch_md_t<float, 0>(b, p, st);
   } else {
     if (b->model == MM_MODEL_NANOCELL) launch_md_t<double, 1>(b, p, st);
@@ -767,7 +758,8 @@ void launch_relax_t(mm_batch* b, int max_iter, double gtol, cudaStream_t st) {
 
 void launch_relax(mm_batch* b, int max_iter, double gtol, cudaStream_t st) {
   if (b->prec == MM_PREC_FP32) {
-    if (b->model == MM_MODEL_NANOCELL) launch_relax_t<float, 1>(b, max_iter, gtol, st);
+    if (b->model == MM_MODEL_NANOCELL && b->simple) launch_relax_t<float, 2>(b, max_iter, gtol, st);
+    else if (b->model == MM_MODEL_NANOCELL) launch_relax_t<float, 1>(b, max_iter, gtol, st);
     else launch_relax_t<float, 0>(b, max_iter, gtol, st);
   } else {
     if (b->model == MM_MODEL_NANOCELL) launch_relax_t<double, 1>(b, max_iter, gtol, st);
@@ -839,6 +831,7 @@ mm_status mm_batch_create(int nsys, const int32_t* shapes, const int32_t* cell_t
       tt.s[st].df = free_energy[slot];
     }
   }
+  b->simple = mm::tables_are_simple(b->tt, ntypes);
   int dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, dev);

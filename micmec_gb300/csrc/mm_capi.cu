@@ -194,7 +194,7 @@ mm_status mm_create(int nnodes, int ncells, const int32_t* node_coords, const in
             dev_alloc(&h->d_u, 3 * (size_t)N) && dev_alloc(&h->d_v, 3 * (size_t)N) &&
             dev_alloc((char**)&h->d_disp, 3 * (size_t)N * esz) && dev_alloc((char**)&h->d_G, 24 * (size_t)M * esz) &&
             dev_alloc(&h->d_ecell, M) && dev_alloc(&h->d_cpart, (size_t)ncb * 10) &&
-            dev_alloc(&h->d_npart, (size_t)nnb * 9) && dev_alloc(&h->d_ticket, 1) && dev_alloc(&h->d_carry, 4) &&
+            dev_alloc(&h->d_npart, (size_t)nnb * 9 + 16) && dev_alloc(&h->d_ticket, 1) && dev_alloc(&h->d_carry, 4) &&
             dev_alloc(&h->d_io, 9 * (size_t)N + 64) && dev_alloc(&h->d_flag, 1) && dev_alloc(&h->d_nodef, N);
   if (ok && !structured)
     ok = dev_alloc(&h->d_cell_nodes, 8 * (size_t)M) && dev_alloc(&h->d_node_cells, 8 * (size_t)N) &&
@@ -471,6 +471,17 @@ mm_status mm_md_time_kernels(mm_handle* h, int nsteps, void* flush_buf, size_t f
   return MM_OK;
 }
 
+// Device address of a pinned (page-locked, mapped) host buffer, or nullptr for any
+// other memory.
+static void* mapped_host_ptr(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  return (a.type == cudaMemoryTypeHost) ? a.devicePointer : nullptr;
+}
+
 mm_status mm_md_step_host(mm_handle* h, double* pos, double* vel, double* gpos, double* record, double timestep,
                           int thermo, double temp, double timecon, uint64_t seed, int64_t step) {
   if (!h || !pos || !vel || !gpos) return MM_ERR_ARG;
@@ -478,6 +489,29 @@ mm_status mm_md_step_host(mm_handle* h, double* pos, double* vel, double* gpos, 
   mm_status s = md_prepare(h, timestep, thermo, temp, timecon, seed, st);
   if (s != MM_OK) return s;
   const size_t n3 = 3 * (size_t)h->N;
+  // carry (pre-thermostat correction) is produced by the begin kernel only through ekin;
+  // the host-buffer step reports the post-thermostat correction alone.
+  MM_CUDA(cudaMemsetAsync(h->d_carry, 0, sizeof(double), st));
+  double* m_pos = (double*)mapped_host_ptr(pos);
+  double* m_vel = (double*)mapped_host_ptr(vel);
+  double* m_gpos = (double*)mapped_host_ptr(gpos);
+  double* m_rec = record ? (double*)mapped_host_ptr(record) : nullptr;
+  if (m_pos && m_vel && m_gpos) {
+    // pinned caller buffers: the kernels read and write them in place over the host
+    // link (the begin kernel reads pos/vel/gpos, the node kernel writes the new
+    // gradient and the record, the end kernel writes pos/vel); no staging copies
+    double* d_rec = m_rec ? m_rec : h->d_io + 3 * n3;
+    mm::launch_md_host_begin(h, h->md.dt, h->md.c1, seed, step, thermo, m_pos, m_vel, m_gpos, st);
+    mm::launch_cells(h, st, nullptr);
+    mm::launch_md_nodes(h, h->md.dt, h->md.c1, seed, step, step, 1, 0, thermo, nullptr, d_rec, m_gpos, st);
+    mm::launch_md_host_end(h, m_pos, m_vel, st);
+    MM_CUDA(cudaGetLastError());
+    if (record && !m_rec)
+      MM_CUDA(cudaMemcpyAsync(record, d_rec, MM_REC_LEN * sizeof(double), cudaMemcpyDeviceToHost, st));
+    MM_CUDA(cudaStreamSynchronize(st));
+    return MM_OK;
+  }
+  // pageable caller buffers: staged through device buffers
   double* d_pos = h->d_io;
   double* d_gpos = h->d_io + n3;
   double* d_vel = h->d_io + 2 * n3;
@@ -485,16 +519,10 @@ mm_status mm_md_step_host(mm_handle* h, double* pos, double* vel, double* gpos, 
   MM_CUDA(cudaMemcpyAsync(d_pos, pos, n3 * sizeof(double), cudaMemcpyHostToDevice, st));
   MM_CUDA(cudaMemcpyAsync(d_vel, vel, n3 * sizeof(double), cudaMemcpyHostToDevice, st));
   MM_CUDA(cudaMemcpyAsync(d_gpos, gpos, n3 * sizeof(double), cudaMemcpyHostToDevice, st));
-  mm::launch_pos_to_state(h, d_pos, st);
-  mm::launch_aos_to_soa(h->N, d_vel, h->d_v, st);
-  // carry (pre-thermostat correction) is produced by the begin kernel only through ekin;
-  // the host-buffer step reports the post-thermostat correction alone.
-  MM_CUDA(cudaMemsetAsync(h->d_carry, 0, sizeof(double), st));
-  mm::launch_md_begin_gpos(h, h->md.dt, h->md.c1, seed, step, thermo, d_gpos, nullptr, st);
+  mm::launch_md_host_begin(h, h->md.dt, h->md.c1, seed, step, thermo, d_pos, d_vel, d_gpos, st);
   mm::launch_cells(h, st, nullptr);
   mm::launch_md_nodes(h, h->md.dt, h->md.c1, seed, step, step, 1, 0, thermo, nullptr, d_rec, d_gpos, st);
-  mm::launch_state_to_pos(h, d_pos, st);
-  mm::launch_soa_to_aos(h->N, h->d_v, d_vel, st);
+  mm::launch_md_host_end(h, d_pos, d_vel, st);
   MM_CUDA(cudaGetLastError());
   MM_CUDA(cudaMemcpyAsync(pos, d_pos, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
   MM_CUDA(cudaMemcpyAsync(vel, d_vel, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));

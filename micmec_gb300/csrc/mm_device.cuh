@@ -30,21 +30,26 @@ __host__ __device__ constexpr int bits_to_corner(int b) {
 }
 __host__ __device__ constexpr int corner_to_bits(int k) { return k == 3 ? 4 : (k == 4 ? 3 : k); }
 
-// Per (type, state) parameters in the precision T of the cell arithmetic.
+// Per (type, state) parameters in the precision T of the cell arithmetic. The first
+// 20 values are what the cubic form reads (16-byte aligned, vector loads).
 template <typename T>
 struct __align__(16) StateParams {
-  T A[36];     // 6x6: symmetric stress (Voigt 00,11,22,12,02,01) = A . strain (first: 16-byte aligned rows)
-  T hinv[9];   // h0^-1, row-major
   T B[9];      // L - h0 (rows), for the current lattice matrix L
   T v0;        // det(h0)
   T df;        // state free energy
-  T pad[2];
+  T hd[3];     // diagonal of h0^-1 (cubic form)
+  T cub[3];    // A00 - A01, A01, A33 (cubic form)
+  T pad0[3];
+  T A[36];     // 6x6: symmetric stress (Voigt 00,11,22,12,02,01) = A . strain
+  T hinv[9];   // h0^-1, row-major
+  T pad1[3];
 };
 
 template <typename T>
 struct TypeParams {
   StateParams<T> s[MM_MAX_STATES];
   T kT;        // boltzmann * effective temperature
+  T lkT;       // log2(e) / kT
   int nstates;
 };
 
@@ -63,6 +68,36 @@ struct TypeTable {
   int pad;
 };
 
+// Cell-precision copy of one (type, state) entry for the lattice matrix L
+// (B = L - h0 formed in FP64, then rounded).
+template <typename T>
+__device__ __forceinline__ void fill_state_params(StateParams<T>& dst, const StateTable& src, const double* L) {
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    dst.hinv[i] = (T)src.hinv[i];
+    dst.B[i] = (T)(L[i] - src.h0[i]);
+  }
+#pragma unroll
+  for (int i = 0; i < 36; ++i) dst.A[i] = (T)src.A[i];
+  dst.v0 = (T)src.v0;
+  dst.df = (T)src.df;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    dst.hd[i] = (T)src.hinv[4 * i];
+    dst.pad0[i] = T(0);
+    dst.pad1[i] = T(0);
+  }
+  dst.cub[0] = (T)(src.A[0] - src.A[1]);
+  dst.cub[1] = (T)src.A[1];
+  dst.cub[2] = (T)src.A[21];
+}
+template <typename T>
+__device__ __forceinline__ void fill_type_scalars(TypeParams<T>& dst, const TypeTable& src) {
+  dst.kT = (T)src.kT;
+  dst.lkT = (T)(1.4426950408889634 / src.kT);
+  dst.nstates = src.nstates;
+}
+
 // Elastic energy of one state and its gradient with respect to the rows of W.
 // W = M - h0 (rows: edge deviations). F = M^T h0^-T = I + D with
 // D[i][k] = sum_j W[j][i] hinv[k][j]; eps = (D + D^T + D^T D)/2;
@@ -78,7 +113,7 @@ __device__ __forceinline__ T state_energy_grad(const T* __restrict__ W, const St
                                                T* __restrict__ GW) {
   T D[9];
   if (SIMPLE) {
-    const T h[3] = {p.hinv[0], p.hinv[4], p.hinv[8]};
+    const T h[3] = {p.hd[0], p.hd[1], p.hd[2]};
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -100,11 +135,11 @@ __device__ __forceinline__ T state_energy_grad(const T* __restrict__ W, const St
   e[5] = h * (D[1] + D[3] + D[0] * D[1] + D[3] * D[4] + D[6] * D[7]);
   T s[6];
   if (SIMPLE) {
-    const T a = p.A[0], b = p.A[1], c = p.A[21];
+    const T amb = p.cub[0], b = p.cub[1], c = p.cub[2];
     const T tr = e[0] + e[1] + e[2];
-    s[0] = (a - b) * e[0] + b * tr;
-    s[1] = (a - b) * e[1] + b * tr;
-    s[2] = (a - b) * e[2] + b * tr;
+    s[0] = amb * e[0] + b * tr;
+    s[1] = amb * e[1] + b * tr;
+    s[2] = amb * e[2] + b * tr;
     s[3] = c * e[3];
     s[4] = c * e[4];
     s[5] = c * e[5];
@@ -131,7 +166,7 @@ __device__ __forceinline__ T state_energy_grad(const T* __restrict__ W, const St
   if (SIMPLE) {
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-      const T sj = scale * p.hinv[j * 4];
+      const T sj = scale * p.hd[j];
 #pragma unroll
       for (int i = 0; i < 3; ++i) GW[j * 3 + i] = sj * GF[i * 3 + j];
     }
@@ -293,11 +328,11 @@ __device__ __forceinline__ void warp_sum_f2(F2 (&v)[NV]) {
 }
 
 // Block sum: compensated FP32 within each warp and across the warps (warp 0 adds the
-// warps' (hi, lo) pairs in fixed order); one FP64 conversion per value per block.
-// Result valid in thread 0. smem must hold NV * (blockDim.x / 32) doubles. Ends
-// without a barrier: a caller that reuses smem afterwards synchronises first.
+// warps' (hi, lo) pairs in fixed order). The totals are left in v of thread 0.
+// smem must hold NV * (blockDim.x / 32) doubles. Ends without a barrier: a caller
+// that reuses smem afterwards synchronises first.
 template <int NV>
-__device__ __forceinline__ void block_sum_f2(F2 (&v)[NV], double (&out)[NV], double* smem) {
+__device__ __forceinline__ void block_sum_f2_pairs(F2 (&v)[NV], double* smem) {
   warp_sum_f2<NV>(v);
   F2* s2 = reinterpret_cast<F2*>(smem);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -316,10 +351,27 @@ __device__ __forceinline__ void block_sum_f2(F2 (&v)[NV], double (&out)[NV], dou
         v[i] = f2_add(v[i], o);
       }
     }
-    if (lane == 0)
-#pragma unroll
-      for (int i = 0; i < NV; ++i) out[i] = (double)v[i].hi + (double)v[i].lo;
   }
+}
+// The same with the totals converted to FP64 in thread 0 (one conversion per value).
+template <int NV>
+__device__ __forceinline__ void block_sum_f2(F2 (&v)[NV], double (&out)[NV], double* smem) {
+  block_sum_f2_pairs<NV>(v, smem);
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int i = 0; i < NV; ++i) out[i] = (double)v[i].hi + (double)v[i].lo;
+}
+
+// Per-block partial sums in global memory, one 8-byte slot per value, value-major
+// (slot v * nblocks + block): FP64 kernels store doubles, FP32 kernels the compensated
+// pair (hi, lo) as two floats. Readers of other blocks' slots (after a fence and a
+// ticket) load through L2.
+__device__ __forceinline__ void store_pair(double* slot, F2 v) {
+  *reinterpret_cast<float2*>(slot) = make_float2(v.hi, v.lo);
+}
+__device__ __forceinline__ F2 load_pair(const double* slot) {
+  const float2 p = __ldcg(reinterpret_cast<const float2*>(slot));
+  return F2{p.x, p.y};
 }
 
 // IEEE 754 binary64 <-> binary32 conversions built from the bit layouts with integer
@@ -370,6 +422,33 @@ __device__ __forceinline__ double f2d(float x) {
   }
   return __hiloint2double((int)hi, (int)lo);
 }
+
+// exp(d / kT) for d <= 0 and log(w) of the state combination. FP32: exp2 of d log2(e)/kT
+// (no division) and log2 times ln 2; FP64: exp and log.
+template <typename T>
+__device__ __forceinline__ T lse_weight(T d, T kT, T lkT) {
+  if constexpr (sizeof(T) == 4) return exp2f(d * lkT);
+  else return exp(d / kT);
+}
+template <typename T>
+__device__ __forceinline__ T lse_log(T w) {
+  if constexpr (sizeof(T) == 4) return log2f(w) * 0.69314718055994531f;
+  else return log(w);
+}
+
+// n / d for 0 <= n < 2^31 by a multiply-high and a shift (Granlund and Montgomery,
+// "Division by invariant integers using multiplication", PLDI 1994, section 4):
+// l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1, n / d = (mulhi(m, n) + n) >> l.
+struct FastDiv {
+  uint32_t m, l;
+};
+inline FastDiv make_fastdiv(uint32_t d) {
+  uint32_t l = 0;
+  while ((1ull << l) < d) ++l;
+  const unsigned long long m = ((1ull << 32) * ((1ull << l) - d)) / d + 1ull;
+  return FastDiv{(uint32_t)m, l};
+}
+__device__ __forceinline__ int fdiv(int n, FastDiv f) { return (int)((__umulhi((uint32_t)n, f.m) + (uint32_t)n) >> f.l); }
 
 // Eight lanes per cell (eight-corner-matrix model). Lane a (corner offset bits) of an
 // aligned 8-lane group holds the displacement du of vertex a; it evaluates corner
@@ -427,13 +506,13 @@ __device__ __forceinline__ T cell8_eval(const T (&du)[3], int a, const TypeParam
 #pragma unroll
         for (int x = 0; x < 3; ++x) g[x] = gs[x];
       } else if (E < m) {
-        const T r = exp((E - m) / kT);
+        const T r = lse_weight<T>(E - m, kT, tpl.lkT);
         wsum = wsum * r + T(1);
 #pragma unroll
         for (int x = 0; x < 3; ++x) g[x] = g[x] * r + gs[x];
         m = E;
       } else {
-        const T w = exp((m - E) / kT);
+        const T w = lse_weight<T>(m - E, kT, tpl.lkT);
         wsum += w;
 #pragma unroll
         for (int x = 0; x < 3; ++x) g[x] += w * gs[x];
@@ -445,7 +524,7 @@ __device__ __forceinline__ T cell8_eval(const T (&du)[3], int a, const TypeParam
     const T inv = T(1) / wsum;
 #pragma unroll
     for (int x = 0; x < 3; ++x) g[x] *= inv;
-    Ecell = m - kT * log(wsum);
+    Ecell = m - kT * lse_log<T>(wsum);
   }
   return Ecell;
 }

@@ -67,13 +67,26 @@ __global__ void k_eng_gather(ETopo t, const T* __restrict__ G, double* __restric
 }
 
 // energy and virial of the last cell kernel (block partials, fixed order) into ctl
+// (FP32 handles: the cell kernel's partials are compensated FP32 pairs)
+template <bool PAIRS>
 __global__ void k_eng_energy(const double* __restrict__ cpart, int nblk, double* __restrict__ ctl) {
   __shared__ double red[10 * (kET / 32)];
   double acc[10];
-  for (int i = 0; i < 10; ++i) acc[i] = 0.0;
-  for (int b = threadIdx.x; b < nblk; b += blockDim.x)
-    for (int i = 0; i < 10; ++i) acc[i] += cpart[b * 10 + i];
-  block_sum<10>(acc, red);
+  if constexpr (PAIRS) {
+    F2 f[10];
+    for (int i = 0; i < 10; ++i) f[i] = F2{0.0f, 0.0f};
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x)
+      for (int i = 0; i < 10; ++i) {
+        const float2 p = __ldcg(reinterpret_cast<const float2*>(cpart + i * nblk + b));
+        f[i] = f2_add(f[i], F2{p.x, p.y});
+      }
+    block_sum_f2<10>(f, acc, red);
+  } else {
+    for (int i = 0; i < 10; ++i) acc[i] = 0.0;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x)
+      for (int i = 0; i < 10; ++i) acc[i] += cpart[i * nblk + b];
+    block_sum<10>(acc, red);
+  }
   if (threadIdx.x == 0) {
     ctl[C_EPOT] = acc[0];
     for (int i = 0; i < 9; ++i) ctl[C_VT + i] = acc[1 + i];
@@ -303,7 +316,8 @@ struct Engine {
       if (h->structured) k_eng_gather<double, true><<<nb, kET, 0, st>>>(t, (const double*)h->d_G, gs);
       else k_eng_gather<double, false><<<nb, kET, 0, st>>>(t, (const double*)h->d_G, gs);
     }
-    k_eng_energy<<<1, kET, 0, st>>>(h->d_cpart, cell_grid(h), ctl);
+    if (h->prec == MM_PREC_FP32) k_eng_energy<true><<<1, kET, 0, st>>>(h->d_cpart, cell_grid(h), ctl);
+    else k_eng_energy<false><<<1, kET, 0, st>>>(h->d_cpart, cell_grid(h), ctl);
   }
   void baro_half() {
     ctlop(CT_BARO_VEL);

@@ -38,24 +38,30 @@ namespace {
 
 constexpr int kCellThreads = 128;
 constexpr int kNodeThreads = 256;
+constexpr int kMDThreads = 1024;  // node-update blocks: one resident block per SM, few partials
 constexpr int kCellPart = 10;  // energy + virial(9)
 constexpr int kNodePart = 9;   // ekin_a, ekin_b, ekin_c, ktens(6)
 
 struct Topo {
   int N, M, structured, nx, ny, nz;
+  FastDiv div_nyz, div_nz;  // / (ny nz), / nz for the implicit lattice index
   const int32_t* cell_nodes;  // [8][M]
   const int32_t* node_cells;  // [8][N]
   const int32_t* node_lat;    // [3][N]
   const uint8_t* cell_type;   // [M]
 };
 
+// (i, j, k) of a node or cell index of the implicit lattice (lexicographic, k fastest)
+__device__ __forceinline__ void split_index(const Topo& t, int n, int& i, int& j, int& k) {
+  i = fdiv(n, t.div_nyz);
+  const int r = n - i * (t.ny * t.nz);
+  j = fdiv(r, t.div_nz);
+  k = r - j * t.nz;
+}
+
 __device__ __forceinline__ void lattice_of(const Topo& t, int n, int& a, int& b, int& c) {
   if (t.structured) {
-    const int nyz = t.ny * t.nz;
-    a = n / nyz;
-    const int r = n - a * nyz;
-    b = r / t.nz;
-    c = r - b * t.nz;
+    split_index(t, n, a, b, c);
   } else {
     a = t.node_lat[n];
     b = t.node_lat[t.N + n];
@@ -87,21 +93,8 @@ template <typename T>
 __device__ void load_params(TypeParams<T>* tp, const TypeTable* tt, int ntypes, const double* box) {
   for (int idx = threadIdx.x; idx < ntypes * MM_MAX_STATES; idx += blockDim.x) {
     const int ty = idx / MM_MAX_STATES, s = idx % MM_MAX_STATES;
-    const StateTable& src = tt[ty].s[s];
-    StateParams<T>& dst = tp[ty].s[s];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) {
-      dst.hinv[i] = (T)src.hinv[i];
-      dst.B[i] = (T)(box[i] - src.h0[i]);
-    }
-#pragma unroll
-    for (int i = 0; i < 36; ++i) dst.A[i] = (T)src.A[i];
-    dst.v0 = (T)src.v0;
-    dst.df = (T)src.df;
-    if (s == 0) {
-      tp[ty].kT = (T)tt[ty].kT;
-      tp[ty].nstates = tt[ty].nstates;
-    }
+    fill_state_params<T>(tp[ty].s[s], tt[ty].s[s], box);
+    if (s == 0) fill_type_scalars<T>(tp[ty], tt[ty]);
   }
 }
 
@@ -167,8 +160,8 @@ __global__ void __launch_bounds__(kCellThreads) k_cells(Topo t, const TypeTable*
   if (cell < t.M) {
     T du[8][3];
     if (STRUCT) {
-      const int nyz = t.ny * t.nz;
-      const int i = cell / nyz, r = cell - i * nyz, j = r / t.nz, k = r - j * t.nz;
+      int i, j, k;
+      split_index(t, cell, i, j, k);
 #pragma unroll
       for (int b = 0; b < 8; ++b) {
         const int node = struct_corner_node(t, i, j, k, b);
@@ -220,6 +213,9 @@ __global__ void __launch_bounds__(kCellThreads) k_cells(Topo t, const TypeTable*
   }
   if constexpr (sizeof(T) == 8) {
     block_sum<kCellPart>(acc, red);
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int i = 0; i < kCellPart; ++i) cpart[i * gridDim.x + blockIdx.x] = acc[i];
   } else {
     F2 f[kCellPart];
 #pragma unroll
@@ -227,11 +223,11 @@ __global__ void __launch_bounds__(kCellThreads) k_cells(Topo t, const TypeTable*
       const float hi = (float)acc[i];
       f[i] = F2{hi, i == 0 ? (float)(acc[i] - (double)hi) : 0.0f};
     }
-    block_sum_f2<kCellPart>(f, acc, red);
-  }
-  if (threadIdx.x == 0)
+    block_sum_f2_pairs<kCellPart>(f, red);
+    if (threadIdx.x == 0)
 #pragma unroll
-    for (int i = 0; i < kCellPart; ++i) cpart[blockIdx.x * kCellPart + i] = acc[i];
+      for (int i = 0; i < kCellPart; ++i) store_pair(cpart + i * gridDim.x + blockIdx.x, f[i]);
+  }
 }
 
 // Eight lanes per cell for the eight-corner-matrix model: lane a (offset bits of
@@ -239,37 +235,48 @@ __global__ void __launch_bounds__(kCellThreads) k_cells(Topo t, const TypeTable*
 // join vertex a to its neighbours a^1, a^2, a^4, whose displacements come from
 // xor-shuffles inside the 8-lane group; state energies are summed with three
 // xor-shuffles; vertex a's gradient collects, for each direction d, the row-d
-// gradient of matrix a and of matrix a^(1<<d) (the same edge). Corner gradients are
-// staged in shared memory and written as contiguous runs of the corner-major
-// layout. Energy and virial are summed per warp in compensated FP32 and per block
-// in FP64.
+// gradient of matrix a and of matrix a^(1<<d) (the same edge). Corner gradients and
+// vertex offsets are staged in shared memory; the gradients are written as
+// contiguous runs of the corner-major layout, and the per-cell virial components
+// sum_a g_a (x) (r_a - r_0) and energies are formed from the staged tiles by one warp
+// per component (warp w: component w; warps 0, 1 also components 8 and 9), so each
+// thread carries one or two running sums (compensated FP32 for FP32 cells) and a
+// block's partial of a component is one warp sum.
 constexpr int kCell8Threads = 256;
 constexpr int kCell8Cells = kCell8Threads / 8;
+static_assert(kCell8Threads == 256 && kCellPart == 10, "component ownership assumes 8 warps and 10 components");
 
 template <typename T, bool STRUCT, bool SIMPLE>
-__global__ void __launch_bounds__(kCell8Threads) k_cells8(Topo t, const TypeTable* __restrict__ tt, int ntypes,
+__global__ void __launch_bounds__(kCell8Threads, sizeof(T) == 4 ? (SIMPLE ? 4 : 3) : 2) k_cells8(Topo t, const TypeTable* __restrict__ tt, int ntypes,
                                                           const double* __restrict__ box, const T* __restrict__ disp,
                                                           T* __restrict__ G, double* __restrict__ ecell,
                                                           double* __restrict__ cpart) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   TypeParams<T>* tp = reinterpret_cast<TypeParams<T>*>(smem_raw);
   const size_t tp_bytes = ((sizeof(TypeParams<T>) * ntypes + 15) / 16) * 16;
-  T* tile = reinterpret_cast<T*>(smem_raw + tp_bytes);  // [24][kCell8Cells]
-  double* red = reinterpret_cast<double*>(smem_raw + tp_bytes + ((sizeof(T) * 24 * kCell8Cells + 15) / 16) * 16);
+  // two buffers (alternating groups), so one barrier per group suffices
+  T* const buf0 = reinterpret_cast<T*>(smem_raw + tp_bytes);
+  constexpr int kBuf = (2 * 24 + 1) * kCell8Cells;
   __shared__ T Ls[9];
   load_params<T>(tp, tt, ntypes, box);
   if (threadIdx.x < 9) Ls[threadIdx.x] = (T)box[threadIdx.x];
   __syncthreads();
 
   const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
   const int a = threadIdx.x & 7;
   const int cl = threadIdx.x >> 3;
   const int ngroups = (t.M + kCell8Cells - 1) / kCell8Cells;
+  // components owned by this warp: c0 = warp (virial x = c0 / 3, y = c0 % 3), and for
+  // warps 0, 1 also c1 = 8 (virial zz) / 9 (energy)
+  const int c0x = warp / 3, c0y = warp % 3;
   typedef typename std::conditional<sizeof(T) == 8, double, F2>::type Acc;
-  Acc accum[kCellPart];
-#pragma unroll
-  for (int i = 0; i < kCellPart; ++i) accum[i] = Acc{};
-  for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+  Acc acc0{}, acc1{};
+  int parity = 0;
+  for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x, parity ^= 1) {
+  T* tile = buf0 + parity * kBuf;      // [24][kCell8Cells] corner gradients
+  T* relt = tile + 24 * kCell8Cells;   // [24][kCell8Cells] vertex offsets r_a - r_0
+  T* et = relt + 24 * kCell8Cells;     // [kCell8Cells] cell energies
   const int cell = grp * kCell8Cells + cl;
   const bool valid = cell < t.M;
   T du[3] = {T(0), T(0), T(0)};
@@ -277,8 +284,8 @@ __global__ void __launch_bounds__(kCell8Threads) k_cells8(Topo t, const TypeTabl
   if (valid) {
     int node;
     if (STRUCT) {
-      const int nyz = t.ny * t.nz;
-      const int i = cell / nyz, r = cell - i * nyz, j = r / t.nz, k = r - j * t.nz;
+      int i, j, k;
+      split_index(t, cell, i, j, k);
       node = struct_corner_node(t, i, j, k, a);
     } else {
       node = t.cell_nodes[bits_to_corner(a) * t.M + cell];
@@ -289,63 +296,79 @@ __global__ void __launch_bounds__(kCell8Threads) k_cells8(Topo t, const TypeTabl
   }
   T g[3];
   const T Ecell = cell8_eval<T, SIMPLE>(du, a, tp[ty], valid, g);
-  // stage corner gradients: tile[(corner*3 + x)][cl]
+  // stage corner gradients and vertex offsets r_a - r_0 = offset(a) . L + du_a - du_0
   const int corner = bits_to_corner(a);
-#pragma unroll
-  for (int x = 0; x < 3; ++x) tile[(corner * 3 + x) * kCell8Cells + cl] = g[x];
-  if (valid && a == 0 && ecell) ecell[cell] = (double)Ecell;
-  // virial: g_a (x) (offset(a) . L + du_a - du_0)
   const int src0 = lane & ~7;
-  T rel[3];
 #pragma unroll
-  for (int y = 0; y < 3; ++y) {
-    const T d0 = __shfl_sync(0xffffffffu, du[y], src0);
-    T r = du[y] - d0;
-    if (a & 1) r += Ls[0 * 3 + y];
-    if (a & 2) r += Ls[1 * 3 + y];
-    if (a & 4) r += Ls[2 * 3 + y];
-    rel[y] = r;
+  for (int x = 0; x < 3; ++x) {
+    tile[(corner * 3 + x) * kCell8Cells + cl] = valid ? g[x] : T(0);
+    const T d0 = __shfl_sync(0xffffffffu, du[x], src0);
+    T r = du[x] - d0;
+    if (a & 1) r += Ls[0 * 3 + x];
+    if (a & 2) r += Ls[1 * 3 + x];
+    if (a & 4) r += Ls[2 * 3 + x];
+    relt[(corner * 3 + x) * kCell8Cells + cl] = r;
   }
-  T vals[kCellPart];
-  vals[0] = (valid && a == 0) ? Ecell : T(0);
-#pragma unroll
-  for (int x = 0; x < 3; ++x)
-#pragma unroll
-    for (int y = 0; y < 3; ++y) vals[1 + x * 3 + y] = valid ? g[x] * rel[y] : T(0);
-  if constexpr (sizeof(T) == 8) {
-#pragma unroll
-    for (int i = 0; i < kCellPart; ++i) accum[i] += vals[i];
-  } else {
-#pragma unroll
-    for (int i = 0; i < kCellPart; ++i) accum[i] = f2_add(accum[i], F2{(float)vals[i], 0.0f});
-  }
+  if (a == 0) et[cl] = valid ? Ecell : T(0);
+  if (valid && a == 0 && ecell) ecell[cell] = (double)Ecell;
   __syncthreads();
-  for (int idx = threadIdx.x; idx < 24 * kCell8Cells; idx += blockDim.x) {
-    const int row = idx / kCell8Cells, col = idx - row * kCell8Cells;
-    const int c = grp * kCell8Cells + col;
-    if (c < t.M) G[row * (size_t)t.M + c] = tile[idx];
+  {
+    // component c0 of cell slot `lane`, corners in reference order
+    T v = T(0);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v += tile[(k * 3 + c0x) * kCell8Cells + lane] * relt[(k * 3 + c0y) * kCell8Cells + lane];
+    if constexpr (sizeof(T) == 8) acc0 += v;
+    else acc0 = f2_add(acc0, F2{v, 0.0f});
+    if (warp < 2) {
+      T w = T(0);
+      if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) w += tile[(k * 3 + 2) * kCell8Cells + lane] * relt[(k * 3 + 2) * kCell8Cells + lane];
+      } else {
+        w = et[lane];
+      }
+      if constexpr (sizeof(T) == 8) acc1 += w;
+      else acc1 = f2_add(acc1, F2{w, 0.0f});
+    }
   }
-  __syncthreads();
+  // corner-gradient rows: warp w writes rows w, w + 8, w + 16 (one 128-byte run each)
+  {
+    const int c = grp * kCell8Cells + lane;
+    if (c < t.M)
+#pragma unroll
+      for (int r = warp; r < 24; r += 8) G[r * (size_t)t.M + c] = tile[r * kCell8Cells + lane];
+  }
   }  // groups
-  double out[kCellPart];
+  // block partials: slot 0 energy, slot 1 + 3x + y virial; component c -> slot (c == 9 ? 0 : 1 + c)
   if constexpr (sizeof(T) == 8) {
 #pragma unroll
-    for (int i = 0; i < kCellPart; ++i) out[i] = accum[i];
-    block_sum<kCellPart>(out, red);
+    for (int off = 16; off > 0; off >>= 1) {
+      acc0 += __shfl_down_sync(0xffffffffu, acc0, off);
+      acc1 += __shfl_down_sync(0xffffffffu, acc1, off);
+    }
+    if (lane == 0) {
+      cpart[(1 + warp) * gridDim.x + blockIdx.x] = acc0;
+      if (warp < 2) cpart[(warp == 0 ? 9 : 0) * gridDim.x + blockIdx.x] = acc1;
+    }
   } else {
-    block_sum_f2<kCellPart>(accum, out, red);
-  }
-  if (threadIdx.x == 0)
 #pragma unroll
-    for (int i = 0; i < kCellPart; ++i) cpart[blockIdx.x * kCellPart + i] = out[i];
+    for (int off = 16; off > 0; off >>= 1) {
+      acc0 = f2_add(acc0, F2{__shfl_down_sync(0xffffffffu, acc0.hi, off), __shfl_down_sync(0xffffffffu, acc0.lo, off)});
+      acc1 = f2_add(acc1, F2{__shfl_down_sync(0xffffffffu, acc1.hi, off), __shfl_down_sync(0xffffffffu, acc1.lo, off)});
+    }
+    if (lane == 0) {
+      store_pair(cpart + (1 + warp) * gridDim.x + blockIdx.x, acc0);
+      if (warp < 2) store_pair(cpart + (warp == 0 ? 9 : 0) * gridDim.x + blockIdx.x, acc1);
+    }
+  }
 }
 
 template <typename T, bool STRUCT>
 __device__ __forceinline__ void gather_node(const Topo& t, const T* __restrict__ G, int n, T (&s)[3]) {
   s[0] = s[1] = s[2] = T(0);
   if (STRUCT) {
-    const int nyz = t.ny * t.nz;
-    const int i = n / nyz, r = n - i * nyz, j = r / t.nz, k = r - j * t.nz;
+    int i, j, k;
+    split_index(t, n, i, j, k);
 #pragma unroll
     for (int kc = 0; kc < 8; ++kc) {
       const int cell = struct_corner_cell(t, i, j, k, corner_to_bits(kc));
@@ -379,17 +402,50 @@ __global__ void k_gather(Topo t, const T* __restrict__ G, double* __restrict__ g
   if (bad && flag) atomicOr(flag, 1);
 }
 
+// Totals of per-block partials (value-major: slot v * na + k of a, v * nb + k of b, for
+// block k, so the lanes of a warp read consecutive slots) summed by one
+// block in a fixed order: warp w sums values w, w + nw, ...; its lanes stride over the
+// blocks, then a fixed shuffle tree. PAIRS: the slots hold compensated FP32 pairs,
+// summed in compensated FP32 and converted to FP64 once; else doubles summed in FP64.
+// Results in out_s (shared, NA + NB doubles), valid for every thread after the closing
+// barrier.
+template <int NA, int NB, bool PAIRS>
+__device__ __forceinline__ void sum_partials_by_warp(const double* a, int na, const double* b, int nb,
+                                                     double* out_s) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int v = wid; v < NA + NB; v += nw) {
+    const bool first = v < NA;
+    const double* base = first ? a + (size_t)v * na : b + (size_t)(v - NA) * nb;
+    const int n = first ? na : nb;
+    if constexpr (PAIRS) {
+      F2 acc{0.0f, 0.0f};
+#pragma unroll 8
+      for (int k = lane; k < n; k += 32) acc = f2_add(acc, load_pair(base + k));
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const F2 o{__shfl_down_sync(0xffffffffu, acc.hi, off), __shfl_down_sync(0xffffffffu, acc.lo, off)};
+        acc = f2_add(acc, o);
+      }
+      if (lane == 0) out_s[v] = (double)acc.hi + (double)acc.lo;
+    } else {
+      double acc = 0.0;
+#pragma unroll 8
+      for (int k = lane; k < n; k += 32) acc += __ldcg(base + k);
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+      if (lane == 0) out_s[v] = acc;
+    }
+  }
+  __syncthreads();
+}
+
+
 // Sum the per-block partials in block order: energy written, virial added.
+template <bool PAIRS>
 __global__ void k_finalize(const double* __restrict__ cpart, int nblk, double* __restrict__ energy,
                            double* __restrict__ vtens, int* __restrict__ flag) {
-  __shared__ double red[kCellPart * 8];
-  double acc[kCellPart];
-#pragma unroll
-  for (int i = 0; i < kCellPart; ++i) acc[i] = 0.0;
-  for (int b = threadIdx.x; b < nblk; b += blockDim.x)
-#pragma unroll
-    for (int i = 0; i < kCellPart; ++i) acc[i] += cpart[b * kCellPart + i];
-  block_sum<kCellPart>(acc, red);
+  __shared__ double acc[kCellPart];
+  sum_partials_by_warp<kCellPart, 0, PAIRS>(cpart, nblk, nullptr, 0, acc);
   if (threadIdx.x == 0) {
     *energy = acc[0];
     bool bad = isnan(acc[0]);
@@ -416,9 +472,38 @@ struct MDArgs {
   int start;            // pre thermostat + kick + drift of `step + 1`
 };
 
+// The block that arrives last: totals of the nb node-block partials and of the cell
+// totals, the step record and the conserved-energy carry. Deterministic (fixed order).
+template <typename T>
+__device__ __forceinline__ void md_nodes_final(const MDArgs& p, const double* npart, int nb, const double* cell_tot,
+                                               unsigned* ticket, double* carry, double* record) {
+  __shared__ double tn[kNodePart];
+  __threadfence();
+  sum_partials_by_warp<kNodePart, 0, sizeof(T) == 4>(npart, nb, nullptr, 0, tn);
+  if (threadIdx.x == 0) {
+    double tc[kCellPart];
+#pragma unroll
+    for (int i = 0; i < kCellPart; ++i) tc[i] = __ldcg(cell_tot + i);
+    const double ek = (sizeof(T) == 4) ? 0.5 * (tn[3] + tn[4] + tn[5]) : tn[1];
+    *ticket = 0u;
+    if (record) {
+      record[MM_REC_EPOT] = tc[0];
+      record[MM_REC_EKIN] = ek;
+      record[MM_REC_DECONS] = (p.finish ? (tn[0] - ek) : 0.0) + (p.finish ? carry[0] : 0.0);
+#pragma unroll
+      for (int i = 0; i < 9; ++i) record[MM_REC_VTENS + i] = tc[1 + i];
+      const double k[9] = {tn[3], tn[8], tn[7], tn[8], tn[4], tn[6], tn[7], tn[6], tn[5]};
+#pragma unroll
+      for (int i = 0; i < 9; ++i) record[MM_REC_KTENS + i] = k[i];
+    }
+    carry[0] = p.start ? (ek - tn[2]) : 0.0;
+    carry[1] = tc[0];
+  }
+}
+
 // One thread per node: gather, kick, thermostat, drift, and per-step observables.
 template <typename T, bool STRUCT, int THERMO>
-__global__ void __launch_bounds__(kNodeThreads, 4) k_md_nodes(Topo t, MDArgs p, const T* __restrict__ G,
+__global__ void __launch_bounds__(kMDThreads, 1) k_md_nodes(Topo t, MDArgs p, const T* __restrict__ G,
                                                            double* __restrict__ u, double* __restrict__ v,
                                                            T* __restrict__ disp, const double* __restrict__ mass,
                                                            const double* __restrict__ invm, const double* __restrict__ c2,
@@ -427,8 +512,25 @@ __global__ void __launch_bounds__(kNodeThreads, 4) k_md_nodes(Topo t, MDArgs p, 
                                                            unsigned* __restrict__ ticket, double* __restrict__ carry,
                                                            double* __restrict__ record, double* __restrict__ gpos_out,
                                                            const float4* __restrict__ nodef) {
-  __shared__ double red[kNodePart * (kNodeThreads / 32)];
+  __shared__ double red[kNodePart * (kMDThreads / 32)];
+  __shared__ double ctot[kCellPart];
   __shared__ bool last;
+  // blocks 0 .. nb-1 update the nodes; block nb (the last one) sums the cell kernel's
+  // partials meanwhile, so the block that finishes last has only nb node partials left
+  const int nb = gridDim.x - 1;
+  double* const cell_tot = npart + (size_t)kNodePart * nb;  // cell totals (FP64), after the node partials
+  if (blockIdx.x == nb) {
+    sum_partials_by_warp<kCellPart, 0, sizeof(T) == 4>(cpart, ncblk, nullptr, 0, ctot);
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int i = 0; i < kCellPart; ++i) cell_tot[i] = ctot[i];
+      __threadfence();
+      last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (last) md_nodes_final<T>(p, npart, nb, cell_tot, ticket, carry, record);
+    return;
+  }
   // per-node observables: FP64 for an FP64 handle; for an FP32 handle in FP32, summed
   // per warp with compensated FP32 and per block in FP64
   typedef typename std::conditional<sizeof(T) == 8, double, float>::type R;
@@ -437,7 +539,7 @@ __global__ void __launch_bounds__(kNodeThreads, 4) k_md_nodes(Topo t, MDArgs p, 
 #pragma unroll
   for (int i = 0; i < kNodePart; ++i) accum[i] = Acc{};
   // grid-stride over the nodes (the grid holds as many blocks as are resident at once)
-  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < t.N; n += gridDim.x * blockDim.x) {
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < t.N; n += nb * blockDim.x) {
   R obs[kNodePart];
 #pragma unroll
   for (int i = 0; i < kNodePart; ++i) obs[i] = R(0);
@@ -640,55 +742,25 @@ __global__ void __launch_bounds__(kNodeThreads, 4) k_md_nodes(Topo t, MDArgs p, 
     acc[0] = accum[0];
 #pragma unroll
     for (int i = 2; i < kNodePart; ++i) acc[i - 1] = accum[i];
-    double t8[kNodePart - 1];
-    block_sum_f2<kNodePart - 1>(acc, t8, red);
+    block_sum_f2_pairs<kNodePart - 1>(acc, red);
     if (threadIdx.x == 0) {
-      tot[0] = t8[0];
+      store_pair(npart + 0 * nb + blockIdx.x, acc[0]);
+      store_pair(npart + 1 * nb + blockIdx.x, F2{0.0f, 0.0f});
 #pragma unroll
-      for (int i = 2; i < kNodePart; ++i) tot[i] = t8[i - 1];
-      tot[1] = 0.5 * (tot[3] + tot[4] + tot[5]);
+      for (int i = 2; i < kNodePart; ++i) store_pair(npart + i * nb + blockIdx.x, acc[i - 1]);
     }
   }
   if (threadIdx.x == 0) {
+    if constexpr (sizeof(T) == 8) {
 #pragma unroll
-    for (int i = 0; i < kNodePart; ++i) npart[blockIdx.x * kNodePart + i] = tot[i];
+      for (int i = 0; i < kNodePart; ++i) npart[i * nb + blockIdx.x] = tot[i];
+    }
     __threadfence();
     const unsigned prev = atomicAdd(ticket, 1u);
     last = (prev == gridDim.x - 1);
   }
   __syncthreads();
-  if (!last) return;
-  __threadfence();
-  // last block: totals of all partials; each thread takes a fixed strided subset,
-  // then a fixed-order block tree (deterministic)
-  double tt[kNodePart + kCellPart];
-#pragma unroll
-  for (int i = 0; i < kNodePart + kCellPart; ++i) tt[i] = 0.0;
-  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
-#pragma unroll
-    for (int i = 0; i < kNodePart; ++i) tt[i] += ((volatile double*)npart)[b * kNodePart + i];
-  for (int b = threadIdx.x; b < ncblk; b += blockDim.x)
-#pragma unroll
-    for (int i = 0; i < kCellPart; ++i) tt[kNodePart + i] += cpart[b * kCellPart + i];
-  __shared__ double red2[(kNodePart + kCellPart) * (kNodeThreads / 32)];
-  block_sum<kNodePart + kCellPart>(tt, red2);
-  double* tn = tt;
-  double* tc = tt + kNodePart;
-  if (threadIdx.x == 0) {
-    *ticket = 0u;
-    if (record) {
-      record[MM_REC_EPOT] = tc[0];
-      record[MM_REC_EKIN] = tn[1];
-      record[MM_REC_DECONS] = (p.finish ? (tn[0] - tn[1]) : 0.0) + (p.finish ? carry[0] : 0.0);
-#pragma unroll
-      for (int i = 0; i < 9; ++i) record[MM_REC_VTENS + i] = tc[1 + i];
-      const double k[9] = {tn[3], tn[8], tn[7], tn[8], tn[4], tn[6], tn[7], tn[6], tn[5]};
-#pragma unroll
-      for (int i = 0; i < 9; ++i) record[MM_REC_KTENS + i] = k[i];
-    }
-    carry[0] = p.start ? (tn[1] - tn[2]) : 0.0;
-    carry[1] = tc[0];
-  }
+  if (last) md_nodes_final<T>(p, npart, nb, cell_tot, ticket, carry, record);
 }
 
 // First half of a step from a caller-provided gradient (AoS): "pre" thermostat,
@@ -727,6 +799,59 @@ __global__ void k_md_begin_gpos(Topo t, MDArgs p, const double* __restrict__ gpo
   }
 }
 
+// Host-buffer step, first half in one pass: u = pos - X(L) and v from the caller's
+// AoS arrays, then the "pre" thermostat, kick with the caller's gradient, and drift
+// (the arithmetic of k_pos_to_state + k_aos_to_soa + k_md_begin_gpos, in that order).
+// pos / vel / gpos may be device pointers of mapped pinned host memory.
+template <typename T, int THERMO>
+__global__ void k_md_host_begin(Topo t, MDArgs p, const double* __restrict__ pos, const double* __restrict__ vel,
+                                const double* __restrict__ gpos, const double* __restrict__ box,
+                                double* __restrict__ u, double* __restrict__ v, T* __restrict__ disp,
+                                const double* __restrict__ invm, const double* __restrict__ c2) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= t.N) return;
+  int la, lb, lc;
+  lattice_of(t, n, la, lb, lc);
+  double uu[3], vv[3], gg[3];
+#pragma unroll
+  for (int x = 0; x < 3; ++x) {
+    uu[x] = pos[3 * n + x] - (la * box[x] + lb * box[3 + x] + lc * box[6 + x]);
+    vv[x] = vel[3 * n + x];
+    gg[x] = gpos[3 * n + x];
+  }
+  if (THERMO == MM_THERMO_LANGEVIN) {
+    float zf[3];
+    normal3(p.seed, (uint32_t)n, (uint32_t)p.step, 0u, zf);
+    const double amp = c2[n];
+#pragma unroll
+    for (int x = 0; x < 3; ++x) vv[x] = p.c1 * vv[x] + amp * (double)zf[x];
+  }
+  const double im = invm[n];
+#pragma unroll
+  for (int x = 0; x < 3; ++x) {
+    vv[x] += 0.5 * (-gg[x] * im) * p.dt;
+    const double un = uu[x] + p.dt * vv[x];
+    u[x * t.N + n] = un;
+    disp[x * t.N + n] = (T)un;
+    v[x * t.N + n] = vv[x];
+  }
+}
+
+// Host-buffer step, output: pos = X(L) + u and vel in AoS (the arithmetic of
+// k_state_to_pos + k_soa_to_aos); pos / vel may be mapped pinned host memory.
+__global__ void k_md_host_end(Topo t, const double* __restrict__ u, const double* __restrict__ v,
+                              const double* __restrict__ box, double* __restrict__ pos, double* __restrict__ vel) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= t.N) return;
+  int la, lb, lc;
+  lattice_of(t, n, la, lb, lc);
+#pragma unroll
+  for (int x = 0; x < 3; ++x) {
+    pos[3 * n + x] = (la * box[x] + lb * box[3 + x] + lc * box[6 + x]) + u[x * t.N + n];
+    vel[3 * n + x] = v[x * t.N + n];
+  }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ host side
@@ -745,6 +870,8 @@ static void topo_of(const mm_handle* h, Topo& t) {
   t.nx = h->nn[0];
   t.ny = h->nn[1];
   t.nz = h->nn[2];
+  t.div_nyz = make_fastdiv((uint32_t)(t.ny * t.nz > 0 ? t.ny * t.nz : 1));
+  t.div_nz = make_fastdiv((uint32_t)(t.nz > 0 ? t.nz : 1));
   t.cell_nodes = h->d_cell_nodes;
   t.node_cells = h->d_node_cells;
   t.node_lat = h->d_node_lat;
@@ -754,9 +881,7 @@ static void topo_of(const mm_handle* h, Topo& t) {
 static size_t cell_smem(const mm_handle* h) {
   const size_t esz = h->prec == MM_PREC_FP32 ? sizeof(float) : sizeof(double);
   const size_t tp = (h->prec == MM_PREC_FP32 ? sizeof(TypeParams<float>) : sizeof(TypeParams<double>)) * h->ntypes;
-  if (h->model == MM_MODEL_NANOCELL)
-    return ((tp + 15) / 16) * 16 + ((esz * 24 * kCell8Cells + 15) / 16) * 16 +
-           sizeof(double) * kCellPart * (kCell8Threads / 32);
+  if (h->model == MM_MODEL_NANOCELL) return ((tp + 15) / 16) * 16 + 2 * esz * (2 * 24 + 1) * kCell8Cells;
   return ((tp + 15) / 16) * 16 + sizeof(double) * kCellPart * (kCellThreads / 32);
 }
 
@@ -865,7 +990,8 @@ void launch_gather(mm_handle* h, double* gpos, int* flag, cudaStream_t st) {
 }
 
 void launch_finalize(mm_handle* h, double* energy, double* vtens, int* flag, cudaStream_t st) {
-  k_finalize<<<1, 256, 0, st>>>(h->d_cpart, cell_grid(h), energy, vtens, flag);
+  if (h->prec == MM_PREC_FP32) k_finalize<true><<<1, 256, 0, st>>>(h->d_cpart, cell_grid(h), energy, vtens, flag);
+  else k_finalize<false><<<1, 256, 0, st>>>(h->d_cpart, cell_grid(h), energy, vtens, flag);
 }
 
 __global__ void k_selftest_convert(const double* din, float* dout, const float* fin, double* fout, int n) {
@@ -891,17 +1017,17 @@ static void launch_md_nodes_t(mm_handle* h, const MDArgs& a, const double* noise
   Topo t;
   topo_of(h, t);
   int& occ = h->node_occ[THERMO == MM_THERMO_LANGEVIN ? 1 : 0];
-  if (occ == 0) occ = occupancy_of(k_md_nodes<T, STRUCT, THERMO>, kNodeThreads, 0);
-  k_md_nodes<T, STRUCT, THERMO><<<node_grid(h, THERMO), kNodeThreads, 0, st>>>(
+  if (occ == 0) occ = occupancy_of(k_md_nodes<T, STRUCT, THERMO>, kMDThreads, 0);
+  k_md_nodes<T, STRUCT, THERMO><<<node_grid(h, THERMO) + 1, kMDThreads, 0, st>>>(
       t, a, (const T*)h->d_G, h->d_u, h->d_v, (T*)h->d_disp, h->d_mass, h->d_invm, h->d_c2, noise, h->d_npart,
       h->d_cpart, cell_grid(h), h->d_ticket, h->d_carry, record, gpos_out, h->d_nodef);
 }
 
-// Node grid: as many blocks as fit at once (grid-stride over the nodes), at most one
-// block per 256 nodes.
+// Node-update grid: as many blocks as fit at once (grid-stride over the nodes), at most
+// one block per kMDThreads nodes (the kernel adds one block for the cell partials).
 int node_grid(mm_handle* h, int thermo) {
   const int occ = h->node_occ[thermo == MM_THERMO_LANGEVIN ? 1 : 0];
-  const int nb = node_blocks(h);
+  const int nb = (h->N + kMDThreads - 1) / kMDThreads;
   if (occ <= 0) return nb;
   const int cap = (h->num_sms > 0 ? h->num_sms : 152) * occ;
   return nb < cap ? nb : cap;
@@ -961,6 +1087,39 @@ void launch_md_begin_gpos(mm_handle* h, double dt, double c1, uint64_t seed, int
     else
       k_md_begin_gpos<double, MM_THERMO_NONE><<<nb, kNodeThreads, 0, st>>>(t, a, gpos, h->d_u, h->d_v, (double*)h->d_disp, h->d_invm, h->d_c2, noise);
   }
+}
+
+void launch_md_host_begin(mm_handle* h, double dt, double c1, uint64_t seed, int64_t step, int thermo,
+                          const double* pos, const double* vel, const double* gpos, cudaStream_t st) {
+  Topo t;
+  topo_of(h, t);
+  MDArgs a;
+  a.dt = dt;
+  a.c1 = c1;
+  a.seed = seed;
+  a.step = step;
+  a.noise_step0 = step;
+  a.finish = 0;
+  a.start = 1;
+  const int nb = node_blocks(h);
+  const bool lang = thermo == MM_THERMO_LANGEVIN;
+  if (h->prec == MM_PREC_FP32) {
+    if (lang)
+      k_md_host_begin<float, MM_THERMO_LANGEVIN><<<nb, kNodeThreads, 0, st>>>(t, a, pos, vel, gpos, h->d_box, h->d_u, h->d_v, (float*)h->d_disp, h->d_invm, h->d_c2);
+    else
+      k_md_host_begin<float, MM_THERMO_NONE><<<nb, kNodeThreads, 0, st>>>(t, a, pos, vel, gpos, h->d_box, h->d_u, h->d_v, (float*)h->d_disp, h->d_invm, h->d_c2);
+  } else {
+    if (lang)
+      k_md_host_begin<double, MM_THERMO_LANGEVIN><<<nb, kNodeThreads, 0, st>>>(t, a, pos, vel, gpos, h->d_box, h->d_u, h->d_v, (double*)h->d_disp, h->d_invm, h->d_c2);
+    else
+      k_md_host_begin<double, MM_THERMO_NONE><<<nb, kNodeThreads, 0, st>>>(t, a, pos, vel, gpos, h->d_box, h->d_u, h->d_v, (double*)h->d_disp, h->d_invm, h->d_c2);
+  }
+}
+
+void launch_md_host_end(mm_handle* h, double* pos, double* vel, cudaStream_t st) {
+  Topo t;
+  topo_of(h, t);
+  k_md_host_end<<<node_blocks(h), kNodeThreads, 0, st>>>(t, h->d_u, h->d_v, h->d_box, pos, vel);
 }
 
 }  // namespace mm
