@@ -398,6 +398,33 @@ def measure_grad_over_fwd(n=16, reps=5):
     return {"lattice": [n] * 3, "forward_ms": 1e3 * f, "backward_ms": 1e3 * b, "grad_over_fwd": b / f}
 
 
+def host_link_rates(pinned, dev, reps=5):
+    """Pinned host <-> device copy rates (GB/s) for one array of the e2e step, and for
+    three such copies on three streams (what the host-buffer step issues)."""
+    import torch
+
+    n = pinned.numel()
+    h = [pinned.clone().pin_memory() for _ in range(3)]
+    d = [torch.empty(n, dtype=pinned.dtype, device=dev).view(pinned.shape) for _ in range(3)]
+    streams = [torch.cuda.Stream(dev) for _ in range(3)]
+    out = {}
+    for name, fn in (("h2d", lambda i: d[i].copy_(h[i], non_blocking=True)),
+                     ("d2h", lambda i: h[i].copy_(d[i], non_blocking=True))):
+        for k in (1, 3):
+            best = None
+            for _ in range(reps):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                for i in range(k):
+                    with torch.cuda.stream(streams[i]):
+                        fn(i)
+                torch.cuda.synchronize()
+                dt = time.perf_counter() - t0
+                best = dt if best is None else min(best, dt)
+            out["%s_gbs_x%d" % (name, k)] = k * pinned.numel() * pinned.element_size() / best / 1e9
+    return out
+
+
 def run_gpu(args):
     import torch
 
@@ -488,6 +515,7 @@ def run_gpu(args):
                                     rec_h.data_ptr(), dt, 1, temp, tau, SEED, 10**6 + i), "mm_md_step_host")
     e2e_s = time.perf_counter() - t0
     e2e_value = world * M * e_steps / e2e_s
+    link = host_link_rates(pos_h, dev)
 
     # ---- roofline of the dominant kernel (cells)
     hbm, kind = peaks()
@@ -513,7 +541,7 @@ def run_gpu(args):
                                  "frac_of_nominal": flops / fp32_peak},
                      "step_hbm_gbs": STEP_BYTES * M * args.steps / (ms * 1e-3) / 1e9},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 3 * 24 * s.nnodes,
-                "d2h_bytes_per_step": 3 * 24 * s.nnodes + 8 * nat.MM_REC_LEN},
+                "d2h_bytes_per_step": 3 * 24 * s.nnodes + 8 * nat.MM_REC_LEN, "host_link": link},
         "gpu_launches": 2 * args.steps,
         "clocks": clk,
     }

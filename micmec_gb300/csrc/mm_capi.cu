@@ -67,6 +67,10 @@ bool dev_alloc(X** p, size_t count) {
 
 void free_handle(mm_handle* h) {
   if (!h) return;
+  for (int i = 0; i < 2; ++i)
+    if (h->copy_st[i]) cudaStreamDestroy(h->copy_st[i]);
+  for (int i = 0; i < 3; ++i)
+    if (h->copy_ev[i]) cudaEventDestroy(h->copy_ev[i]);
   void* bufs[] = {h->d_tt, h->d_box, h->d_cell_nodes, h->d_node_cells, h->d_node_lat, h->d_cell_type,
                   h->d_mass, h->d_invm, h->d_c2, h->d_u, h->d_v, h->d_disp, h->d_G, h->d_ecell,
                   h->d_cpart, h->d_npart, h->d_ticket, h->d_carry, h->d_io, h->d_flag, h->d_adj, h->d_nodef, h->d_eng};
@@ -471,15 +475,30 @@ mm_status mm_md_time_kernels(mm_handle* h, int nsteps, void* flush_buf, size_t f
   return MM_OK;
 }
 
-// Device address of a pinned (page-locked, mapped) host buffer, or nullptr for any
-// other memory.
-static void* mapped_host_ptr(const void* p) {
-  cudaPointerAttributes a;
-  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-    (void)cudaGetLastError();
-    return nullptr;
+// The host-buffer step moves pos, vel and the gradient (three arrays of 24 B per
+// node) each way; one copy per array on its own stream lets several copy engines
+// share the host link.
+static mm_status ensure_copy_streams(mm_handle* h) {
+  for (int i = 0; i < 2; ++i)
+    if (!h->copy_st[i]) MM_CUDA(cudaStreamCreateWithFlags(&h->copy_st[i], cudaStreamNonBlocking));
+  for (int i = 0; i < 3; ++i)
+    if (!h->copy_ev[i]) MM_CUDA(cudaEventCreateWithFlags(&h->copy_ev[i], cudaEventDisableTiming));
+  return MM_OK;
+}
+
+// dst[i] <- src[i] (n bytes each) for three arrays: array 0 on st, arrays 1 and 2 on the
+// side streams; st waits for all three.
+static mm_status copy3(mm_handle* h, void* const* dst, const void* const* src, size_t n, cudaMemcpyKind kind,
+                       cudaStream_t st) {
+  MM_CUDA(cudaEventRecord(h->copy_ev[0], st));
+  for (int i = 0; i < 2; ++i) {
+    MM_CUDA(cudaStreamWaitEvent(h->copy_st[i], h->copy_ev[0], 0));
+    MM_CUDA(cudaMemcpyAsync(dst[1 + i], src[1 + i], n, kind, h->copy_st[i]));
+    MM_CUDA(cudaEventRecord(h->copy_ev[1 + i], h->copy_st[i]));
   }
-  return (a.type == cudaMemoryTypeHost) ? a.devicePointer : nullptr;
+  MM_CUDA(cudaMemcpyAsync(dst[0], src[0], n, kind, st));
+  for (int i = 0; i < 2; ++i) MM_CUDA(cudaStreamWaitEvent(st, h->copy_ev[1 + i], 0));
+  return MM_OK;
 }
 
 mm_status mm_md_step_host(mm_handle* h, double* pos, double* vel, double* gpos, double* record, double timestep,
@@ -488,45 +507,33 @@ mm_status mm_md_step_host(mm_handle* h, double* pos, double* vel, double* gpos, 
   cudaStream_t st = 0;
   mm_status s = md_prepare(h, timestep, thermo, temp, timecon, seed, st);
   if (s != MM_OK) return s;
-  const size_t n3 = 3 * (size_t)h->N;
-  // carry (pre-thermostat correction) is produced by the begin kernel only through ekin;
-  // the host-buffer step reports the post-thermostat correction alone.
-  MM_CUDA(cudaMemsetAsync(h->d_carry, 0, sizeof(double), st));
-  double* m_pos = (double*)mapped_host_ptr(pos);
-  double* m_vel = (double*)mapped_host_ptr(vel);
-  double* m_gpos = (double*)mapped_host_ptr(gpos);
-  double* m_rec = record ? (double*)mapped_host_ptr(record) : nullptr;
-  if (m_pos && m_vel && m_gpos) {
-    // pinned caller buffers: the kernels read and write them in place over the host
-    // link (the begin kernel reads pos/vel/gpos, the node kernel writes the new
-    // gradient and the record, the end kernel writes pos/vel); no staging copies
-    double* d_rec = m_rec ? m_rec : h->d_io + 3 * n3;
-    mm::launch_md_host_begin(h, h->md.dt, h->md.c1, seed, step, thermo, m_pos, m_vel, m_gpos, st);
-    mm::launch_cells(h, st, nullptr);
-    mm::launch_md_nodes(h, h->md.dt, h->md.c1, seed, step, step, 1, 0, thermo, nullptr, d_rec, m_gpos, st);
-    mm::launch_md_host_end(h, m_pos, m_vel, st);
-    MM_CUDA(cudaGetLastError());
-    if (record && !m_rec)
-      MM_CUDA(cudaMemcpyAsync(record, d_rec, MM_REC_LEN * sizeof(double), cudaMemcpyDeviceToHost, st));
-    MM_CUDA(cudaStreamSynchronize(st));
-    return MM_OK;
-  }
-  // pageable caller buffers: staged through device buffers
+  s = ensure_copy_streams(h);
+  if (s != MM_OK) return s;
+  const size_t n3 = 3 * (size_t)h->N, bytes = n3 * sizeof(double);
   double* d_pos = h->d_io;
   double* d_gpos = h->d_io + n3;
   double* d_vel = h->d_io + 2 * n3;
   double* d_rec = h->d_io + 3 * n3;
-  MM_CUDA(cudaMemcpyAsync(d_pos, pos, n3 * sizeof(double), cudaMemcpyHostToDevice, st));
-  MM_CUDA(cudaMemcpyAsync(d_vel, vel, n3 * sizeof(double), cudaMemcpyHostToDevice, st));
-  MM_CUDA(cudaMemcpyAsync(d_gpos, gpos, n3 * sizeof(double), cudaMemcpyHostToDevice, st));
+  // carry (pre-thermostat correction) is produced by the begin kernel only through ekin;
+  // the host-buffer step reports the post-thermostat correction alone.
+  MM_CUDA(cudaMemsetAsync(h->d_carry, 0, sizeof(double), st));
+  {
+    void* dst[3] = {d_pos, d_vel, d_gpos};
+    const void* src[3] = {pos, vel, gpos};
+    s = copy3(h, dst, src, bytes, cudaMemcpyHostToDevice, st);
+    if (s != MM_OK) return s;
+  }
   mm::launch_md_host_begin(h, h->md.dt, h->md.c1, seed, step, thermo, d_pos, d_vel, d_gpos, st);
   mm::launch_cells(h, st, nullptr);
   mm::launch_md_nodes(h, h->md.dt, h->md.c1, seed, step, step, 1, 0, thermo, nullptr, d_rec, d_gpos, st);
   mm::launch_md_host_end(h, d_pos, d_vel, st);
   MM_CUDA(cudaGetLastError());
-  MM_CUDA(cudaMemcpyAsync(pos, d_pos, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
-  MM_CUDA(cudaMemcpyAsync(vel, d_vel, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
-  MM_CUDA(cudaMemcpyAsync(gpos, d_gpos, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  {
+    void* dst[3] = {pos, vel, gpos};
+    const void* src[3] = {d_pos, d_vel, d_gpos};
+    s = copy3(h, dst, src, bytes, cudaMemcpyDeviceToHost, st);
+    if (s != MM_OK) return s;
+  }
   if (record) MM_CUDA(cudaMemcpyAsync(record, d_rec, MM_REC_LEN * sizeof(double), cudaMemcpyDeviceToHost, st));
   MM_CUDA(cudaStreamSynchronize(st));
   return MM_OK;

@@ -45,53 +45,51 @@ struct BMD {
 
 // ------------------------------------------------------------ small 3x3 helpers (thread 0, FP64)
 
-__device__ inline void jacobi3(const double* Ain, double* w, double* Q) {
-  double A[9];
-  for (int i = 0; i < 9; ++i) A[i] = Ain[i];
-  for (int i = 0; i < 9; ++i) Q[i] = (i % 4 == 0) ? 1.0 : 0.0;
-  for (int sweep = 0; sweep < 50; ++sweep) {
-    const double off = A[1] * A[1] + A[2] * A[2] + A[5] * A[5];
-    const double diag = A[0] * A[0] + A[4] * A[4] + A[8] * A[8];
-    if (off <= 1e-34 * diag || off == 0.0) break;
-    for (int p = 0; p < 2; ++p)
-      for (int q = p + 1; q < 3; ++q) {
-        const double apq = A[p * 3 + q];
-        if (apq == 0.0) continue;
-        const double app = A[p * 3 + p], aqq = A[q * 3 + q];
-        const double theta = (aqq - app) / (2.0 * apq);
-        const double tt = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-        const double c = 1.0 / sqrt(tt * tt + 1.0), sn = tt * c;
-        for (int k = 0; k < 3; ++k) {  // A <- J^T A J
-          const double akp = A[k * 3 + p], akq = A[k * 3 + q];
-          A[k * 3 + p] = c * akp - sn * akq;
-          A[k * 3 + q] = sn * akp + c * akq;
-        }
-        for (int k = 0; k < 3; ++k) {
-          const double apk = A[p * 3 + k], aqk = A[q * 3 + k];
-          A[p * 3 + k] = c * apk - sn * aqk;
-          A[q * 3 + k] = sn * apk + c * aqk;
-        }
-        for (int k = 0; k < 3; ++k) {  // Q <- Q J
-          const double qkp = Q[k * 3 + p], qkq = Q[k * 3 + q];
-          Q[k * 3 + p] = c * qkp - sn * qkq;
-          Q[k * 3 + q] = sn * qkp + c * qkq;
-        }
-      }
+__device__ inline double norm1_3(const double* A) {
+  double m = 0.0;
+  for (int j = 0; j < 3; ++j) {
+    const double c = fabs(A[j]) + fabs(A[3 + j]) + fabs(A[6 + j]);
+    m = c > m ? c : m;
   }
-  w[0] = A[0];
-  w[1] = A[4];
-  w[2] = A[8];
+  return m;
+}
+__device__ inline void matmul3(const double* A, const double* B, double* C) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) C[i * 3 + j] = A[i * 3] * B[j] + A[i * 3 + 1] * B[3 + j] + A[i * 3 + 2] * B[6 + j];
 }
 
-// R = Q diag(exp(f * w)) Q^T for a symmetric S (eigenpairs w, Q)
+// R = exp(f S) for a symmetric 3x3 S: the matrix exponential the reference forms from
+// an eigen-decomposition (np.linalg.eigh, npt.py:700-716), here by scaling and squaring
+// of the Taylor series (Moler and Van Loan, "Nineteen dubious ways to compute the
+// exponential of a matrix, twenty-five years later", SIAM Review 45, 2003): A = f S / 2^k
+// with ||A||_1 <= 1/8, T = sum_n A^n / n! until a term falls below 1e-18 ||T||_1, then
+// R = T^(2^k). The barostat's arguments are small (k = 0, a handful of terms), and the
+// result agrees with the eigen-decomposition form to FP64 rounding.
 __device__ inline void sym_exp(const double* S, double f, double* R) {
-  double w[3], Q[9];
-  jacobi3(S, w, Q);
-  double e[3];
-  for (int i = 0; i < 3; ++i) e[i] = exp(f * w[i]);
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) R[i * 3 + j] = Q[i * 3 + 0] * e[0] * Q[j * 3 + 0] + Q[i * 3 + 1] * e[1] * Q[j * 3 + 1] +
-                                              Q[i * 3 + 2] * e[2] * Q[j * 3 + 2];
+  double A[9];
+  for (int i = 0; i < 9; ++i) A[i] = f * S[i];
+  int k = 0;
+  double nrm = norm1_3(A);
+  while (nrm > 0.125 && k < 64) {
+    for (int i = 0; i < 9; ++i) A[i] *= 0.5;
+    nrm *= 0.5;
+    ++k;
+  }
+  double term[9], tmp[9];
+  for (int i = 0; i < 9; ++i) R[i] = term[i] = (i % 4 == 0) ? 1.0 : 0.0;
+  for (int n = 1; n <= 20; ++n) {
+    matmul3(term, A, tmp);
+    const double inv = 1.0 / n;
+    for (int i = 0; i < 9; ++i) {
+      term[i] = tmp[i] * inv;
+      R[i] += term[i];
+    }
+    if (norm1_3(term) <= 1e-18 * norm1_3(R)) break;
+  }
+  for (int q = 0; q < k; ++q) {
+    matmul3(R, R, tmp);
+    for (int i = 0; i < 9; ++i) R[i] = tmp[i];
+  }
 }
 
 // MTK: update of the barostat velocity tensor (npt.py:654-681), thread 0

@@ -53,6 +53,8 @@ struct mm_handle {
   double* d_adj = nullptr;            // adjoint scratch (allocated on first mm_adjoint call)
   size_t adj_len = 0;
   double* d_eng = nullptr;            // NHC/MTK engine scratch (allocated on first mm_md_engine call)
+  cudaStream_t copy_st[2] = {nullptr, nullptr};  // host-buffer step: side streams for parallel copies
+  cudaEvent_t copy_ev[3] = {nullptr, nullptr, nullptr};
   size_t eng_len = 0;
   // MD session
   struct {

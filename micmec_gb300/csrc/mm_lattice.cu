@@ -538,8 +538,10 @@ __global__ void __launch_bounds__(kMDThreads, 1) k_md_nodes(Topo t, MDArgs p, co
   Acc accum[kNodePart];
 #pragma unroll
   for (int i = 0; i < kNodePart; ++i) accum[i] = Acc{};
-  // grid-stride over the nodes (the grid holds as many blocks as are resident at once)
-  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < t.N; n += nb * blockDim.x) {
+  // block b owns the contiguous node range [N b / nb, N (b + 1) / nb): equal shares
+  // for all SMs; its threads stride through it
+  const int n_end = (int)(((long long)t.N * (blockIdx.x + 1)) / nb);
+  for (int n = (int)(((long long)t.N * blockIdx.x) / nb) + threadIdx.x; n < n_end; n += blockDim.x) {
   R obs[kNodePart];
 #pragma unroll
   for (int i = 0; i < kNodePart; ++i) obs[i] = R(0);
@@ -1023,13 +1025,16 @@ static void launch_md_nodes_t(mm_handle* h, const MDArgs& a, const double* noise
       h->d_cpart, cell_grid(h), h->d_ticket, h->d_carry, record, gpos_out, h->d_nodef);
 }
 
-// Node-update grid: as many blocks as fit at once (grid-stride over the nodes), at most
-// one block per kMDThreads nodes (the kernel adds one block for the cell partials).
+// Node-update grid: at most one block per kMDThreads nodes, and one block fewer than fit
+// on the GPU at once: the kernel adds one block for the cell partials, which must be
+// resident together with the node blocks (else it would start only when a node block
+// retires, and the step would end one reduction later).
 int node_grid(mm_handle* h, int thermo) {
   const int occ = h->node_occ[thermo == MM_THERMO_LANGEVIN ? 1 : 0];
   const int nb = (h->N + kMDThreads - 1) / kMDThreads;
   if (occ <= 0) return nb;
-  const int cap = (h->num_sms > 0 ? h->num_sms : 152) * occ;
+  int cap = (h->num_sms > 0 ? h->num_sms : 152) * occ - 1;
+  if (cap < 1) cap = 1;
   return nb < cap ? nb : cap;
 }
 
