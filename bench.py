@@ -364,6 +364,66 @@ def measure_plain_per_system(systems, nsteps):
             "cell_steps_per_s": sum(s.ncells for s in systems) * nsteps / t}
 
 
+def measure_large_mtk(n=256, nsteps=20, fp64_steps=4):
+    """Large single system (periodic n^3 lattice, 20% clustered defects, two states per
+    type) under NHC + MTK NPT at 300 K and 100 MPa, dt = 2 fs, through VerletIntegrator
+    (device=True routes it to the lattice engine); FP32 cells, and a short FP64 run from
+    the same state for the conserved-energy drift."""
+    import torch
+
+    from micmec_gb300 import lattices, units
+    from micmec_gb300.pes.mmff import ForcePartMechanical, MicMecForceField
+    from micmec_gb300.sampling.iterative import Hook
+    from micmec_gb300.sampling.npt import MTKBarostat
+    from micmec_gb300.sampling.nvt import NHCThermostat
+    from micmec_gb300.sampling.verlet import VerletIntegrator
+    from micmec_gb300.system import System
+
+    rng = np.random.default_rng(SEED + 5)
+    t0 = time.perf_counter()
+    d = lattices.make_lattice(lattices.defect_grid(n, 0.2, rng, clustered=True), nstates=2)
+    d["pos"] = lattices.displace(d["pos"], 0.02 * units.angstrom, rng)
+    t_setup = time.perf_counter() - t0
+    kT = units.boltzmann * 300.0
+    out = {"lattice": [n] * 3, "cells": n ** 3, "hooks": "NHC + MTK, 300 K, 100 MPa", "timestep_fs": 2.0,
+           "host_setup_s": t_setup}
+
+    class Econs(Hook):
+        # called after the warm-up and at the end only (a per-step host hook would
+        # bring the state back to the host every step)
+        def __init__(self, start, step):
+            Hook.__init__(self, start, step)
+            self.rows = []
+
+        def __call__(self, it):
+            self.rows.append((it.counter, it.econs, it.epot))
+
+    vel = None
+    for prec, steps in (("fp32", nsteps), ("fp64", fp64_steps)):
+        s = System.from_dict(d)
+        if vel is None:
+            vel = rng.normal(0.0, 1.0, s.pos.shape) * np.sqrt(kT / s.masses)[:, None]
+            vel -= (s.masses @ vel) / s.masses.sum()
+        ff = MicMecForceField(s, [ForcePartMechanical(s, precision=prec)])
+        rec = Econs(2, steps)
+        hooks = [NHCThermostat(300.0, timecon=100 * units.femtosecond),
+                 MTKBarostat(ff, 300.0, 100e6 * units.pascal, timecon=1000 * units.femtosecond), rec]
+        vi = VerletIntegrator(ff, 2.0 * units.femtosecond, hooks=hooks, vel0=vel.copy(), device=True)
+        vi.run(2)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        vi.run(steps)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        rows = np.array(rec.rows[-2:])
+        e = rows[:, 1]
+        out[prec] = {"steps": steps, "s": dt, "cell_steps_per_s": n ** 3 * steps / dt,
+                     "econs_drift_per_step_rel": float((e[-1] - e[0]) / steps / abs(rows[0, 2]))}
+        del vi, ff, s
+        torch.cuda.empty_cache()
+    return out
+
+
 def measure_grad_over_fwd(n=16, reps=5):
     """Cost of the adjoint (backward of a force loss) relative to the forward force evaluation, 16^3 FP64."""
     import torch
@@ -564,6 +624,7 @@ def run_gpu(args):
                                "batched_fp32_over_plain_fp64_systems_per_s":
                                    bf["systems_steps_per_s"] / plain["systems_steps_per_s"]}
             line["adjoint"] = measure_grad_over_fwd()
+            line["large_mtk"] = measure_large_mtk()
         except Exception as exc:  # extra measurements never block the main line
             line["extra_error"] = repr(exc)[:300]
     if rank == 0 and not args.no_cpu_baseline:
@@ -587,12 +648,43 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the FP64 / batched / adjoint side measurements")
+    ap.add_argument("--batch-only", action="store_true",
+                    help="only the batched workload (512 systems, NHC + MTK, FP32 cells): one warm-up launch of "
+                         "--warmup steps and one launch of --steps steps, no autotuning or graph (for kernel profiles)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.batch_only:
+        return run_batch_only(args)
     return run_gpu(args)
+
+
+def run_batch_only(args):
+    import torch
+
+    from micmec_gb300 import units
+    from micmec_gb300.batch import BatchSystems
+
+    systems, _ = batch_workload()
+    b = BatchSystems(systems, model="nanocell", precision="fp32")
+    fs = units.femtosecond
+    b.setup_md(temp=300.0, thermostat="nhc", barostat="mtk", timecon=100 * fs, baro_timecon=1000 * fs, seed=5)
+    kw = dict(thermostat="nhc", temp=300.0, barostat="mtk", press=0.0, use_graph=False)
+    b.md(args.warmup, **kw)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    b.md(args.steps, step0=args.warmup, **kw)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    cells = float(np.sum(b.sizes))
+    print(json.dumps({"workload": "batched 512 systems, NHC + MTK, FP32 cells", "steps": args.steps, "ms": ms,
+                      "systems_steps_per_s": len(systems) * args.steps / (ms * 1e-3),
+                      "cell_steps_per_s": cells * args.steps / (ms * 1e-3)}), flush=True)
+    return 0
 
 
 if __name__ == "__main__":

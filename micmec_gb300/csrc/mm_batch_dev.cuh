@@ -220,11 +220,11 @@ __device__ void forces(const BArgs& a, Shared<T>& sh, const BSys& sy) {
   } else {
     cta_sum<10>(acc, sh.red);
   }
+  // (the CTA sum's barrier also orders every corner-gradient write before the gather)
   if (threadIdx.x == 0) {
     sh.ctl[C_EPOT] = acc[0];
     for (int i = 0; i < 9; ++i) sh.ctl[C_VT + i] = acc[1 + i];
   }
-  __syncthreads();  // G complete
   for (int n = threadIdx.x; n < M; n += blockDim.x) {
     const int nyz = sy.ny * sy.nz, i = n / nyz, r = n - i * nyz, j = r / sy.nz, k = r - j * sy.nz;
     T s[3] = {T(0), T(0), T(0)};
@@ -238,47 +238,97 @@ __device__ void forces(const BArgs& a, Shared<T>& sh, const BSys& sy) {
   __syncthreads();
 }
 
-// ekin and kinetic tensor into sh.ctl. FP32 cells: from an FP32 copy of the velocities,
-// summed in compensated FP32 (observables at the precision of the forces).
+// Per-node velocity updates that a kinetic-energy sum follows directly (fused into one
+// pass over the system's nodes; the thread that updates a node also sums it):
+enum { KV_NONE = 0, KV_SCALE = 1, KV_KICK = 2 };
+
+// v <- v R (row vector times a 3x3 matrix). FP32 cells: R = I + (R - I) with R - I small
+// (the exponential of a barostat half step); the increment v (R - I) is formed in FP32
+// and added to the FP64 state.
 template <typename T>
-__device__ void kinetic(const BArgs& a, double* ctl, double* red, const BSys& sy) {
+__device__ __forceinline__ void rows_times(double& x, double& y, double& z, const double* R) {
+  if constexpr (sizeof(T) == 4) {
+    const float xf = d2f_rn(x), yf = d2f_rn(y), zf = d2f_rn(z);
+    const float d0 = (float)(R[0] - 1.0), d4 = (float)(R[4] - 1.0), d8 = (float)(R[8] - 1.0);
+    const double nx = x + f2d(xf * d0 + yf * (float)R[3] + zf * (float)R[6]);
+    const double ny = y + f2d(xf * (float)R[1] + yf * d4 + zf * (float)R[7]);
+    const double nz = z + f2d(xf * (float)R[2] + yf * (float)R[5] + zf * d8);
+    x = nx;
+    y = ny;
+    z = nz;
+  } else {
+    const double nx = x * R[0] + y * R[3] + z * R[6];
+    const double ny = x * R[1] + y * R[4] + z * R[7];
+    const double nz = x * R[2] + y * R[5] + z * R[8];
+    x = nx;
+    y = ny;
+    z = nz;
+  }
+}
+
+// Velocity-Verlet half kick v += -g/m dt/2 of one component. FP32 cells: the increment
+// in FP32, added to the FP64 state.
+template <typename T>
+__device__ __forceinline__ double half_kick(double v, double g, double im, double dt) {
+  if constexpr (sizeof(T) == 4) return v + f2d((float)(0.5 * dt) * (-d2f_rn(g) * d2f_rn(im)));
+  else return v + 0.5 * (-g * im) * dt;
+}
+
+// Optional velocity update (op, see KV_*), then ekin and the kinetic tensor into ctl.
+// FP32 cells: from an FP32 copy of the velocities, summed in compensated FP32
+// (observables at the precision of the forces).
+template <typename T>
+__device__ void kinetic(const BArgs& a, double* ctl, double* red, const BSys& sy, int op = KV_NONE,
+                        const double* R = nullptr, double dt = 0.0) {
   double acc[7];
   const long long N3 = a.Ntot;
-  if constexpr (sizeof(T) == 4) {
-    F2 f[6];
-    for (int i = 0; i < 6; ++i) f[i] = F2{0.0f, 0.0f};
-    for (int n = threadIdx.x; n < sy.M; n += blockDim.x) {
-      const long long g = sy.off + n;
-      const float m = d2f_rn(a.mass[g]), v0 = d2f_rn(a.v[g]), v1 = d2f_rn(a.v[N3 + g]), v2 = d2f_rn(a.v[2 * N3 + g]);
+  typedef typename std::conditional<sizeof(T) == 4, F2, double>::type Acc;
+  Acc f[6];
+  for (int i = 0; i < 6; ++i) f[i] = Acc{};
+  for (int n = threadIdx.x; n < sy.M; n += blockDim.x) {
+    const long long g = sy.off + n;
+    double w0 = a.v[g], w1 = a.v[N3 + g], w2 = a.v[2 * N3 + g];
+    if (op == KV_SCALE) {
+      rows_times<T>(w0, w1, w2, R);
+    } else if (op == KV_KICK) {
+      const double im = a.invm[g];
+      w0 = half_kick<T>(w0, a.gpos[g], im, dt);
+      w1 = half_kick<T>(w1, a.gpos[N3 + g], im, dt);
+      w2 = half_kick<T>(w2, a.gpos[2 * N3 + g], im, dt);
+    }
+    if (op != KV_NONE) {
+      a.v[g] = w0;
+      a.v[N3 + g] = w1;
+      a.v[2 * N3 + g] = w2;
+    }
+    if constexpr (sizeof(T) == 4) {
+      const float m = d2f_rn(a.mass[g]), v0 = d2f_rn(w0), v1 = d2f_rn(w1), v2 = d2f_rn(w2);
       f[0] = f2_add(f[0], F2{m * v0 * v0, 0.0f});
       f[1] = f2_add(f[1], F2{m * v1 * v1, 0.0f});
       f[2] = f2_add(f[2], F2{m * v2 * v2, 0.0f});
       f[3] = f2_add(f[3], F2{m * v1 * v2, 0.0f});
       f[4] = f2_add(f[4], F2{m * v0 * v2, 0.0f});
       f[5] = f2_add(f[5], F2{m * v0 * v1, 0.0f});
+    } else {
+      const double m = a.mass[g];
+      f[0] += m * w0 * w0;
+      f[1] += m * w1 * w1;
+      f[2] += m * w2 * w2;
+      f[3] += m * w1 * w2;
+      f[4] += m * w0 * w2;
+      f[5] += m * w0 * w1;
     }
-    double t6[6];
+  }
+  double t6[6];
+  if constexpr (sizeof(T) == 4) {
     block_sum_f2<6>(f, t6, red);
-    if (threadIdx.x == 0) {
-      acc[0] = 0.5 * (t6[0] + t6[1] + t6[2]);
-      for (int i = 0; i < 6; ++i) acc[1 + i] = t6[i];
-    }
   } else {
-    for (int i = 0; i < 7; ++i) acc[i] = 0.0;
-    for (int n = threadIdx.x; n < sy.M; n += blockDim.x) {
-      const long long g = sy.off + n;
-      const double m = a.mass[g], v0 = a.v[g], v1 = a.v[N3 + g], v2 = a.v[2 * N3 + g];
-      acc[0] += 0.5 * m * (v0 * v0 + v1 * v1 + v2 * v2);
-      acc[1] += m * v0 * v0;
-      acc[2] += m * v1 * v1;
-      acc[3] += m * v2 * v2;
-      acc[4] += m * v1 * v2;
-      acc[5] += m * v0 * v2;
-      acc[6] += m * v0 * v1;
-    }
-    block_sum<7>(acc, red);
+    for (int i = 0; i < 6; ++i) t6[i] = f[i];
+    block_sum<6>(t6, red);
   }
   if (threadIdx.x == 0) {
+    acc[0] = 0.5 * (t6[0] + t6[1] + t6[2]);
+    for (int i = 0; i < 6; ++i) acc[1 + i] = t6[i];
     ctl[C_EKIN] = acc[0];
     const double k[9] = {acc[1], acc[6], acc[5], acc[6], acc[2], acc[4], acc[5], acc[4], acc[3]};
     for (int i = 0; i < 9; ++i) ctl[C_KT + i] = k[i];
@@ -286,60 +336,34 @@ __device__ void kinetic(const BArgs& a, double* ctl, double* red, const BSys& sy
   __syncthreads();
 }
 
-// u <- u R (positions of all nodes times a 3x3 matrix, row-vector convention); same for v.
-// FP32 cells: R = I + (R - I) with R - I small (the exponential of a barostat half step);
-// the increment u (R - I) is formed in FP32 and added to the FP64 state.
+// Positions: u <- u R (barostat scaling), or the first half kick and drift
+// (v += -g/m dt/2, u += dt v); then the cell-precision copy of u, in one pass.
+// FP32 cells: increments formed in FP32 and added to the FP64 state.
 template <typename T>
-__device__ void scale_rows(double* arr, long long N3, const BSys& sy, const double* R) {
-  if constexpr (sizeof(T) == 4) {
-    const float d0 = (float)(R[0] - 1.0), d4 = (float)(R[4] - 1.0), d8 = (float)(R[8] - 1.0);
-    const float r1 = (float)R[1], r2 = (float)R[2], r3 = (float)R[3], r5 = (float)R[5], r6 = (float)R[6],
-                r7 = (float)R[7];
-    for (int n = threadIdx.x; n < sy.M; n += blockDim.x) {
-      const long long g = sy.off + n;
-      const double x = arr[g], y = arr[N3 + g], z = arr[2 * N3 + g];
-      const float xf = d2f_rn(x), yf = d2f_rn(y), zf = d2f_rn(z);
-      arr[g] = x + f2d(xf * d0 + yf * r3 + zf * r6);
-      arr[N3 + g] = y + f2d(xf * r1 + yf * d4 + zf * r7);
-      arr[2 * N3 + g] = z + f2d(xf * r2 + yf * r5 + zf * d8);
-    }
-  } else {
-    for (int n = threadIdx.x; n < sy.M; n += blockDim.x) {
-      const long long g = sy.off + n;
-      const double x = arr[g], y = arr[N3 + g], z = arr[2 * N3 + g];
-      arr[g] = x * R[0] + y * R[3] + z * R[6];
-      arr[N3 + g] = x * R[1] + y * R[4] + z * R[7];
-      arr[2 * N3 + g] = x * R[2] + y * R[5] + z * R[8];
-    }
-  }
-}
-
-// Velocity-Verlet kick (v += -g/m dt/2) and, with drift, u += dt v. FP32 cells: the
-// increments are formed in FP32 and added to the FP64 state.
-template <typename T>
-__device__ void kick(const BArgs& a, const BSys& sy, double dt, bool drift) {
+__device__ void positions(const BArgs& a, const BSys& sy, const double* R, double dt) {
+  T* disp = (T*)a.disp;
   const long long N3 = a.Ntot;
-  if constexpr (sizeof(T) == 4) {
-    const float hf = (float)(0.5 * dt), dtf = (float)dt;
-    for (int n = threadIdx.x; n < sy.M; n += blockDim.x) {
-      const long long g = sy.off + n;
-      const float imf = d2f_rn(a.invm[g]);
-      for (int x = 0; x < 3; ++x) {
-        const double vv = a.v[x * N3 + g] + f2d(hf * (-d2f_rn(a.gpos[x * N3 + g]) * imf));
-        a.v[x * N3 + g] = vv;
-        if (drift) a.u[x * N3 + g] += f2d(dtf * d2f_rn(vv));
-      }
-    }
-  } else {
-    for (int n = threadIdx.x; n < sy.M; n += blockDim.x) {
-      const long long g = sy.off + n;
+  for (int n = threadIdx.x; n < sy.M; n += blockDim.x) {
+    const long long g = sy.off + n;
+    double x = a.u[g], y = a.u[N3 + g], z = a.u[2 * N3 + g];
+    if (R) {
+      rows_times<T>(x, y, z, R);
+    } else {
       const double im = a.invm[g];
-      for (int x = 0; x < 3; ++x) {
-        const double vv = a.v[x * N3 + g] + 0.5 * (-a.gpos[x * N3 + g] * im) * dt;
-        a.v[x * N3 + g] = vv;
-        if (drift) a.u[x * N3 + g] += dt * vv;
+      double* uu[3] = {&x, &y, &z};
+      for (int c = 0; c < 3; ++c) {
+        const double vv = half_kick<T>(a.v[c * N3 + g], a.gpos[c * N3 + g], im, dt);
+        a.v[c * N3 + g] = vv;
+        if constexpr (sizeof(T) == 4) *uu[c] += f2d((float)dt * d2f_rn(vv));
+        else *uu[c] += dt * vv;
       }
     }
+    a.u[g] = x;
+    a.u[N3 + g] = y;
+    a.u[2 * N3 + g] = z;
+    disp[g] = from_double<T>(x);
+    disp[N3 + g] = from_double<T>(y);
+    disp[2 * N3 + g] = from_double<T>(z);
   }
 }
 
@@ -394,9 +418,12 @@ __device__ void thermostat(const BArgs& a, double* c, double* red, const BSys& s
     const double f = factor;
     for (int n = threadIdx.x; n < sy.M; n += blockDim.x)
       for (int x = 0; x < 3; ++x) a.v[x * N3 + sy.off + n] *= f;
-    __syncthreads();
-    kinetic<T>(a, c, red, sy);  // ktens for the barostat; ekin re-summed
-    if (threadIdx.x == 0 && call == 1) c[C_ECT] = nhc_econs(c, p, kT);
+    // the chain scales ekin by f^2 (NHChain.__call__, nvt.py:441-446); the kinetic
+    // tensor the barostat reads next scales the same way
+    if (threadIdx.x == 0) {
+      for (int i = 0; i < 9; ++i) c[C_KT + i] *= f * f;
+      if (call == 1) c[C_ECT] = nhc_econs(c, p, kT);
+    }
     __syncthreads();
   }
 }
@@ -430,10 +457,8 @@ __device__ void baro_half(const BArgs& a, Shared<T>& sh, const BSys& sy, const B
                     r[2] * (r[3] * r[7] - r[4] * r[6]));
   }
   __syncthreads();
-  scale_rows<T>(a.u, N3, sy, sh.mat);
+  positions<T>(a, sy, sh.mat, 0.0);
   refresh_B<T>(sh, a.tt, a.ntypes, c + C_L);
-  __syncthreads();
-  write_disp<T>(a, sy);
   __syncthreads();
   forces<T, MODEL>(a, sh, sy);
   if (threadIdx.x == 0) {
@@ -443,15 +468,33 @@ __device__ void baro_half(const BArgs& a, Shared<T>& sh, const BSys& sy, const B
     sym_exp(S, -p.dt / 2, sh.mat);
   }
   __syncthreads();
-  scale_rows<T>(a.v, N3, sy, sh.mat);
-  __syncthreads();
-  kinetic<T>(a, c, sh.red, sy);
-  if (threadIdx.x == 0) update_baro_vel(c, p, chain, chain ? *cv0p : 0.0);
+  // v <- v R; the kinetic tensor follows as R^T K R (no second sum over the nodes)
+  for (int n = threadIdx.x; n < sy.M; n += blockDim.x) {
+    const long long g = sy.off + n;
+    double x = a.v[g], y = a.v[N3 + g], z = a.v[2 * N3 + g];
+    rows_times<T>(x, y, z, sh.mat);
+    a.v[g] = x;
+    a.v[N3 + g] = y;
+    a.v[2 * N3 + g] = z;
+  }
+  if (threadIdx.x == 0) {
+    const double* R = sh.mat;
+    double KR[9], K2[9];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        KR[i * 3 + j] = c[C_KT + i * 3] * R[j] + c[C_KT + i * 3 + 1] * R[3 + j] + c[C_KT + i * 3 + 2] * R[6 + j];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) K2[i * 3 + j] = R[i] * KR[j] + R[3 + i] * KR[3 + j] + R[6 + i] * KR[6 + j];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) c[C_KT + i * 3 + j] = 0.5 * (K2[i * 3 + j] + K2[j * 3 + i]);
+    c[C_EKIN] = 0.5 * (c[C_KT + 0] + c[C_KT + 4] + c[C_KT + 8]);
+    update_baro_vel(c, p, chain, chain ? *cv0p : 0.0);
+  }
   __syncthreads();
 }
 
 template <typename T, int MODEL, int BT>
-__global__ void __launch_bounds__(BT) k_batch_md(BArgs a, BMD p) {
+__global__ void __launch_bounds__(BT, (sizeof(T) == 4 && MODEL >= 1) ? 512 / BT : 1) k_batch_md(BArgs a, BMD p) {
   const int THERMO = p.thermo, BARO = p.baro;
   __shared__ Shared<T> sh;
   __shared__ double cv0;
@@ -480,14 +523,10 @@ __global__ void __launch_bounds__(BT) k_batch_md(BArgs a, BMD p) {
       if (THERMO == 1) thermostat<T, 1>(a, c, sh.red, sy, p, step, 0u, BARO == 1, kT);
       if (THERMO == 2) thermostat<T, 2>(a, c, sh.red, sy, p, step, 0u, BARO == 1, kT);
       // ---- velocity Verlet
-      kick<T>(a, sy, p.dt, true);
-      __syncthreads();
-      write_disp<T>(a, sy);
+      positions<T>(a, sy, nullptr, p.dt);
       __syncthreads();
       forces<T, MODEL>(a, sh, sy);
-      kick<T>(a, sy, p.dt, false);
-      __syncthreads();
-      kinetic<T>(a, c, sh.red, sy);
+      kinetic<T>(a, c, sh.red, sy, KV_KICK, nullptr, p.dt);
       // ---- post hooks: thermostat, then barostat
       if (THERMO == 1) thermostat<T, 1>(a, c, sh.red, sy, p, step, 1u, BARO == 1, kT);
       if (THERMO == 2) thermostat<T, 2>(a, c, sh.red, sy, p, step, 1u, BARO == 1, kT);

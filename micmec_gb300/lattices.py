@@ -67,8 +67,10 @@ def defect_grid(n, fraction, rng, clustered=False):
     """(n, n, n) grid of types: 1 (fcu) with round(fraction * n^3) cells set to 2 (reo).
 
     Uniform: the defect cells are a random subset drawn with ``rng.permutation``.
-    Clustered: face-connected clusters of 1-8 cells, each grown by a random walk
-    from a random seed cell, until the defect count is reached.
+    Clustered: face-connected clusters of 1-8 cells, each grown by a random walk of
+    ``size - 1`` face steps from a random seed cell (size ~ U{1..8}), until the defect
+    count is reached. Clusters are grown in rounds of many walkers at once (vectorised);
+    the last round is trimmed to the exact count.
     """
     shape = (n, n, n) if np.isscalar(n) else tuple(n)
     total = int(np.prod(shape))
@@ -77,21 +79,29 @@ def defect_grid(n, fraction, rng, clustered=False):
     if not clustered:
         grid[rng.permutation(total)[:ndef]] = 2
         return grid.reshape(shape)
-    grid = grid.reshape(shape)
-    steps = np.array([(1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)])
-    placed = 0
     shp = np.array(shape)
+    steps = np.array([(1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)])
+    flat = grid
+    placed = 0
     while placed < ndef:
-        size = int(rng.integers(1, 9))
-        cur = rng.integers(0, shp)
-        for _ in range(size):
-            if placed >= ndef:
-                break
-            if grid[tuple(cur)] != 2:
-                grid[tuple(cur)] = 2
-                placed += 1
-            cur = (cur + steps[rng.integers(0, 6)]) % shp
-    return grid
+        nwalk = max(1, (ndef - placed) // 4)
+        size = rng.integers(1, 9, nwalk)
+        cur = rng.integers(0, shp, size=(nwalk, 3))
+        cells = []
+        for k in range(8):
+            alive = size > k
+            idx = np.ravel_multi_index(cur[alive].T, shape)
+            cells.append(np.stack([np.nonzero(alive)[0], np.full(alive.sum(), k), idx], axis=1))
+            cur = (cur + steps[rng.integers(0, 6, nwalk)]) % shp
+        order = np.concatenate(cells)
+        order = order[np.lexsort((order[:, 1], order[:, 0]))]  # walker by walker, step by step
+        idx = order[:, 2]
+        new = idx[flat[idx] != 2]
+        _, first = np.unique(new, return_index=True)
+        new = new[np.sort(first)][: ndef - placed]
+        flat[new] = 2
+        placed += len(new)
+    return grid.reshape(shape)
 
 
 def make_lattice(grid, nstates=1, pbc=True):
