@@ -14,6 +14,11 @@ them differentiate exactly (to FP64 rounding).
 that Function, recomputing segments of ``checkpoint_every`` steps in the backward
 pass (torch.utils.checkpoint) instead of storing every step.
 
+``relaxed_stress`` gives the stress at relaxed positions, differentiable in the
+parameters through the relaxation (implicit differentiation: one Hessian solve by
+conjugate gradients on adjoint Hessian-vector products per backward pass), for losses
+on relaxed stress-strain curves.
+
 Elasticity in Voigt notation C_v (6x6, symmetric, order 00,11,22,12,02,01, as
 micmec/analysis/tensor.py:96-149 with mode="elasticity"); the kernel's stress map is
 A = C_v diag(1,1,1,2,2,2).
@@ -24,7 +29,8 @@ import torch
 
 from micmec_gb300 import _native as nat
 
-__all__ = ["MicMecParameters", "energy_and_gradient", "verlet_trajectory", "voigt21_to_tensor"]
+__all__ = ["MicMecParameters", "energy_and_gradient", "verlet_trajectory", "voigt21_to_tensor", "stress",
+           "relaxed_stress", "relaxed_stress_gradient"]
 
 _IU = np.triu_indices(6)
 _VPAIRS = [(0, 0), (1, 1), (2, 2), (1, 2), (0, 2), (0, 1)]
@@ -97,7 +103,7 @@ class MicMecParameters(object):
                                           self.temp.ctypes.data), "mm_set_params")
 
 
-def _adjoint(part, pos, lam):
+def _adjoint(part, pos, lam, dlattice=None, with_virial=False):
     dev = pos.device
     N = pos.shape[0]
     T = len(part.type_ids)
@@ -106,11 +112,30 @@ def _adjoint(part, pos, lam):
     hvp = torch.zeros((N, 3), dtype=torch.float64, device=dev) if lam is not None else None
     vt = torch.zeros(18, dtype=torch.float64, device=dev)
     pg = torch.zeros((T, 4, 46, 2), dtype=torch.float64, device=dev)
-    st = nat.lib().mm_adjoint(part.handle, pos.contiguous().data_ptr(), nat.ptr(None if lam is None else lam.contiguous()),
-                              None, energy.data_ptr(), gpos.data_ptr(), nat.ptr(hvp), vt.data_ptr(), pg.data_ptr(),
+    dl = None if dlattice is None else np.ascontiguousarray(dlattice, dtype=np.float64)
+    lam_c = None if lam is None else lam.contiguous()
+    st = nat.lib().mm_adjoint(part.handle, pos.contiguous().data_ptr(), nat.ptr(lam_c), nat.ptr(dl),
+                              energy.data_ptr(), gpos.data_ptr(), nat.ptr(hvp), vt.data_ptr(), pg.data_ptr(),
                               torch.cuda.current_stream().cuda_stream)
     nat.check(st, "mm_adjoint")
+    if with_virial:
+        return energy, gpos, hvp, pg, vt
     return energy, gpos, hvp, pg
+
+
+def _slots_to_params(slot, params, device):
+    """dL/d(raw slot) (T, 4, 46): [dE/dA (36), dE/dh0 (9), dE/dF (1)] -> (c21, h0, free energy)."""
+    dA = slot[..., :36].reshape(slot.shape[:2] + (6, 6))
+    w = torch.tensor([1.0, 1.0, 1.0, 2.0, 2.0, 2.0], dtype=torch.float64)
+    dCv = dA * w  # A = C_v diag(w)  ->  dL/dC_v[p, q] = dL/dA[p, q] w_q
+    i0, i1 = torch.as_tensor(_IU[0]), torch.as_tensor(_IU[1])
+    dC21 = dCv[..., i0, i1] + torch.where(i0 != i1, dCv[..., i1, i0], torch.zeros_like(dCv[..., i0, i1]))
+    dh0 = slot[..., 36:45].reshape(slot.shape[:2] + (3, 3))
+    ddf = slot[..., 45]
+    mask = torch.zeros(slot.shape[:2], dtype=torch.float64)
+    for t, n in enumerate(params.nstates):
+        mask[t, :n] = 1.0
+    return (dC21 * mask[..., None]).to(device), (dh0 * mask[..., None, None]).to(device), (ddf * mask).to(device)
 
 
 class _EnergyGrad(torch.autograd.Function):
@@ -134,18 +159,103 @@ class _EnergyGrad(torch.autograd.Function):
         # dL/dtheta per slot: gE * value + tangent (small: on the host)
         pg = pg.cpu()
         slot = float(gE) * pg[..., 0] + pg[..., 1]  # (T, 4, 46)
-        dA = slot[..., :36].reshape(slot.shape[:2] + (6, 6))
-        w = torch.tensor([1.0, 1.0, 1.0, 2.0, 2.0, 2.0], dtype=torch.float64)
-        dCv = dA * w  # A = C_v diag(w)  ->  dL/dC_v[p, q] = dL/dA[p, q] w_q
-        i0, i1 = torch.as_tensor(_IU[0]), torch.as_tensor(_IU[1])
-        dC21 = dCv[..., i0, i1] + torch.where(i0 != i1, dCv[..., i1, i0], torch.zeros_like(dCv[..., i0, i1]))
-        dh0 = slot[..., 36:45].reshape(slot.shape[:2] + (3, 3))
-        ddf = slot[..., 45]
-        mask = torch.zeros(slot.shape[:2], dtype=torch.float64)
-        for t, n in enumerate(params.nstates):
-            mask[t, :n] = 1.0
-        return (grad_pos, (dC21 * mask[..., None]).to(c21.device), (dh0 * mask[..., None, None]).to(h0.device),
-                (ddf * mask).to(df.device), None)
+        dC21, dh0, ddf = _slots_to_params(slot, params, c21.device)
+        return grad_pos, dC21, dh0, ddf, None
+
+
+def _hessian_solve(part, pos, rhs, tol=1e-11, maxiter=5000):
+    """mu with H mu = rhs (H = d2E/dx2 at pos, FP64 adjoint products) by conjugate
+    gradients on the translation-free subspace (rhs and iterates have zero mean)."""
+
+    def H(p):
+        return _adjoint(part, pos, p)[2]
+
+    b = rhs - rhs.mean(dim=0)
+    x = torch.zeros_like(b)
+    r = b.clone()
+    p = r.clone()
+    rr = float((r * r).sum())
+    b2 = float((b * b).sum())
+    if b2 == 0.0:
+        return x
+    for _ in range(maxiter):
+        Ap = H(p)
+        Ap = Ap - Ap.mean(dim=0)
+        alpha = rr / float((p * Ap).sum())
+        x = x + alpha * p
+        r = r - alpha * Ap
+        rr_new = float((r * r).sum())
+        if rr_new <= tol * tol * b2:
+            break
+        p = r + (rr_new / rr) * p
+        rr = rr_new
+    return x
+
+
+def stress(pos, params):
+    """Stress tensor sigma = vtens / V (3x3, FP64) at device positions pos."""
+    part = params.part
+    params.upload(params.c21, params.h0, params.free_energy)
+    vt = _adjoint(part, pos.detach(), None, with_virial=True)[4]
+    return vt[:9].reshape(3, 3) / float(part.system.domain.volume)
+
+
+def relaxed_stress_gradient(pos, params, w, tol=1e-11):
+    """Stress at relaxed positions and the total parameter derivative of s = sum(w * sigma).
+
+    pos: device (N, 3) positions at an energy minimum for the current parameters (the
+    caller relaxes them); w: (3, 3) weights (e.g. dLoss/dsigma). The relaxed positions
+    move with the parameters, x*(theta) with g(x*, theta) = 0, so
+    ds/dtheta = ds/dtheta|_x - mu . dg/dtheta with H mu = ds/dx (implicit differentiation).
+    The homogeneous deformation pos -> pos (I + eps), L -> L (I + eps) with eps = w^T is the
+    tangent whose energy derivative is sum(w * vtens); in the kernel's variables
+    (u = pos - X(L), L) it is (u eps, L eps). One adjoint evaluation along that tangent
+    gives V ds/dtheta|_x and the Hessian part of V ds/dx; conjugate gradients with
+    adjoint Hessian products give mu; a last adjoint evaluation with lam = mu gives
+    mu . dg/dtheta. Returns (sigma (3, 3) tensor, d/dc21, d/dh0, d/dfree_energy).
+    """
+    part = params.part
+    params.upload(params.c21, params.h0, params.free_energy)
+    dev = pos.device
+    V = float(part.system.domain.volume)
+    L = part.lattice_matrix()
+    eps = np.asarray(w, dtype=np.float64).T
+    D = L @ eps
+    nc = torch.tensor(np.asarray(part.node_coords, dtype=np.float64), device=dev)
+    epst = torch.tensor(eps, device=dev)
+    pos = pos.detach()
+    lam = pos @ epst - nc @ torch.tensor(D, device=dev)
+    _, g, hvp, pg, vt = _adjoint(part, pos, lam, D, with_virial=True)
+    sigma = vt[:9].reshape(3, 3) / V
+    q = (hvp + g @ epst.T) / V  # ds/dx: Hessian-tangent part + derivative of the tangent u eps
+    mu = _hessian_solve(part, pos, q, tol=tol)
+    pg_mu = _adjoint(part, pos, mu)[3]
+    slot = (pg[..., 1] / V - pg_mu[..., 1]).cpu()
+    dC21, dh0, ddf = _slots_to_params(slot, params, params.c21.device)
+    return sigma, dC21, dh0, ddf
+
+
+class _RelaxedStress(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, c21, h0, df, params, pos):
+        params.upload(c21, h0, df)
+        vt = _adjoint(params.part, pos.detach(), None, with_virial=True)[4]
+        ctx.params = params
+        ctx.save_for_backward(pos.detach())
+        return vt[:9].reshape(3, 3) / float(params.part.system.domain.volume)
+
+    @staticmethod
+    def backward(ctx, gs):
+        pos, = ctx.saved_tensors
+        _, dC21, dh0, ddf = relaxed_stress_gradient(pos, ctx.params, gs.detach().cpu().numpy())
+        return dC21, dh0, ddf, None, None
+
+
+def relaxed_stress(pos, params):
+    """Stress (3, 3) at relaxed device positions ``pos``, differentiable in the parameters
+    through the relaxation (the caller relaxes ``pos`` for the current parameters)."""
+    c21, h0, df = params.tensors()
+    return _RelaxedStress.apply(c21, h0, df, params, pos)
 
 
 def energy_and_gradient(pos, params):

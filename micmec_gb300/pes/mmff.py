@@ -262,6 +262,14 @@ class ForcePartMechanical(ForcePart):
     def handle(self):
         return self._handle
 
+    def lattice_matrix(self):
+        """Rows L_d: the lattice translation between neighbouring nodes along d (rvecs_d / n_d
+        for a periodic domain, the mean edge vector for an isolated one)."""
+        if self._lattice is not None:
+            return np.array(self._lattice)
+        rv = np.asarray(self.system.domain.rvecs, dtype=np.float64).reshape(3, 3)
+        return rv / np.asarray(self.lattice_shape, dtype=np.float64)[:, None]
+
     # ---------------------------------------------------------------- API
     def update_rvecs(self, rvecs):
         ForcePart.update_rvecs(self, rvecs)

@@ -129,3 +129,74 @@ def test_trajectory_gradient_with_checkpointing():
         floor = 1e-13 * abs(l0.item()) / h
         assert abs(fd - grad[idx].item()) <= 1e-6 * max(abs(fd), 1e-3 * grad.abs().max().item()) + floor, \
             (idx, fd, grad[idx])
+
+
+def test_relaxed_stress_loss_gradient_matches_central_differences():
+    """Loss on relaxed stresses over strain points (each point relaxed for the current
+    parameters): the implicit-differentiation gradient against central differences that
+    re-relax every point (h = 1e-4 relative)."""
+    import torch
+    from scipy.optimize import minimize
+
+    from micmec_gb300.autograd import energy_and_gradient, relaxed_stress
+
+    s, part, params, pos, rng = _setup(n=3, seed=4)
+    base_rv = np.array(s.domain.rvecs)
+    pos0 = np.array(s.pos)
+    strains = [0.0, 0.01, 0.02]
+    targets = [torch.tensor(rng.normal(size=(3, 3)) * 1e-5, dtype=torch.float64, device="cuda") for _ in strains]
+
+    def relax(x0):
+        def f(x):
+            pt = torch.tensor(x.reshape(-1, 3), dtype=torch.float64, device="cuda")
+            with torch.no_grad():
+                E, g = energy_and_gradient(pt, params)
+            return float(E), g.cpu().numpy().ravel()
+
+        r = minimize(f, x0.ravel(), jac=True, method="L-BFGS-B",
+                     options=dict(gtol=1e-14, ftol=1e-22, maxiter=20000, maxcor=40))
+        return r.x.reshape(-1, 3)
+
+    def set_strain(e):
+        F = np.eye(3)
+        F[0, 0] += e
+        rv = base_rv @ F
+        s.domain.update_rvecs(rv)
+        part.update_rvecs(rv)
+        return F
+
+    def loss_value():
+        total = 0.0
+        for e, tgt in zip(strains, targets):
+            F = set_strain(e)
+            x = torch.tensor(relax(pos0 @ F), dtype=torch.float64, device="cuda")
+            with torch.no_grad():
+                sig = relaxed_stress(x, params)
+            total += float(((sig - tgt) ** 2).sum())
+        return total
+
+    # analytic gradient
+    grads = [torch.zeros_like(t) for t in params.tensors()]
+    for e, tgt in zip(strains, targets):
+        F = set_strain(e)
+        x = torch.tensor(relax(pos0 @ F), dtype=torch.float64, device="cuda")
+        sig = relaxed_stress(x, params)
+        loss = ((sig - tgt) ** 2).sum()
+        for acc, gr in zip(grads, torch.autograd.grad(loss, list(params.tensors()))):
+            acc += gr
+    # central differences on a few parameters: C11 (type 0, state 0), h0_xx (type 1,
+    # state 1), the free energy of type 0 state 1
+    picks = [(0, (0, 0, 0)), (1, (1, 1, 0, 0)), (2, (0, 1))]
+    for which, idx in picks:
+        t = params.tensors()[which]
+        v0 = float(t.data[idx])
+        h = 1e-4 * abs(v0) if v0 != 0.0 else 1e-4 * float(t.data.abs().max())
+        with torch.no_grad():
+            t.data[idx] = v0 + h
+            lp = loss_value()
+            t.data[idx] = v0 - h
+            lm = loss_value()
+            t.data[idx] = v0
+        fd = (lp - lm) / (2 * h)
+        an = float(grads[which][idx])
+        assert abs(an - fd) <= 1e-4 * abs(fd) + 1e-8 * abs(lp) / h, (which, idx, an, fd)
