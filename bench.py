@@ -364,11 +364,12 @@ def measure_plain_per_system(systems, nsteps):
             "cell_steps_per_s": sum(s.ncells for s in systems) * nsteps / t}
 
 
-def measure_large_mtk(n=256, nsteps=20, fp64_steps=4):
+def measure_large_mtk(n=256, nsteps=20, cmp_steps=4):
     """Large single system (periodic n^3 lattice, 20% clustered defects, two states per
     type) under NHC + MTK NPT at 300 K and 100 MPa, dt = 2 fs, through VerletIntegrator
-    (device=True routes it to the lattice engine); FP32 cells, and a short FP64 run from
-    the same state for the conserved-energy drift."""
+    (device=True routes it to the lattice engine). FP64 and FP32 cells run the same
+    cmp_steps steps from the same state (conserved quantity compared at the end); the FP32
+    run then continues for nsteps timed steps."""
     import torch
 
     from micmec_gb300 import lattices, units
@@ -389,38 +390,51 @@ def measure_large_mtk(n=256, nsteps=20, fp64_steps=4):
            "host_setup_s": t_setup}
 
     class Econs(Hook):
-        # called after the warm-up and at the end only (a per-step host hook would
+        # fires after step 2 and after step 2 + cmp_steps only (a per-step host hook would
         # bring the state back to the host every step)
-        def __init__(self, start, step):
-            Hook.__init__(self, start, step)
+        def __init__(self):
+            Hook.__init__(self, 2, cmp_steps)
             self.rows = []
 
         def __call__(self, it):
             self.rows.append((it.counter, it.econs, it.epot))
 
     vel = None
-    for prec, steps in (("fp32", nsteps), ("fp64", fp64_steps)):
+    end = {}
+    for prec in ("fp64", "fp32"):
         s = System.from_dict(d)
         if vel is None:
             vel = rng.normal(0.0, 1.0, s.pos.shape) * np.sqrt(kT / s.masses)[:, None]
             vel -= (s.masses @ vel) / s.masses.sum()
         ff = MicMecForceField(s, [ForcePartMechanical(s, precision=prec)])
-        rec = Econs(2, steps)
+        rec = Econs()
         hooks = [NHCThermostat(300.0, timecon=100 * units.femtosecond),
                  MTKBarostat(ff, 300.0, 100e6 * units.pascal, timecon=1000 * units.femtosecond), rec]
         vi = VerletIntegrator(ff, 2.0 * units.femtosecond, hooks=hooks, vel0=vel.copy(), device=True)
         vi.run(2)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        vi.run(steps)
+        vi.run(cmp_steps)
         torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
-        rows = np.array(rec.rows[-2:])
-        e = rows[:, 1]
-        out[prec] = {"steps": steps, "s": dt, "cell_steps_per_s": n ** 3 * steps / dt,
-                     "econs_drift_per_step_rel": float((e[-1] - e[0]) / steps / abs(rows[0, 2]))}
+        t_cmp = time.perf_counter() - t0
+        (c0, e0, p0), (c1, e1, p1) = rec.rows[-2], rec.rows[-1]
+        end[prec] = (e1, p1)
+        res = {"econs_change_over_cmp_steps": e1 - e0, "epot": p1}
+        if prec == "fp64":
+            res.update({"steps": cmp_steps, "s": t_cmp, "cell_steps_per_s": n ** 3 * cmp_steps / t_cmp})
+        else:
+            rec.step = 10 ** 9  # no further host hook calls in the timed run
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            vi.run(nsteps)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            res.update({"steps": nsteps, "s": dt, "cell_steps_per_s": n ** 3 * nsteps / dt})
+        out[prec] = res
         del vi, ff, s
         torch.cuda.empty_cache()
+    out["cmp_steps"] = cmp_steps
+    out["econs_fp32_minus_fp64_rel"] = float((end["fp32"][0] - end["fp64"][0]) / abs(end["fp64"][1]))
     return out
 
 
@@ -455,7 +469,44 @@ def measure_grad_over_fwd(n=16, reps=5):
         fwd.append(t1 - t0)
         bwd.append(t2 - t1)
     f, b = float(np.median(fwd[1:])), float(np.median(bwd[1:]))
-    return {"lattice": [n] * 3, "forward_ms": 1e3 * f, "backward_ms": 1e3 * b, "grad_over_fwd": b / f}
+    # central differences (h = 1e-4 relative) of the same loss for three parameters
+    gc, gh, gd = torch.autograd.grad((w * energy_and_gradient(pos, params)[1]).sum(),
+                                     [params.c21, params.h0, params.free_energy])
+    errs = []
+    for tensor, grad, idx in ((params.c21, gc, (0, 0, 0)), (params.c21, gc, (1, 1, 3)), (params.h0, gh, (0, 0, 1, 1))):
+        base = float(tensor.detach()[idx])
+        h = 1e-4 * abs(base)
+        vals = []
+        for sgn in (1, -1):
+            with torch.no_grad():
+                tensor[idx] = base + sgn * h
+                vals.append(float((w * energy_and_gradient(pos, params)[1]).sum()))
+        with torch.no_grad():
+            tensor[idx] = base
+        fd = (vals[0] - vals[1]) / (2 * h)
+        errs.append(abs(float(grad[idx]) - fd) / abs(fd))
+    return {"lattice": [n] * 3, "forward_ms": 1e3 * f, "backward_ms": 1e3 * b, "grad_over_fwd": b / f,
+            "fd_rel_err_max": max(errs), "fd_h": "1e-4 relative"}
+
+
+def force_error_fp32(s):
+    """Relative force and energy error of the FP32-cell path against the FP64 path (itself
+    equal to the reference's forces to 1e-10) at the same positions."""
+    from micmec_gb300.pes.mmff import ForcePartMechanical
+
+    out = {}
+    res = {}
+    for prec in ("fp64", "fp32"):
+        fp = ForcePartMechanical(s, model="nanocell", precision=prec)
+        g = np.zeros((s.nnodes, 3))
+        v = np.zeros((3, 3))
+        e = fp.compute(g, v)
+        res[prec] = (e, g, v)
+    (e64, g64, v64), (e32, g32, v32) = res["fp64"], res["fp32"]
+    out["force_rel_err"] = float(np.abs(g32 - g64).max() / np.abs(g64).max())
+    out["energy_rel_err"] = float(abs(e32 - e64) / abs(e64))
+    out["virial_rel_err"] = float(np.abs(v32 - v64).max() / np.abs(v64).max())
+    return out
 
 
 def host_link_rates(pinned, dev, reps=5):
@@ -610,6 +661,7 @@ def run_gpu(args):
             v64, ms64 = measure_lattice(s, vel, max(5, min(args.steps, 30)), flush, "fp64")
             line["fp64_lattice"] = {"value": v64, "unit": UNIT, "ms_per_step": ms64,
                                     "fp32_over_fp64": value / world / v64}
+            line["fp32_error_vs_fp64"] = force_error_fp32(s)
             from micmec_gb300.system import System
 
             sg = System.from_dict(general_form(d))
@@ -620,6 +672,9 @@ def run_gpu(args):
             bf = measure_batch(systems, strains, "fp32", 200, 400)
             bd = measure_batch(systems, strains, "fp64", 20, 100)
             plain = measure_plain_per_system(systems[:6], 10)
+            sx32 = np.array(list(bf["stress_xx_gpa_by_strain"].values()))
+            sx64 = np.array(list(bd["stress_xx_gpa_by_strain"].values()))
+            bf["stress_rel_err_vs_fp64"] = float(np.abs(sx32 - sx64).max() / np.abs(sx64).max())
             line["batched"] = {"fp32": bf, "fp64": bd, "plain_fp64_per_system": plain,
                                "batched_fp32_over_plain_fp64_systems_per_s":
                                    bf["systems_steps_per_s"] / plain["systems_steps_per_s"]}
