@@ -143,6 +143,16 @@ class ClockSampler(object):
         }
 
 
+def max_over_ranks(x, dist, device):
+    """Largest value of x over all ranks of the default process group (the step time
+    that the whole job waited for)."""
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -510,29 +520,40 @@ def force_error_fp32(s):
 
 
 def host_link_rates(pinned, dev, reps=5):
-    """Pinned host <-> device copy rates (GB/s) for one array of the e2e step, and for
-    three such copies on three streams (what the host-buffer step issues)."""
+    """Pinned host <-> device copy rates (GB/s) for the three arrays of the e2e step,
+    copied as 1 stream per array (x3) and as 2 halves per array on 6 streams (x6), and
+    for one array alone (x1)."""
     import torch
 
     n = pinned.numel()
-    h = [pinned.clone().pin_memory() for _ in range(3)]
-    d = [torch.empty(n, dtype=pinned.dtype, device=dev).view(pinned.shape) for _ in range(3)]
-    streams = [torch.cuda.Stream(dev) for _ in range(3)]
+    h = [pinned.clone().reshape(-1).pin_memory() for _ in range(3)]
+    d = [torch.empty(n, dtype=pinned.dtype, device=dev) for _ in range(3)]
+    streams = [torch.cuda.Stream(dev) for _ in range(6)]
     out = {}
-    for name, fn in (("h2d", lambda i: d[i].copy_(h[i], non_blocking=True)),
-                     ("d2h", lambda i: h[i].copy_(d[i], non_blocking=True))):
-        for k in (1, 3):
+    for name in ("h2d", "d2h"):
+        for k in (1, 3, 6):
+            pieces = []
+            if k == 1:
+                pieces = [(0, 0, n)]
+            elif k == 3:
+                pieces = [(i, 0, n) for i in range(3)]
+            else:
+                pieces = [(i, j * (n // 2), (j + 1) * (n // 2) if j == 0 else n) for i in range(3) for j in range(2)]
             best = None
             for _ in range(reps):
                 torch.cuda.synchronize()
                 t0 = time.perf_counter()
-                for i in range(k):
-                    with torch.cuda.stream(streams[i]):
-                        fn(i)
+                for sidx, (i, lo, hi) in enumerate(pieces):
+                    with torch.cuda.stream(streams[sidx]):
+                        if name == "h2d":
+                            d[i][lo:hi].copy_(h[i][lo:hi], non_blocking=True)
+                        else:
+                            h[i][lo:hi].copy_(d[i][lo:hi], non_blocking=True)
                 torch.cuda.synchronize()
                 dt = time.perf_counter() - t0
                 best = dt if best is None else min(best, dt)
-            out["%s_gbs_x%d" % (name, k)] = k * pinned.numel() * pinned.element_size() / best / 1e9
+            nbytes = sum(hi - lo for _, lo, hi in pieces) * pinned.element_size()
+            out["%s_gbs_x%d" % (name, k)] = nbytes / best / 1e9
     return out
 
 
@@ -595,9 +616,7 @@ def run_gpu(args):
     clk = clocks.stop()
     ms = float(sum(a.elapsed_time(b) for a, b in ev))
     if pg is not None:
-        t = torch.tensor([ms], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, pg, dev)
     recs = rec.cpu().numpy()
     finite = bool(np.isfinite(recs[: args.steps, :2]).all())
     value = world * M * args.steps / (ms * 1e-3)

@@ -15,6 +15,7 @@
 // W = (L - h0) + dU: a small number in every precision.
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -108,11 +109,11 @@ __device__ __forceinline__ void fill_type_scalars(TypeParams<T>& dst, const Type
 // SIMPLE: every rest matrix is diagonal and every stress map has cubic form
 // (A00 = A11 = A22, A01 = A02 = A12 and symmetric, A33 = A44 = A55, all else 0); the
 // products with h0^-1 and A then reduce to scalings (detected exactly on the host).
-template <typename T, bool SIMPLE = false>
-__device__ __forceinline__ T state_energy_grad(const T* __restrict__ W, const StateParams<T>& p, T scale,
+template <typename T, bool SIMPLE = false, typename P = StateParams<T>>
+__device__ __forceinline__ T state_energy_grad(const T* __restrict__ W, const P& p, T scale,
                                                T* __restrict__ GW) {
   T D[9];
-  if (SIMPLE) {
+  if constexpr (SIMPLE) {
     const T h[3] = {p.hd[0], p.hd[1], p.hd[2]};
 #pragma unroll
     for (int i = 0; i < 3; ++i)
@@ -134,7 +135,7 @@ __device__ __forceinline__ T state_energy_grad(const T* __restrict__ W, const St
   e[4] = h * (D[2] + D[6] + D[0] * D[2] + D[3] * D[5] + D[6] * D[8]);
   e[5] = h * (D[1] + D[3] + D[0] * D[1] + D[3] * D[4] + D[6] * D[7]);
   T s[6];
-  if (SIMPLE) {
+  if constexpr (SIMPLE) {
     const T amb = p.cub[0], b = p.cub[1], c = p.cub[2];
     const T tr = e[0] + e[1] + e[2];
     s[0] = amb * e[0] + b * tr;
@@ -163,7 +164,7 @@ __device__ __forceinline__ T state_energy_grad(const T* __restrict__ W, const St
     for (int l = 0; l < 3; ++l)
       GF[i * 3 + l] = S[i * 3 + l] + D[i * 3 + 0] * S[0 * 3 + l] + D[i * 3 + 1] * S[1 * 3 + l] + D[i * 3 + 2] * S[2 * 3 + l];
   // GW[j][i] = scale * sum_k GF[i][k] hinv[k][j]
-  if (SIMPLE) {
+  if constexpr (SIMPLE) {
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
       const T sj = scale * p.hd[j];
@@ -450,6 +451,30 @@ inline FastDiv make_fastdiv(uint32_t d) {
 }
 __device__ __forceinline__ int fdiv(int n, FastDiv f) { return (int)((__umulhi((uint32_t)n, f.m) + (uint32_t)n) >> f.l); }
 
+// The part of StateParams the cubic form reads, loaded with four 16-byte shared-memory
+// loads (FP32: B[9], v0, df, hd[3], cub[3] are the first 17 of 20 aligned floats).
+template <typename T>
+struct CubicView {
+  T B[9];
+  T v0, df;
+  T hd[3];
+  T cub[3];
+};
+__device__ __forceinline__ void load_cubic(const StateParams<float>& p, CubicView<float>& c) {
+  const float4* q = reinterpret_cast<const float4*>(&p);
+  const float4 q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3];
+  const float q4 = p.cub[2];
+  c.B[0] = q0.x; c.B[1] = q0.y; c.B[2] = q0.z; c.B[3] = q0.w;
+  c.B[4] = q1.x; c.B[5] = q1.y; c.B[6] = q1.z; c.B[7] = q1.w;
+  c.B[8] = q2.x; c.v0 = q2.y; c.df = q2.z; c.hd[0] = q2.w;
+  c.hd[1] = q3.x; c.hd[2] = q3.y; c.cub[0] = q3.z; c.cub[1] = q3.w;
+  c.cub[2] = q4;
+}
+static_assert(offsetof(StateParams<float>, B) == 0 && offsetof(StateParams<float>, v0) == 36 &&
+                  offsetof(StateParams<float>, df) == 40 && offsetof(StateParams<float>, hd) == 44 &&
+                  offsetof(StateParams<float>, cub) == 56,
+              "load_cubic assumes this layout");
+
 // Eight lanes per cell (eight-corner-matrix model). Lane a (corner offset bits) of an
 // aligned 8-lane group holds the displacement du of vertex a; it evaluates corner
 // matrix a for every state of the cell's type. Edges to the neighbours a^1, a^2,
@@ -473,55 +498,74 @@ __device__ __forceinline__ T cell8_eval(const T (&du)[3], int a, const TypeParam
   }
   const int ns_lane = valid ? tpl.nstates : 1;
   const int ns = __reduce_max_sync(0xffffffffu, ns_lane);
-  g[0] = g[1] = g[2] = T(0);
+  // state-weighted row gradients of matrix a (online -kT log-sum-exp weights); the
+  // exchange with the neighbouring matrices happens once, after the state loop
+  T Gacc[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) Gacc[i] = T(0);
   T m = T(0), wsum = T(0);
   const T kT = tpl.kT;
   for (int s = 0; s < ns; ++s) {
     const bool active = s < ns_lane;
     const StateParams<T>& p = tpl.s[active ? s : 0];
-    T W[9], GW[9];
+    T W[9], GW[9], Es, df;
+    if constexpr (SIMPLE && sizeof(T) == 4) {
+      CubicView<float> cv;
+      load_cubic(p, cv);
 #pragma unroll
-    for (int d = 0; d < 3; ++d)
+      for (int d = 0; d < 3; ++d)
 #pragma unroll
-      for (int x = 0; x < 3; ++x) W[d * 3 + x] = p.B[d * 3 + x] + ed[d][x];
-    T Es = state_energy_grad<T, SIMPLE>(W, p, T(0.125) * p.v0, GW);
+        for (int x = 0; x < 3; ++x) W[d * 3 + x] = cv.B[d * 3 + x] + ed[d][x];
+      Es = state_energy_grad<T, true, CubicView<float>>(W, cv, T(0.125) * cv.v0, GW);
+      df = cv.df;
+    } else {
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int x = 0; x < 3; ++x) W[d * 3 + x] = p.B[d * 3 + x] + ed[d][x];
+      Es = state_energy_grad<T, SIMPLE>(W, p, T(0.125) * p.v0, GW);
+      df = p.df;
+    }
     Es += __shfl_xor_sync(0xffffffffu, Es, 1);
     Es += __shfl_xor_sync(0xffffffffu, Es, 2);
     Es += __shfl_xor_sync(0xffffffffu, Es, 4);
-    T gs[3] = {T(0), T(0), T(0)};
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const T sg = ((a >> d) & 1) ? T(1) : T(-1);
-#pragma unroll
-      for (int x = 0; x < 3; ++x) {
-        const T mine = GW[d * 3 + x];
-        gs[x] += sg * (mine + __shfl_xor_sync(0xffffffffu, mine, 1 << d));
-      }
-    }
     if (active) {
-      const T E = Es + p.df;
+      const T E = Es + df;
       if (s == 0) {
         m = E;
         wsum = T(1);
 #pragma unroll
-        for (int x = 0; x < 3; ++x) g[x] = gs[x];
+        for (int i = 0; i < 9; ++i) Gacc[i] = GW[i];
       } else if (E < m) {
         const T r = lse_weight<T>(E - m, kT, tpl.lkT);
         wsum = wsum * r + T(1);
 #pragma unroll
-        for (int x = 0; x < 3; ++x) g[x] = g[x] * r + gs[x];
+        for (int i = 0; i < 9; ++i) Gacc[i] = Gacc[i] * r + GW[i];
         m = E;
       } else {
         const T w = lse_weight<T>(m - E, kT, tpl.lkT);
         wsum += w;
 #pragma unroll
-        for (int x = 0; x < 3; ++x) g[x] += w * gs[x];
+        for (int i = 0; i < 9; ++i) Gacc[i] += w * GW[i];
       }
+    }
+  }
+  // vertex a's gradient: row d of matrix a and of matrix a^(1<<d) (the same edge)
+  g[0] = g[1] = g[2] = T(0);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const T sg = ((a >> d) & 1) ? T(1) : T(-1);
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+      const T mine = Gacc[d * 3 + x];
+      g[x] += sg * (mine + __shfl_xor_sync(0xffffffffu, mine, 1 << d));
     }
   }
   T Ecell = m;
   if (ns_lane > 1) {
-    const T inv = T(1) / wsum;
+    T inv;
+    if constexpr (sizeof(T) == 4) inv = __frcp_rn(wsum);
+    else inv = T(1) / wsum;
 #pragma unroll
     for (int x = 0; x < 3; ++x) g[x] *= inv;
     Ecell = m - kT * lse_log<T>(wsum);

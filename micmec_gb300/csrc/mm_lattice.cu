@@ -39,6 +39,9 @@ namespace {
 constexpr int kCellThreads = 128;
 constexpr int kNodeThreads = 256;
 constexpr int kMDThreads = 1024;  // node-update blocks: one resident block per SM, few partials
+// FP32 node update: per-thread staging slots for 24 gradient floats, v and u (3 doubles each)
+// and the mass data (one float4)
+constexpr size_t kMDStageBytes = (size_t)kMDThreads * (24 * 4 + 6 * 8 + 16);
 constexpr int kCellPart = 10;  // energy + virial(9)
 constexpr int kNodePart = 9;   // ekin_a, ekin_b, ekin_c, ktens(6)
 
@@ -86,6 +89,20 @@ __device__ __forceinline__ int struct_corner_cell(const Topo& t, int i, int j, i
   c = (c < 0) ? t.nz - 1 : c;
   return (a * t.ny + b) * t.nz + c;
 }
+
+// Asynchronous global -> shared copies (cp.async, no registers held while in flight);
+// each thread waits for its own copies only.
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((unsigned)__cvta_generic_to_shared(smem)), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((unsigned)__cvta_generic_to_shared(smem)), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(smem)), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 // Build the per-block parameter table in precision T from the FP64 table and
 // the current lattice matrix L: B = L - h0 is formed in FP64, then rounded.
@@ -515,6 +532,7 @@ __global__ void __launch_bounds__(kMDThreads, 1) k_md_nodes(Topo t, MDArgs p, co
   __shared__ double red[kNodePart * (kMDThreads / 32)];
   __shared__ double ctot[kCellPart];
   __shared__ bool last;
+  extern __shared__ __align__(16) float md_stage[];  // FP32 cells: per-thread input slots (kMDStageBytes)
   // blocks 0 .. nb-1 update the nodes; block nb (the last one) sums the cell kernel's
   // partials meanwhile, so the block that finishes last has only nb node partials left
   const int nb = gridDim.x - 1;
@@ -545,7 +563,7 @@ __global__ void __launch_bounds__(kMDThreads, 1) k_md_nodes(Topo t, MDArgs p, co
   R obs[kNodePart];
 #pragma unroll
   for (int i = 0; i < kNodePart; ++i) obs[i] = R(0);
-  if (sizeof(T) == 4) {
+  if constexpr (sizeof(T) == 4) {
     // FP32 cells: the velocity and position increments of the whole step are formed in
     // FP32, the state update itself is FP64:
     //   v' = cv v + q,  u' = u + dt v'
@@ -553,48 +571,84 @@ __global__ void __launch_bounds__(kMDThreads, 1) k_md_nodes(Topo t, MDArgs p, co
     // cv = c1, q = c1 h a + n1; (start only) cv = c1, q = h a + n2; h = dt/2, a = -g/m,
     // n1/n2 the post/pre thermostat noise terms (c1 = 1, n = 0 without a thermostat).
     // The observables come from an FP32 copy of the same velocity sequence.
-    T s[3];
-    gather_node<T, STRUCT>(t, G, n, s);
-    const float4 nf = nodef[n];  // mass, 1/mass, Langevin amplitude
-    const float hf = p.hf;
-    float af[3], n1[3] = {0.f, 0.f, 0.f}, n2[3] = {0.f, 0.f, 0.f};
+    // The node's inputs (24 corner-gradient values, v, u, mass data) are staged in this
+    // thread's shared-memory slots with asynchronous copies; the Langevin draws are
+    // computed while they are in flight.
+    // regions (bases, then this thread's slot in each): gradients [24][kMDThreads] floats,
+    // v [3][kMDThreads] and u [3][kMDThreads] doubles, mass data [kMDThreads] float4
+    double* const v_base = reinterpret_cast<double*>(md_stage + 24 * kMDThreads);
+    double* const u_base = v_base + 3 * kMDThreads;
+    float4* const nf_base = reinterpret_cast<float4*>(u_base + 3 * kMDThreads);
+    float* const sg = md_stage + threadIdx.x;
+    double* const sv = v_base + threadIdx.x;
+    double* const su = u_base + threadIdx.x;
+    float4* const snf = nf_base + threadIdx.x;
+    {
+      int ci = 0, cj = 0, ck = 0;
+      if (STRUCT) split_index(t, n, ci, cj, ck);
 #pragma unroll
-    for (int x = 0; x < 3; ++x) af[x] = -(float)s[x] * nf.y;
-    if (gpos_out)
+      for (int kc = 0; kc < 8; ++kc) {
+        const int cell = STRUCT ? struct_corner_cell(t, ci, cj, ck, corner_to_bits(kc)) : t.node_cells[kc * t.N + n];
 #pragma unroll
-      for (int x = 0; x < 3; ++x) gpos_out[3 * n + x] = f2d(s[x]);
+        for (int x = 0; x < 3; ++x) {
+          float* dst = sg + (kc * 3 + x) * kMDThreads;
+          if (cell >= 0) cp_async4(dst, G + (kc * 3 + x) * (size_t)t.M + cell);
+          else *dst = 0.0f;
+        }
+      }
+#pragma unroll
+      for (int x = 0; x < 3; ++x) {
+        cp_async8(sv + x * kMDThreads, v + x * (size_t)t.N + n);
+        if (p.start) cp_async8(su + x * kMDThreads, u + x * (size_t)t.N + n);
+      }
+      cp_async16(snf, nodef + n);
+      cp_async_commit();
+    }
+    float z1[3] = {0.f, 0.f, 0.f}, z2[3] = {0.f, 0.f, 0.f};
     if (THERMO == MM_THERMO_LANGEVIN) {
       if (p.finish) {
         if (noise) {
           const size_t base = ((size_t)(p.step - p.noise_step0) * 2 + 1) * (size_t)t.N * 3;
 #pragma unroll
-          for (int x = 0; x < 3; ++x) n1[x] = nf.z * d2f_rn(noise[base + 3 * n + x]);
+          for (int x = 0; x < 3; ++x) z1[x] = d2f_rn(noise[base + 3 * n + x]);
         } else {
-          float zf[3];
-          normal3(p.seed, (uint32_t)n, (uint32_t)p.step, 1u, zf);
-#pragma unroll
-          for (int x = 0; x < 3; ++x) n1[x] = nf.z * zf[x];
+          normal3(p.seed, (uint32_t)n, (uint32_t)p.step, 1u, z1);
         }
       }
       if (p.start) {
         if (noise) {
           const size_t base = ((size_t)(p.step + 1 - p.noise_step0) * 2 + 0) * (size_t)t.N * 3;
 #pragma unroll
-          for (int x = 0; x < 3; ++x) n2[x] = nf.z * d2f_rn(noise[base + 3 * n + x]);
+          for (int x = 0; x < 3; ++x) z2[x] = d2f_rn(noise[base + 3 * n + x]);
         } else {
-          float zf[3];
-          normal3(p.seed, (uint32_t)n, (uint32_t)(p.step + 1), 0u, zf);
-#pragma unroll
-          for (int x = 0; x < 3; ++x) n2[x] = nf.z * zf[x];
+          normal3(p.seed, (uint32_t)n, (uint32_t)(p.step + 1), 0u, z2);
         }
       }
     }
+    cp_async_wait_all();
+    T s[3] = {T(0), T(0), T(0)};
+#pragma unroll
+    for (int kc = 0; kc < 8; ++kc)
+#pragma unroll
+      for (int x = 0; x < 3; ++x) s[x] += sg[(kc * 3 + x) * kMDThreads];
+    const float4 nf = *snf;  // mass, 1/mass, Langevin amplitude
+    const float hf = p.hf;
+    float af[3], n1[3], n2[3];
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+      af[x] = -(float)s[x] * nf.y;
+      n1[x] = nf.z * z1[x];
+      n2[x] = nf.z * z2[x];
+    }
+    if (gpos_out)
+#pragma unroll
+      for (int x = 0; x < 3; ++x) gpos_out[3 * n + x] = f2d(s[x]);
     const float c1 = (THERMO == MM_THERMO_LANGEVIN) ? p.c1f : 1.0f;
     double vv[3];
     float vf[3];
 #pragma unroll
     for (int x = 0; x < 3; ++x) {
-      vv[x] = v[x * t.N + n];
+      vv[x] = sv[x * kMDThreads];
       vf[x] = d2f_rn(vv[x]);
     }
     const float mf = nf.x;
@@ -640,7 +694,7 @@ __global__ void __launch_bounds__(kMDThreads, 1) k_md_nodes(Topo t, MDArgs p, co
       if (p.start)
 #pragma unroll
         for (int x = 0; x < 3; ++x) {
-          const double un = fma(p.dt, vv[x], u[x * t.N + n]);
+          const double un = fma(p.dt, vv[x], su[x * kMDThreads]);
           u[x * t.N + n] = un;
           disp[x * t.N + n] = d2f_rn(un);
         }
@@ -1018,9 +1072,13 @@ static void launch_md_nodes_t(mm_handle* h, const MDArgs& a, const double* noise
                               cudaStream_t st) {
   Topo t;
   topo_of(h, t);
+  const size_t smem = sizeof(T) == 4 ? kMDStageBytes : 0;
   int& occ = h->node_occ[THERMO == MM_THERMO_LANGEVIN ? 1 : 0];
-  if (occ == 0) occ = occupancy_of(k_md_nodes<T, STRUCT, THERMO>, kMDThreads, 0);
-  k_md_nodes<T, STRUCT, THERMO><<<node_grid(h, THERMO) + 1, kMDThreads, 0, st>>>(
+  if (occ == 0) {
+    if (smem) cudaFuncSetAttribute(k_md_nodes<T, STRUCT, THERMO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    occ = occupancy_of(k_md_nodes<T, STRUCT, THERMO>, kMDThreads, smem);
+  }
+  k_md_nodes<T, STRUCT, THERMO><<<node_grid(h, THERMO) + 1, kMDThreads, smem, st>>>(
       t, a, (const T*)h->d_G, h->d_u, h->d_v, (T*)h->d_disp, h->d_mass, h->d_invm, h->d_c2, noise, h->d_npart,
       h->d_cpart, cell_grid(h), h->d_ticket, h->d_carry, record, gpos_out, h->d_nodef);
 }
