@@ -374,7 +374,7 @@ def measure_plain_per_system(systems, nsteps):
             "cell_steps_per_s": sum(s.ncells for s in systems) * nsteps / t}
 
 
-def measure_large_mtk(n=256, nsteps=20, cmp_steps=4):
+def measure_large_mtk(n=256, nsteps=100, cmp_steps=4):
     """Large single system (periodic n^3 lattice, 20% clustered defects, two states per
     type) under NHC + MTK NPT at 300 K and 100 MPa, dt = 2 fs, through VerletIntegrator
     (device=True routes it to the lattice engine). FP64 and FP32 cells run the same
@@ -418,8 +418,11 @@ def measure_large_mtk(n=256, nsteps=20, cmp_steps=4):
             vel -= (s.masses @ vel) / s.masses.sum()
         ff = MicMecForceField(s, [ForcePartMechanical(s, precision=prec)])
         rec = Econs()
-        hooks = [NHCThermostat(300.0, timecon=100 * units.femtosecond),
-                 MTKBarostat(ff, 300.0, 100e6 * units.pascal, timecon=1000 * units.femtosecond), rec]
+        # fixed initial chain and barostat velocities (drawn at random by default): both
+        # precisions start from the same extended state
+        hooks = [NHCThermostat(300.0, timecon=100 * units.femtosecond, chain_vel0=np.zeros(3)),
+                 MTKBarostat(ff, 300.0, 100e6 * units.pascal, timecon=1000 * units.femtosecond,
+                             vel_press0=np.zeros((3, 3))), rec]
         vi = VerletIntegrator(ff, 2.0 * units.femtosecond, hooks=hooks, vel0=vel.copy(), device=True)
         vi.run(2)
         torch.cuda.synchronize()
@@ -722,6 +725,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the FP64 / batched / adjoint side measurements")
+    ap.add_argument("--large-only", type=int, default=0, metavar="N",
+                    help="only the large single-system NHC + MTK run (lattice engine) on an N^3 lattice")
     ap.add_argument("--batch-only", action="store_true",
                     help="only the batched workload (512 systems, NHC + MTK, FP32 cells): one warm-up launch of "
                          "--warmup steps and one launch of --steps steps, no autotuning or graph (for kernel profiles)")
@@ -732,6 +737,9 @@ def main():
         return run_reference(args)
     if args.batch_only:
         return run_batch_only(args)
+    if args.large_only:
+        print(json.dumps(measure_large_mtk(n=args.large_only, nsteps=args.steps)), flush=True)
+        return 0
     return run_gpu(args)
 
 

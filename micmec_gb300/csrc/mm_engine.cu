@@ -5,11 +5,12 @@
 // A step is a sequence of grid-wide kernels on one stream, in the order of the
 // reference's Verlet step with its hooks (micmec/sampling/verlet.py:140-166,
 // TBCombination npt.py:99-148, MTKBarostat.baro npt.py:653-736, NHChain nvt.py:410-458,
-// Langevin nvt.py:196-218): force evaluations (the lattice cell kernel, a per-node
-// gather into an FP64 gradient and a fixed-order energy/virial reduction), node
-// updates (kick, drift, scalings by a 3x3 matrix or a scalar, Langevin) that also
-// reduce the kinetic energy and tensor, and one-thread controller kernels for the
-// barostat and chain algebra in FP64. All totals use fixed-order reductions.
+// Langevin nvt.py:196-218): force evaluations (the lattice cell kernel and a
+// fixed-order energy/virial reduction; FP64 cells also gather an FP64 gradient, FP32
+// cells gather inside the kicks), node updates (kick, drift, scalings by a 3x3 matrix or
+// a scalar, Langevin) that also reduce the kinetic energy and tensor, and one-thread
+// controller kernels for the barostat and chain algebra in FP64. All totals use
+// fixed-order reductions.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -70,23 +71,8 @@ __global__ void k_eng_gather(ETopo t, const T* __restrict__ G, double* __restric
 // (FP32 handles: the cell kernel's partials are compensated FP32 pairs)
 template <bool PAIRS>
 __global__ void k_eng_energy(const double* __restrict__ cpart, int nblk, double* __restrict__ ctl) {
-  __shared__ double red[10 * (kET / 32)];
-  double acc[10];
-  if constexpr (PAIRS) {
-    F2 f[10];
-    for (int i = 0; i < 10; ++i) f[i] = F2{0.0f, 0.0f};
-    for (int b = threadIdx.x; b < nblk; b += blockDim.x)
-      for (int i = 0; i < 10; ++i) {
-        const float2 p = __ldcg(reinterpret_cast<const float2*>(cpart + i * nblk + b));
-        f[i] = f2_add(f[i], F2{p.x, p.y});
-      }
-    block_sum_f2<10>(f, acc, red);
-  } else {
-    for (int i = 0; i < 10; ++i) acc[i] = 0.0;
-    for (int b = threadIdx.x; b < nblk; b += blockDim.x)
-      for (int i = 0; i < 10; ++i) acc[i] += cpart[i * nblk + b];
-    block_sum<10>(acc, red);
-  }
+  __shared__ double acc[10];
+  sum_partials_by_warp<10, 0, PAIRS>(cpart, nblk, nullptr, 0, acc);
   if (threadIdx.x == 0) {
     ctl[C_EPOT] = acc[0];
     for (int i = 0; i < 9; ++i) ctl[C_VT + i] = acc[1 + i];
@@ -187,6 +173,168 @@ __global__ void __launch_bounds__(kET) k_eng_nodes(int N, NodeOp o, const double
     *ticket = 0u;
     ctl[C_EKIN] = tot[0];
     const double k[9] = {tot[1], tot[6], tot[5], tot[6], tot[2], tot[4], tot[5], tot[4], tot[3]};
+    for (int i = 0; i < 9; ++i) ctl[C_KT + i] = k[i];
+  }
+}
+
+// FP32 cells: one kernel per node operation with the corner-gradient gather fused into the
+// kicks (no separate gradient array), the increments of v and u formed in FP32 and added to
+// the FP64 state, and the kinetic sums in compensated FP32. 1024-thread blocks own equal
+// contiguous node ranges; block partials (value-major compensated pairs) are summed by the
+// block that arrives last, one warp per value.
+constexpr int kEN = 1024;
+constexpr int kKin6 = 6;  // kinetic tensor xx, yy, zz, yz, xz, xy (ekin = half the trace)
+
+struct ETopo32 {
+  int N, M, nx, ny, nz;
+  FastDiv div_nyz, div_nz;
+  const int32_t* node_cells;  // [8][N], or null for the implicit lattice
+};
+
+template <bool STRUCT>
+__device__ __forceinline__ void gather32(const ETopo32& t, const float* __restrict__ G, int n, float (&s)[3]) {
+  s[0] = s[1] = s[2] = 0.0f;
+  int i = 0, j = 0, k = 0;
+  if (STRUCT) {
+    i = fdiv(n, t.div_nyz);
+    const int r = n - i * (t.ny * t.nz);
+    j = fdiv(r, t.div_nz);
+    k = r - j * t.nz;
+  }
+#pragma unroll
+  for (int kc = 0; kc < 8; ++kc) {
+    int cell;
+    if (STRUCT) {
+      const int b = corner_to_bits(kc);
+      int a0 = i - (b & 1), b0 = j - ((b >> 1) & 1), c0 = k - (b >> 2);
+      a0 = a0 < 0 ? t.nx - 1 : a0;
+      b0 = b0 < 0 ? t.ny - 1 : b0;
+      c0 = c0 < 0 ? t.nz - 1 : c0;
+      cell = (a0 * t.ny + b0) * t.nz + c0;
+    } else {
+      cell = t.node_cells[kc * t.N + n];
+      if (cell < 0) continue;
+    }
+#pragma unroll
+    for (int x = 0; x < 3; ++x) s[x] += G[(kc * 3 + x) * (size_t)t.M + cell];
+  }
+}
+
+template <bool STRUCT>
+__global__ void __launch_bounds__(kEN, 1) k_eng_nodes32(ETopo32 t, NodeOp o, const float* __restrict__ G,
+                                                        double* __restrict__ u, double* __restrict__ v,
+                                                        float* __restrict__ disp, const float4* __restrict__ nodef,
+                                                        const double* __restrict__ mat, const double* __restrict__ c2,
+                                                        const double* __restrict__ noise, double* __restrict__ npart,
+                                                        unsigned* __restrict__ ticket, double* __restrict__ ctl) {
+  __shared__ double red[kKin6 * (kEN / 32)];
+  __shared__ double tot[kKin6];
+  __shared__ bool last;
+  const int nb = gridDim.x;
+  const size_t N = (size_t)t.N;
+  F2 acc[kKin6];
+#pragma unroll
+  for (int i = 0; i < kKin6; ++i) acc[i] = F2{0.0f, 0.0f};
+  // uniform factors in FP32 (increments), formed once
+  const float hf = (float)(0.5 * o.dt), dtf = (float)o.dt;
+  float rm[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) rm[i] = (float)(mat[i] - ((i % 4 == 0) ? 1.0 : 0.0));  // R - I (scalings)
+  const float fm1 = (float)(mat[0] - 1.0);                                               // f - 1 (scalar scaling)
+  const float c1m1 = (float)(o.c1 - 1.0);
+  const int n_end = (int)(((long long)t.N * (blockIdx.x + 1)) / nb);
+  for (int n = (int)(((long long)t.N * blockIdx.x) / nb) + threadIdx.x; n < n_end; n += blockDim.x) {
+    if (o.op == OP_SCALE_U) {
+      double w[3];
+      float wf[3];
+#pragma unroll
+      for (int x = 0; x < 3; ++x) {
+        w[x] = u[x * N + n];
+        wf[x] = d2f_rn(w[x]);
+      }
+#pragma unroll
+      for (int x = 0; x < 3; ++x) {
+        const double un = w[x] + f2d(wf[0] * rm[x] + wf[1] * rm[3 + x] + wf[2] * rm[6 + x]);
+        u[x * N + n] = un;
+        disp[x * N + n] = d2f_rn(un);
+      }
+      continue;
+    }
+    double vv[3];
+    float vf[3];
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+      vv[x] = v[x * N + n];
+      vf[x] = d2f_rn(vv[x]);
+    }
+    float q[3] = {0.0f, 0.0f, 0.0f};  // velocity increment
+    if (o.op == OP_KICK_DRIFT || o.op == OP_KICK) {
+      float s[3];
+      gather32<STRUCT>(t, G, n, s);
+      const float imf = nodef[n].y;
+#pragma unroll
+      for (int x = 0; x < 3; ++x) q[x] = hf * (-s[x] * imf);
+    } else if (o.op == OP_SCALE_V) {
+#pragma unroll
+      for (int x = 0; x < 3; ++x) q[x] = vf[0] * rm[x] + vf[1] * rm[3 + x] + vf[2] * rm[6 + x];
+    } else if (o.op == OP_SCALE_VS) {
+#pragma unroll
+      for (int x = 0; x < 3; ++x) q[x] = vf[x] * fm1;
+    } else if (o.op == OP_LANGEVIN) {
+      float z[3];
+      if (noise) {
+        const size_t base = ((size_t)(o.step - o.noise_step0) * 2 + o.call) * N * 3;
+#pragma unroll
+        for (int x = 0; x < 3; ++x) z[x] = d2f_rn(noise[base + 3 * n + x]);
+      } else {
+        normal3(o.seed, (uint32_t)n, (uint32_t)o.step, o.call, z);
+      }
+      const float amp = d2f_rn(c2[n]);
+#pragma unroll
+      for (int x = 0; x < 3; ++x) q[x] = c1m1 * vf[x] + amp * z[x];
+    }
+    if (o.op != OP_KINETIC) {
+#pragma unroll
+      for (int x = 0; x < 3; ++x) {
+        vv[x] += f2d(q[x]);
+        v[x * N + n] = vv[x];
+        vf[x] = d2f_rn(vv[x]);
+      }
+      if (o.op == OP_KICK_DRIFT)
+#pragma unroll
+        for (int x = 0; x < 3; ++x) {
+          const double un = u[x * N + n] + f2d(dtf * vf[x]);
+          u[x * N + n] = un;
+          disp[x * N + n] = d2f_rn(un);
+        }
+    }
+    if (o.kinetic) {
+      const float mf = nodef[n].x;
+      acc[0] = f2_add(acc[0], F2{mf * vf[0] * vf[0], 0.0f});
+      acc[1] = f2_add(acc[1], F2{mf * vf[1] * vf[1], 0.0f});
+      acc[2] = f2_add(acc[2], F2{mf * vf[2] * vf[2], 0.0f});
+      acc[3] = f2_add(acc[3], F2{mf * vf[1] * vf[2], 0.0f});
+      acc[4] = f2_add(acc[4], F2{mf * vf[0] * vf[2], 0.0f});
+      acc[5] = f2_add(acc[5], F2{mf * vf[0] * vf[1], 0.0f});
+    }
+  }
+  if (!o.kinetic) return;
+  block_sum_f2_pairs<kKin6>(acc, red);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int i = 0; i < kKin6; ++i) store_pair(npart + (size_t)i * nb + blockIdx.x, acc[i]);
+    __threadfence();
+    last = (atomicAdd(ticket, 1u) == (unsigned)nb - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  sum_partials_by_warp<kKin6, 0, true>(npart, nb, nullptr, 0, tot);
+  if (threadIdx.x == 0) {
+    *ticket = 0u;
+    ctl[C_EKIN] = 0.5 * (tot[0] + tot[1] + tot[2]);
+    const double k[9] = {tot[0], tot[5], tot[4], tot[5], tot[1], tot[3], tot[4], tot[3], tot[2]};
+#pragma unroll
     for (int i = 0; i < 9; ++i) ctl[C_KT + i] = k[i];
   }
 }
@@ -294,6 +442,8 @@ struct Engine {
     k_eng_nodes<T><<<nb, kET, 0, st>>>(h->N, o, gs, h->d_u, h->d_v, (T*)h->d_disp, h->d_mass, h->d_invm, mat, h->d_c2,
                                        p.noise, npart, ticket, ctl);
   }
+  int nb32 = 0;  // node-update blocks of the FP32 kernel
+  ETopo32 t32;
   void nodes(int op, int kinetic, long long step = 0, unsigned call = 0) {
     NodeOp o;
     o.op = op;
@@ -304,15 +454,21 @@ struct Engine {
     o.step = step;
     o.noise_step0 = p.step0 + 1;
     o.call = call;
-    if (h->prec == MM_PREC_FP32) nodes_t<float>(o);
-    else nodes_t<double>(o);
+    if (h->prec == MM_PREC_FP32) {
+      if (h->structured)
+        k_eng_nodes32<true><<<nb32, kEN, 0, st>>>(t32, o, (const float*)h->d_G, h->d_u, h->d_v, (float*)h->d_disp,
+                                                  h->d_nodef, mat, h->d_c2, p.noise, npart, ticket, ctl);
+      else
+        k_eng_nodes32<false><<<nb32, kEN, 0, st>>>(t32, o, (const float*)h->d_G, h->d_u, h->d_v, (float*)h->d_disp,
+                                                   h->d_nodef, mat, h->d_c2, p.noise, npart, ticket, ctl);
+    } else {
+      nodes_t<double>(o);
+    }
   }
   void forces() {
     launch_cells(h, st, nullptr);
-    if (h->prec == MM_PREC_FP32) {
-      if (h->structured) k_eng_gather<float, true><<<nb, kET, 0, st>>>(t, (const float*)h->d_G, gs);
-      else k_eng_gather<float, false><<<nb, kET, 0, st>>>(t, (const float*)h->d_G, gs);
-    } else {
+    // FP32 cells: the kicks gather the corner gradients themselves
+    if (h->prec != MM_PREC_FP32) {
       if (h->structured) k_eng_gather<double, true><<<nb, kET, 0, st>>>(t, (const double*)h->d_G, gs);
       else k_eng_gather<double, false><<<nb, kET, 0, st>>>(t, (const double*)h->d_G, gs);
     }
@@ -378,6 +534,19 @@ extern "C" mm_status mm_md_engine(mm_handle* h, double* pos, double* vel, int ns
   E.ticket = (unsigned*)(E.npart + (size_t)nb * kKin);
   E.nb = nb;
   E.t = ETopo{h->N, h->M, h->structured, h->nn[0], h->nn[1], h->nn[2], h->d_node_cells};
+  {
+    const int nsm = h->num_sms > 0 ? h->num_sms : 152;
+    const int want = (h->N + kEN - 1) / kEN;
+    E.nb32 = want < nsm ? want : nsm;
+    E.t32.N = h->N;
+    E.t32.M = h->M;
+    E.t32.nx = h->nn[0];
+    E.t32.ny = h->nn[1];
+    E.t32.nz = h->nn[2];
+    E.t32.div_nyz = make_fastdiv((uint32_t)(h->nn[1] * h->nn[2] > 0 ? h->nn[1] * h->nn[2] : 1));
+    E.t32.div_nz = make_fastdiv((uint32_t)(h->nn[2] > 0 ? h->nn[2] : 1));
+    E.t32.node_cells = h->structured ? nullptr : h->d_node_cells;
+  }
   BMD& p = E.p;
   p.dt = timestep;
   p.temp = temp;

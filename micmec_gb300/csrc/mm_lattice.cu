@@ -419,44 +419,6 @@ __global__ void k_gather(Topo t, const T* __restrict__ G, double* __restrict__ g
   if (bad && flag) atomicOr(flag, 1);
 }
 
-// Totals of per-block partials (value-major: slot v * na + k of a, v * nb + k of b, for
-// block k, so the lanes of a warp read consecutive slots) summed by one
-// block in a fixed order: warp w sums values w, w + nw, ...; its lanes stride over the
-// blocks, then a fixed shuffle tree. PAIRS: the slots hold compensated FP32 pairs,
-// summed in compensated FP32 and converted to FP64 once; else doubles summed in FP64.
-// Results in out_s (shared, NA + NB doubles), valid for every thread after the closing
-// barrier.
-template <int NA, int NB, bool PAIRS>
-__device__ __forceinline__ void sum_partials_by_warp(const double* a, int na, const double* b, int nb,
-                                                     double* out_s) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int v = wid; v < NA + NB; v += nw) {
-    const bool first = v < NA;
-    const double* base = first ? a + (size_t)v * na : b + (size_t)(v - NA) * nb;
-    const int n = first ? na : nb;
-    if constexpr (PAIRS) {
-      F2 acc{0.0f, 0.0f};
-#pragma unroll 8
-      for (int k = lane; k < n; k += 32) acc = f2_add(acc, load_pair(base + k));
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        const F2 o{__shfl_down_sync(0xffffffffu, acc.hi, off), __shfl_down_sync(0xffffffffu, acc.lo, off)};
-        acc = f2_add(acc, o);
-      }
-      if (lane == 0) out_s[v] = (double)acc.hi + (double)acc.lo;
-    } else {
-      double acc = 0.0;
-#pragma unroll 8
-      for (int k = lane; k < n; k += 32) acc += __ldcg(base + k);
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-      if (lane == 0) out_s[v] = acc;
-    }
-  }
-  __syncthreads();
-}
-
-
 // Sum the per-block partials in block order: energy written, virial added.
 template <bool PAIRS>
 __global__ void k_finalize(const double* __restrict__ cpart, int nblk, double* __restrict__ energy,

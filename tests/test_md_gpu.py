@@ -210,3 +210,35 @@ def test_device_and_host_langevin_paths_agree_with_replayed_noise_fp32():
     a, b = rows[True], rows[False]
     for col in (1, 2, 3):
         assert np.abs(a[:, col] - b[:, col]).max() <= 1e-6 * np.abs(b[:, col]).max()
+
+
+@pytest.mark.parametrize("thermo", ["nhc", "langevin"])
+def test_engine_fp32_tracks_fp64_with_barostat(thermo):
+    """Lattice engine (NHC or Langevin + MTK, 100 MPa): FP32 cells (gather fused into the
+    kicks, FP32 increments, compensated FP32 kinetic sums) against FP64 cells."""
+    from micmec_gb300 import units
+    from micmec_gb300.pes.mmff import ForcePartMechanical, MicMecForceField
+    from micmec_gb300.sampling.npt import MTKBarostat
+    from micmec_gb300.sampling.nvt import LangevinThermostat, NHCThermostat
+    from micmec_gb300.sampling.verlet import VerletIntegrator
+
+    out = {}
+    for prec in ("fp64", "fp32"):
+        s, vel = _lattice(10, 2, 5)
+        ff = MicMecForceField(s, [ForcePartMechanical(s, model="nanocell", precision=prec)])
+        rec = Rec()
+        # fixed initial chain and barostat velocities (by default both are drawn at random)
+        t = (NHCThermostat(300.0, timecon=100 * units.femtosecond, chain_vel0=np.array([1e-5, -2e-5, 1e-5]))
+             if thermo == "nhc" else LangevinThermostat(300.0, timecon=100 * units.femtosecond, seed=3))
+        b = MTKBarostat(ff, 300.0, 100e6 * units.pascal, timecon=1000 * units.femtosecond, vel_press0=np.zeros((3, 3)))
+        vi = VerletIntegrator(ff, 1.0 * units.femtosecond, hooks=[t, b, rec.hook], vel0=vel, device=True)
+        vi.batch_max_cells = 0
+        vi.run(60)
+        out[prec] = np.array(rec.rows)
+    a, b = out["fp64"], out["fp32"]
+    assert np.isfinite(b).all()
+    # epot, ekin and the cell volume follow the FP64 run at FP32 precision
+    de = np.abs(a[:20, 1] - b[:20, 1]).max() / np.abs(a[:20, 1]).max()
+    dk = np.abs(a[:20, 2] - b[:20, 2]).max() / np.abs(a[:20, 2]).max()
+    dv = np.abs(a[:, -1] - b[:, -1]).max() / np.abs(a[:, -1]).max()
+    assert de < 1e-5 and dk < 1e-5 and dv < 1e-6, (de, dk, dv)
