@@ -108,6 +108,4 @@ void launch_md_nodes(mm_handle* h, double dt, double c1, uint64_t seed, int64_t 
 void launch_md_host_begin(mm_handle* h, double dt, double c1, uint64_t seed, int64_t step, int thermo,
                           const double* pos, const double* vel, const double* gpos, cudaStream_t st);
 void launch_md_host_end(mm_handle* h, double* pos, double* vel, cudaStream_t st);
-void launch_md_begin_gpos(mm_handle* h, double dt, double c1, uint64_t seed, int64_t step, int thermo,
-                          const double* gpos, const double* noise, cudaStream_t st);
 }  // namespace mm

@@ -781,45 +781,9 @@ __global__ void __launch_bounds__(kMDThreads, 1) k_md_nodes(Topo t, MDArgs p, co
   if (last) md_nodes_final<T>(p, npart, nb, cell_tot, ticket, carry, record);
 }
 
-// First half of a step from a caller-provided gradient (AoS): "pre" thermostat,
-// kick, drift. Used by the host-buffer step entry point.
-template <typename T, int THERMO>
-__global__ void k_md_begin_gpos(Topo t, MDArgs p, const double* __restrict__ gpos, double* __restrict__ u,
-                                double* __restrict__ v, T* __restrict__ disp, const double* __restrict__ invm,
-                                const double* __restrict__ c2, const double* __restrict__ noise) {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= t.N) return;
-  double vv[3];
-#pragma unroll
-  for (int x = 0; x < 3; ++x) vv[x] = v[x * t.N + n];
-  if (THERMO == MM_THERMO_LANGEVIN) {
-    double z[3];
-    if (noise) {
-#pragma unroll
-      for (int x = 0; x < 3; ++x) z[x] = noise[3 * n + x];
-    } else {
-      float zf[3];
-      normal3(p.seed, (uint32_t)n, (uint32_t)p.step, 0u, zf);
-#pragma unroll
-      for (int x = 0; x < 3; ++x) z[x] = zf[x];
-    }
-#pragma unroll
-    for (int x = 0; x < 3; ++x) vv[x] = p.c1 * vv[x] + c2[n] * z[x];
-  }
-  const double im = invm[n];
-#pragma unroll
-  for (int x = 0; x < 3; ++x) {
-    vv[x] += 0.5 * (-gpos[3 * n + x] * im) * p.dt;
-    const double un = u[x * t.N + n] + p.dt * vv[x];
-    u[x * t.N + n] = un;
-    disp[x * t.N + n] = (T)un;
-    v[x * t.N + n] = vv[x];
-  }
-}
-
 // Host-buffer step, first half in one pass: u = pos - X(L) and v from the caller's
 // AoS arrays, then the "pre" thermostat, kick with the caller's gradient, and drift
-// (the arithmetic of k_pos_to_state + k_aos_to_soa + k_md_begin_gpos, in that order).
+// (u as k_pos_to_state forms it, then the arithmetic of the host step's first half).
 // pos / vel / gpos may be device pointers of mapped pinned host memory.
 template <typename T, int THERMO>
 __global__ void k_md_host_begin(Topo t, MDArgs p, const double* __restrict__ pos, const double* __restrict__ vel,
@@ -1086,32 +1050,6 @@ void launch_md_nodes(mm_handle* h, double dt, double c1, uint64_t seed, int64_t 
   a.c1f = lang ? (float)c1 : 1.0f;
   if (h->prec == MM_PREC_FP32) launch_md_nodes_p<float>(h, a, thermo, noise, record, gpos_out, st);
   else launch_md_nodes_p<double>(h, a, thermo, noise, record, gpos_out, st);
-}
-
-void launch_md_begin_gpos(mm_handle* h, double dt, double c1, uint64_t seed, int64_t step, int thermo,
-                          const double* gpos, const double* noise, cudaStream_t st) {
-  Topo t;
-  topo_of(h, t);
-  MDArgs a;
-  a.dt = dt;
-  a.c1 = c1;
-  a.seed = seed;
-  a.step = step;
-  a.noise_step0 = step;
-  a.finish = 0;
-  a.start = 1;
-  const int nb = node_blocks(h);
-  if (h->prec == MM_PREC_FP32) {
-    if (thermo == MM_THERMO_LANGEVIN)
-      k_md_begin_gpos<float, MM_THERMO_LANGEVIN><<<nb, kNodeThreads, 0, st>>>(t, a, gpos, h->d_u, h->d_v, (float*)h->d_disp, h->d_invm, h->d_c2, noise);
-    else
-      k_md_begin_gpos<float, MM_THERMO_NONE><<<nb, kNodeThreads, 0, st>>>(t, a, gpos, h->d_u, h->d_v, (float*)h->d_disp, h->d_invm, h->d_c2, noise);
-  } else {
-    if (thermo == MM_THERMO_LANGEVIN)
-      k_md_begin_gpos<double, MM_THERMO_LANGEVIN><<<nb, kNodeThreads, 0, st>>>(t, a, gpos, h->d_u, h->d_v, (double*)h->d_disp, h->d_invm, h->d_c2, noise);
-    else
-      k_md_begin_gpos<double, MM_THERMO_NONE><<<nb, kNodeThreads, 0, st>>>(t, a, gpos, h->d_u, h->d_v, (double*)h->d_disp, h->d_invm, h->d_c2, noise);
-  }
 }
 
 void launch_md_host_begin(mm_handle* h, double dt, double c1, uint64_t seed, int64_t step, int thermo,
