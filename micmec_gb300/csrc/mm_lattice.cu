@@ -783,8 +783,8 @@ __global__ void __launch_bounds__(kMDThreads, 1) k_md_nodes(Topo t, MDArgs p, co
 
 // Host-buffer step, first half in one pass: u = pos - X(L) and v from the caller's
 // AoS arrays, then the "pre" thermostat, kick with the caller's gradient, and drift
-// (u as k_pos_to_state forms it, then the arithmetic of the host step's first half).
-// pos / vel / gpos may be device pointers of mapped pinned host memory.
+// (u as k_pos_to_state forms it, then the arithmetic of the host step's first half);
+// pos / vel / gpos are the device copies of the caller's arrays.
 template <typename T, int THERMO>
 __global__ void k_md_host_begin(Topo t, MDArgs p, const double* __restrict__ pos, const double* __restrict__ vel,
                                 const double* __restrict__ gpos, const double* __restrict__ box,
@@ -820,7 +820,7 @@ __global__ void k_md_host_begin(Topo t, MDArgs p, const double* __restrict__ pos
 }
 
 // Host-buffer step, output: pos = X(L) + u and vel in AoS (the arithmetic of
-// k_state_to_pos + k_soa_to_aos); pos / vel may be mapped pinned host memory.
+// k_state_to_pos + k_soa_to_aos), into the device buffers copied back to the caller.
 __global__ void k_md_host_end(Topo t, const double* __restrict__ u, const double* __restrict__ v,
                               const double* __restrict__ box, double* __restrict__ pos, double* __restrict__ vel) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
