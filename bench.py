@@ -486,8 +486,11 @@ def measure_grad_over_fwd(n=16, reps=5):
     gc, gh, gd = torch.autograd.grad((w * energy_and_gradient(pos, params)[1]).sum(),
                                      [params.c21, params.h0, params.free_energy])
     errs = []
-    for tensor, grad, idx in ((params.c21, gc, (0, 0, 0)), (params.c21, gc, (1, 1, 3)), (params.h0, gh, (0, 0, 1, 1))):
+    # C11, C12 of the second state of type 1, a diagonal entry of h0 (all nonzero)
+    for tensor, grad, idx in ((params.c21, gc, (0, 0, 0)), (params.c21, gc, (1, 1, 1)), (params.h0, gh, (0, 0, 1, 1))):
         base = float(tensor.detach()[idx])
+        if base == 0.0:
+            raise ValueError("finite-difference probe on a zero parameter")
         h = 1e-4 * abs(base)
         vals = []
         for sgn in (1, -1):

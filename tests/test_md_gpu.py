@@ -242,3 +242,39 @@ def test_engine_fp32_tracks_fp64_with_barostat(thermo):
     dk = np.abs(a[:20, 2] - b[:20, 2]).max() / np.abs(a[:20, 2]).max()
     dv = np.abs(a[:, -1] - b[:, -1]).max() / np.abs(a[:, -1]).max()
     assert de < 1e-5 and dk < 1e-5 and dv < 1e-6, (de, dk, dv)
+
+
+def test_engine_on_lattice_with_vacancies_follows_host_path():
+    """Lattice engine with the general topology tables (cells removed from a periodic
+    lattice): NHC thermostat, FP64 and FP32 cells, against the host path (FP64)."""
+    from micmec_gb300 import lattices, units
+    from micmec_gb300.pes.mmff import ForcePartMechanical, MicMecForceField
+    from micmec_gb300.sampling.nvt import NHCThermostat
+    from micmec_gb300.sampling.verlet import VerletIntegrator
+    from micmec_gb300.system import System
+
+    rng = np.random.default_rng(21)
+    grid = lattices.defect_grid(8, 0.2, rng)
+    flat = grid.reshape(-1)
+    flat[rng.permutation(flat.size)[:20]] = 0  # vacancies
+    d = lattices.make_lattice(grid, nstates=2)
+    d["pos"] = lattices.displace(d["pos"], 0.05 * units.angstrom, rng)
+    kT = units.boltzmann * 300.0
+    s0 = System.from_dict(d)
+    vel = rng.normal(0.0, 1.0, s0.pos.shape) * np.sqrt(kT / s0.masses)[:, None]
+    out = {}
+    for route, prec in (("host", "fp64"), ("engine", "fp64"), ("engine", "fp32")):
+        s = System.from_dict(d)
+        ff = MicMecForceField(s, [ForcePartMechanical(s, model="nanocell", precision=prec)])
+        rec = Rec()
+        t = NHCThermostat(300.0, timecon=100 * units.femtosecond, chain_vel0=np.array([1e-5, -2e-5, 1e-5]))
+        vi = VerletIntegrator(ff, 1.0 * units.femtosecond, hooks=[t, rec.hook], vel0=vel.copy(),
+                              device=(route == "engine"))
+        vi.batch_max_cells = 0
+        vi.run(30)
+        out[route, prec] = np.array(rec.rows)
+    h, e64, e32 = out["host", "fp64"], out["engine", "fp64"], out["engine", "fp32"]
+    for col in (1, 2, 3):  # epot, ekin, econs
+        scale = np.abs(h[:, col]).max()
+        assert np.abs(e64[:, col] - h[:, col]).max() <= 1e-9 * scale
+        assert np.abs(e32[:, col] - h[:, col]).max() <= 1e-5 * scale
