@@ -146,21 +146,21 @@ mm_status mm_md_advance(mm_handle* h, int nsteps, double* records, int finish, v
 mm_status mm_md_end(mm_handle* h, double* pos, double* vel, void* stream);
 
 /*
- * MD with the Nose-Hoover chain (thermo 2, chain length 3), Langevin (thermo 1) or no
- * thermostat, optionally with the anisotropic MTK barostat (baro 1), for a system of any
- * size spread over the whole GPU: the step of VerletIntegrator.propagate
- * (micmec/sampling/verlet.py:140-166) with TBCombination / NHCThermostat / MTKBarostat
- * (micmec/sampling/npt.py:99-148, 513-757; nvt.py:361-532) as grid-wide kernels and
- * one-thread controller kernels.
+ * MD with the hooks of mm_batch_md (thermo 0..4; baro 0..3; the NHC with chain length 3)
+ * for a system of any size spread over the whole GPU: the step of
+ * VerletIntegrator.propagate (micmec/sampling/verlet.py:140-166) with TBCombination and
+ * the thermostats and barostats (micmec/sampling/npt.py:52-757; nvt.py:110-274,
+ * 361-532) as grid-wide kernels and one-thread controller kernels.
  *  pos, vel (N,3) device: in/out.   ctl_host double[MM_BATCH_CTL] host: hook constants
  *  and state in the layout of mm_batch_control (ndof, chain masses/positions/velocities,
  *  barostat mass/velocity/dof, conserved-energy corrections); returned updated. The
  *  lattice/domain part is taken from the handle and returned after the barostat moved it.
  *  records device (nsteps, MM_BATCH_REC) or NULL.  noise: as mm_md_run, or NULL.
+ *  hook_noise: device (nsteps, 1, MM_HOOK_NOISE) as mm_batch_md, or NULL.
  */
 mm_status mm_md_engine(mm_handle* h, double* pos, double* vel, int nsteps, double timestep, int thermo, double temp,
                        double timecon, int baro, double press, int chain, uint64_t seed, const double* noise,
-                       double* ctl_host, double* records, int64_t step0, void* stream);
+                       const double* hook_noise, double* ctl_host, double* records, int64_t step0, void* stream);
 
 /*
  * Measurement helper: run nsteps steps of the session like mm_md_advance(finish = 0),
@@ -239,23 +239,32 @@ mm_status mm_batch_get_state(mm_batch* b, double* pos, double* vel, double* rvec
  * kinetic energy (20), virial (21..29), kinetic tensor (30..38), barostat velocity
  * tensor (39..47), chain positions (48..50), velocities (51..53), masses (54..56),
  * ndof (57), barostat mass (58), barostat dof (59), thermostat / barostat
- * conserved-energy corrections (60, 61), relaxation: largest gradient (62), iterations (63).
+ * conserved-energy corrections (60, 61), relaxation: largest gradient (62), iterations (63),
+ * chain ndof (65; 0 = ndof), Langevin barostat time constant (66) and temperature (67).
  */
 #define MM_BATCH_CTL 72
 #define MM_BATCH_REC 31
 mm_status mm_batch_control(mm_batch* b, double* ctl, int write);
 /*
  * nsteps MD steps of every system. thermo: 0 none, 1 Langevin, 2 Nose-Hoover chain of
- * length `chain`; baro: 0 none, 1 anisotropic MTK at pressure `press`. The controller
- * block must hold ndof, chain masses/state and barostat mass/velocity/dof (as the
- * reference's hook init sets them). noise (device, (nsteps, 2, sum N, 3)) replays
- * normals instead of the generator; records (device, (nsys, nsteps, MM_BATCH_REC)):
- * energy, kinetic energy, conserved-energy correction, volume, virial(9), kinetic
- * tensor(9), domain vectors(9). use_graph: launch through a cached CUDA graph.
+ * length `chain`, 3 Berendsen, 4 CSVR (no barostat); baro: 0 none, 1 anisotropic MTK,
+ * 2 anisotropic Berendsen, 3 anisotropic Langevin barostat, at pressure `press`. The
+ * controller block must hold ndof, chain masses/state and ndof, barostat mass,
+ * velocity, dof, and for the Langevin barostat its time constant and temperature (as
+ * the reference's hook init sets them). noise (device, (nsteps, 2, sum N, 3)) replays
+ * the Langevin thermostat's normals instead of the generator; hook_noise (device,
+ * (nsteps, nsys, MM_HOOK_NOISE)) replays the CSVR thermostat's R and S and the Langevin
+ * barostat's four unit-normal tensors per step (lower triangles 00, 10, 11, 20, 21,
+ * 22); records (device, (nsys, nsteps, MM_BATCH_REC)): energy, kinetic energy,
+ * conserved-energy correction, volume, virial(9), kinetic tensor(9), domain
+ * vectors(9). use_graph: launch through a cached CUDA graph.
+ * Replaces the loop of VerletIntegrator.run with its hooks (micmec/sampling/verlet.py:
+ * 140-166; nvt.py:110-274, 361-532; npt.py:52-757).
  */
+#define MM_HOOK_NOISE 26
 mm_status mm_batch_md(mm_batch* b, int nsteps, double timestep, int thermo, double temp, double timecon, int baro,
-                      double press, int chain, uint64_t seed, int64_t step0, const double* noise, double* records,
-                      int use_graph, void* stream);
+                      double press, int chain, uint64_t seed, int64_t step0, const double* noise,
+                      const double* hook_noise, double* records, int use_graph, void* stream);
 /* Relax node positions of every system (domain fixed) until max |gradient| < gtol. */
 mm_status mm_batch_relax(mm_batch* b, int max_iter, double gtol, void* stream);
 /* Choose CTA size and persistent CTA count by timing probe_steps MD steps (state restored). */

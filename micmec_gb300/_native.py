@@ -46,7 +46,7 @@ def _declare(L):
     L.mm_set_params.argtypes = [c_void_p, P, P, P, P]
     L.mm_adjoint.argtypes = [c_void_p, P, P, P, P, P, P, P, P, c_void_p]
     L.mm_md_engine.argtypes = [c_void_p, P, P, c_int, c_double, c_int, c_double, c_double, c_int, c_double, c_int,
-                               c_uint64, P, P, P, c_int64, c_void_p]
+                               c_uint64, P, P, P, P, c_int64, c_void_p]
     L.mm_selftest_convert.argtypes = [P, P, P, P, c_int, c_void_p]
     L.mm_last_error.restype = ctypes.c_char_p
     L.mm_version.restype = ctypes.c_char_p

@@ -20,17 +20,20 @@ import ctypes
 import numpy as np
 
 from micmec_gb300 import _native as nat
-from micmec_gb300.units import boltzmann, femtosecond
+from micmec_gb300.units import bar, boltzmann, femtosecond
 
-__all__ = ["BatchSystems", "CTL", "REC"]
+__all__ = ["BatchSystems", "CTL", "REC", "HOOK_NOISE_LEN"]
 
 CTL = dict(L=slice(0, 9), rvecs=slice(9, 18), volume=18, epot=19, ekin=20, vtens=slice(21, 30), ktens=slice(30, 39),
            vel_press=slice(39, 48), chain_pos=slice(48, 51), chain_vel=slice(51, 54), chain_mass=slice(54, 57),
-           ndof=57, mass_press=58, baro_ndof=59, econs_thermo=60, econs_baro=61, gmax=62, iters=63, alpha=64)
+           ndof=57, mass_press=58, baro_ndof=59, econs_thermo=60, econs_baro=61, gmax=62, iters=63, alpha=64,
+           chain_ndof=65, timecon_press=66, temp_press=67)
 CTL_LEN = 72
 REC = dict(epot=0, ekin=1, ecorr=2, volume=3, vtens=slice(4, 13), ktens=slice(13, 22), rvecs=slice(22, 31))
 REC_LEN = 31
-_THERMO = {None: 0, "langevin": 1, "nhc": 2}
+_THERMO = {None: 0, "langevin": 1, "nhc": 2, "berendsen": 3, "csvr": 4}
+_BARO = {None: 0, "mtk": 1, "berendsen": 2, "langevin": 3}
+HOOK_NOISE_LEN = 26  # per system and step: CSVR R, S; Langevin barostat 4 x 6 unit normals
 
 
 def _declare(L):
@@ -44,7 +47,7 @@ def _declare(L):
     L.mm_batch_get_state.argtypes = [P, P, P, P]
     L.mm_batch_control.argtypes = [P, P, ctypes.c_int]
     L.mm_batch_md.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_double,
-                              ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_uint64, ctypes.c_int64, P, P,
+                              ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_uint64, ctypes.c_int64, P, P, P,
                               ctypes.c_int, P]
     L.mm_batch_relax.argtypes = [P, ctypes.c_int, ctypes.c_double, P]
     L.mm_batch_autotune.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_double,
@@ -149,8 +152,9 @@ class BatchSystems(object):
     # ------------------------------------------------------------ hooks set-up
     def setup_md(self, vel=None, temp=300.0, thermostat=None, timecon=100 * femtosecond, chainlength=3,
                  chain_vel0=None, barostat=None, baro_timecon=1000 * femtosecond, vel_press0=None, ndof=None,
-                 seed=0, clean=True):
-        """Initial velocities and hook constants for every system (as the hooks' init does)."""
+                 seed=0, clean=True, beta=4.57e-5 / bar):
+        """Initial velocities and hook constants for every system (as the hooks' init does).
+        beta: the Berendsen barostat's compressibility."""
         rng = np.random.default_rng(seed)
         pos, _, rvecs = self.get_state()
         vels = []
@@ -167,26 +171,40 @@ class BatchSystems(object):
             n3 = 3 * s.nnodes
             nd = ndof
             if nd is None:
-                nd = n3 if (thermostat in (None, "langevin") and barostat is None) else n3 - 3
-            mtk_ndof = nd
+                if barostat == "langevin":
+                    # the hook that initialises first sets ndof: NHC / Berendsen the internal
+                    # count, else the Langevin barostat the full one (npt.py:349-351)
+                    nd = n3 - 3 if thermostat in ("nhc", "berendsen") else n3
+                else:
+                    nd = n3 if (thermostat in (None, "langevin") and barostat is None) else n3 - 3
+            chain_nd = nd
+            vp = np.zeros((3, 3)) if vel_press0 is None else np.asarray(vel_press0[i] if np.ndim(vel_press0) == 3
+                                                                         else vel_press0)
             if barostat == "mtk":
                 angfreq = 2 * np.pi / baro_timecon
-                c[i, CTL["mass_press"]] = (mtk_ndof + 9) * boltzmann * temp / angfreq**2
-                c[i, CTL["baro_ndof"]] = 6
-                vp = np.zeros((3, 3)) if vel_press0 is None else np.asarray(vel_press0[i] if np.ndim(vel_press0) == 3
-                                                                             else vel_press0)
+                c[i, CTL["mass_press"]] = (nd + 9) * boltzmann * temp / angfreq**2
                 c[i, CTL["vel_press"]] = vp.ravel()
-                if thermostat == "langevin" and ndof is None:
-                    nd = n3  # TBCombination: Langevin thermostat lets the centre of mass fluctuate
+            elif barostat == "berendsen":
+                c[i, CTL["mass_press"]] = 3.0 * baro_timecon / beta * np.sqrt(nd)
+            elif barostat == "langevin":
+                c[i, CTL["mass_press"]] = (nd + 3) / 3 * boltzmann * temp * (baro_timecon / (2 * np.pi)) ** 2
+                c[i, CTL["vel_press"]] = vp.ravel()
+                c[i, CTL["timecon_press"]] = baro_timecon
+                c[i, CTL["temp_press"]] = temp
+            if barostat is not None:
+                c[i, CTL["baro_ndof"]] = 6
+                if ndof is None and (thermostat == "langevin" or barostat == "langevin"):
+                    nd = n3  # TBCombination: the centre of mass fluctuates (npt.py:86-90)
             if thermostat == "nhc":
                 afreq = 2 * np.pi / timecon
                 cm = np.ones(3) * (boltzmann * temp / afreq**2)
-                cm[0] *= nd
+                cm[0] *= chain_nd
                 c[i, CTL["chain_mass"]] = cm
                 cv = np.zeros(3) if chain_vel0 is None else np.asarray(chain_vel0[i] if np.ndim(chain_vel0) == 2
                                                                         else chain_vel0)
                 c[i, CTL["chain_vel"]] = cv
                 c[i, CTL["chain_pos"]] = 0.0
+                c[i, CTL["chain_ndof"]] = chain_nd
             c[i, CTL["ndof"]] = nd
             c[i, CTL["econs_thermo"]] = 0.0
             c[i, CTL["econs_baro"]] = 0.0
@@ -201,7 +219,12 @@ class BatchSystems(object):
 
     # ------------------------------------------------------------ kernels
     def md(self, nsteps, timestep=1.0 * femtosecond, thermostat=None, temp=300.0, timecon=100 * femtosecond,
-           barostat=None, press=0.0, chainlength=3, seed=1, step0=0, noise=None, record=False, use_graph=True):
+           barostat=None, press=0.0, chainlength=3, seed=1, step0=0, noise=None, hook_noise=None, record=False,
+           use_graph=True):
+        """nsteps MD steps of every system. thermostat: None, "langevin", "nhc", "berendsen", "csvr";
+        barostat: None, "mtk", "berendsen", "langevin" (anisotropic). The control block holds the
+        hook state (``control`` / ``set_control``). noise: (nsteps, 2, sum N, 3) Langevin normals;
+        hook_noise: (nsteps, nsys, HOOK_NOISE_LEN) CSVR / Langevin-barostat draws."""
         torch = self.torch
         dev = torch.device("cuda", torch.cuda.current_device())
         rec = None
@@ -210,9 +233,15 @@ class BatchSystems(object):
         nz = None
         if noise is not None:
             nz = torch.from_numpy(np.ascontiguousarray(noise, dtype=np.float64)).to(dev)
+        hz = None
+        if hook_noise is not None:
+            hook_noise = np.ascontiguousarray(hook_noise, dtype=np.float64)
+            if hook_noise.shape != (nsteps, len(self), HOOK_NOISE_LEN):
+                raise ValueError("hook_noise must have shape (nsteps, nsys, %d)" % HOOK_NOISE_LEN)
+            hz = torch.from_numpy(hook_noise).to(dev)
         st = self.L.mm_batch_md(self._h, int(nsteps), float(timestep), _THERMO[thermostat], float(temp),
-                                float(timecon), 1 if barostat == "mtk" else 0, float(press), int(chainlength),
-                                int(seed), int(step0), nat.ptr(nz), nat.ptr(rec), int(bool(use_graph)),
+                                float(timecon), _BARO[barostat], float(press), int(chainlength),
+                                int(seed), int(step0), nat.ptr(nz), nat.ptr(hz), nat.ptr(rec), int(bool(use_graph)),
                                 torch.cuda.current_stream().cuda_stream)
         nat.check(st, "mm_batch_md")
         if record:
@@ -231,7 +260,7 @@ class BatchSystems(object):
                  timecon=100 * femtosecond, barostat=None, press=0.0, chainlength=3):
         best = ctypes.c_double()
         nat.check(self.L.mm_batch_autotune(self._h, int(probe_steps), float(timestep), _THERMO[thermostat], float(temp),
-                                           float(timecon), 1 if barostat == "mtk" else 0, float(press),
+                                           float(timecon), _BARO[barostat], float(press),
                                            int(chainlength), ctypes.byref(best)), "mm_batch_autotune")
         bt, nc = ctypes.c_int(), ctypes.c_int()
         nat.check(self.L.mm_batch_config(self._h, ctypes.byref(bt), ctypes.byref(nc)), "mm_batch_config")

@@ -154,7 +154,7 @@ void launch_relax(mm_batch* b, int max_iter, double gtol, cudaStream_t st) {
 bool same_key(const BMD& x, const BMD& y) {
   return x.dt == y.dt && x.temp == y.temp && x.timecon == y.timecon && x.press == y.press && x.nsteps == y.nsteps &&
          x.thermo == y.thermo && x.baro == y.baro && x.chain == y.chain && x.seed == y.seed && x.step0 == y.step0 &&
-         x.noise == y.noise && x.rec == y.rec;
+         x.noise == y.noise && x.hnoise == y.hnoise && x.rec == y.rec;
 }
 
 }  // namespace
@@ -328,10 +328,9 @@ mm_status mm_batch_control(mm_batch* b, double* ctl_host, int write) {
 }
 
 mm_status mm_batch_md(mm_batch* b, int nsteps, double timestep, int thermo, double temp, double timecon, int baro,
-                      double press, int chain, uint64_t seed, int64_t step0, const double* noise, double* records,
-                      int use_graph, void* stream) {
-  if (!b || nsteps < 0 || !(timestep > 0.0) || thermo < 0 || thermo > 2 || baro < 0 || baro > 1 ||
-      (thermo == 2 && (chain < 1 || chain > 3)) || (thermo == 1 && !(timecon > 0.0))) {
+                      double press, int chain, uint64_t seed, int64_t step0, const double* noise,
+                      const double* hook_noise, double* records, int use_graph, void* stream) {
+  if (!b || nsteps < 0 || !(timestep > 0.0) || !hooks_valid(thermo, timecon, baro, chain)) {
     mm::set_error("mm_batch_md: bad argument");
     return MM_ERR_ARG;
   }
@@ -348,6 +347,7 @@ mm_status mm_batch_md(mm_batch* b, int nsteps, double timestep, int thermo, doub
   p.seed = seed;
   p.step0 = step0;
   p.noise = noise;
+  p.hnoise = hook_noise;
   p.rec = records;
   cudaStream_t st = (cudaStream_t)stream;
   if (!use_graph) {
@@ -389,7 +389,7 @@ mm_status mm_batch_relax(mm_batch* b, int max_iter, double gtol, void* stream) {
 // after every probe, and keeps the fastest configuration.
 mm_status mm_batch_autotune(mm_batch* b, int probe_steps, double timestep, int thermo, double temp, double timecon,
                             int baro, double press, int chain, double* best_ms) {
-  if (!b || probe_steps < 1) return MM_ERR_ARG;
+  if (!b || probe_steps < 1 || !(timestep > 0.0) || !hooks_valid(thermo, timecon, baro, chain)) return MM_ERR_ARG;
   const size_t N = (size_t)b->Ntot;
   const size_t cbytes = (size_t)b->nsys * C_LEN * 8;
   BCUDA(cudaDeviceSynchronize());
@@ -420,6 +420,7 @@ mm_status mm_batch_autotune(mm_batch* b, int probe_steps, double timestep, int t
       p.seed = 12345u;
       p.step0 = 0;
       p.noise = nullptr;
+      p.hnoise = nullptr;
       p.rec = nullptr;
       BCUDA(cudaEventRecord(e0, 0));
       launch_md(b, p, 0);

@@ -12,9 +12,9 @@
 // A second persistent kernel relaxes every system with nonlinear conjugate
 // gradients (Polak-Ribiere+, secant line search).
 //
-// This header holds the device code; mm_batch_md.cu and mm_batch_relax.cu instantiate
-// the two kernels (separate translation units compile in parallel) and mm_batch.cu
-// holds the host API.
+// This header holds the device code; mm_batch_md_*.cu (one per cell precision and
+// model) and mm_batch_relax.cu instantiate the two kernels (separate translation units
+// compile in parallel), mm_batch_md.cu dispatches, and mm_batch.cu holds the host API.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -73,6 +73,15 @@ struct BatchLaunch {
 };
 void launch_md(const BatchLaunch& L, const BMD& p, cudaStream_t st);                     // mm_batch_md.cu
 void launch_relax(const BatchLaunch& L, int max_iter, double gtol, cudaStream_t st);    // mm_batch_relax.cu
+// MD launch of one (cell precision, model) pair: each is instantiated in its own
+// translation unit (mm_batch_md_<precision><model>.cu) so that they compile in parallel.
+template <typename T, int MODEL>
+void launch_md_t(const BatchLaunch& L, const BMD& p, cudaStream_t st);
+template <> void launch_md_t<float, 0>(const BatchLaunch&, const BMD&, cudaStream_t);
+template <> void launch_md_t<float, 1>(const BatchLaunch&, const BMD&, cudaStream_t);
+template <> void launch_md_t<float, 2>(const BatchLaunch&, const BMD&, cudaStream_t);
+template <> void launch_md_t<double, 0>(const BatchLaunch&, const BMD&, cudaStream_t);
+template <> void launch_md_t<double, 1>(const BatchLaunch&, const BMD&, cudaStream_t);
 
 namespace {
 
@@ -387,12 +396,14 @@ __device__ __forceinline__ void langevin_noise(const BMD& p, const BArgs& a, lon
   }
 }
 
-// thermostat pre/post (THERMO 1 = Langevin, 2 = NHC)
+// thermostat pre/post (THERMO: TH_LANGEVIN, TH_NHC; TH_BERENDSEN and TH_CSVR act in pre only)
 template <typename T, int THERMO>
-__device__ void thermostat(const BArgs& a, double* c, double* red, const BSys& sy,
-                           const BMD& p, long long step, unsigned call, bool g1, double kT) {
+__device__ void thermostat(const BArgs& a, Shared<T>& sh, const BSys& sy, const BMD& p, long long step,
+                           unsigned call, bool g1, double kT, unsigned sys) {
+  double* c = sh.ctl;
+  double* red = sh.red;
   const long long N3 = a.Ntot;
-  if (THERMO == 1) {
+  if (THERMO == TH_LANGEVIN) {
     const double c1 = exp(-p.dt / p.timecon / 2);
     const double ekin0 = c[C_EKIN];
     __syncthreads();
@@ -407,54 +418,57 @@ __device__ void thermostat(const BArgs& a, double* c, double* red, const BSys& s
     kinetic<T>(a, c, red, sy);
     if (threadIdx.x == 0) c[C_ECT] += ekin0 - c[C_EKIN];
     __syncthreads();
-  } else if (THERMO == 2) {
-    __shared__ double factor;
+  } else if (THERMO == TH_NHC || THERMO == TH_CSVR) {
+    // one scale factor for all velocities; ekin and the kinetic tensor scale by its square
+    // (NHChain.__call__, nvt.py:441-446; CSVRThermostat.pre, nvt.py:267-270)
     if (threadIdx.x == 0) {
-      double G1 = 0.0;
-      if (g1) G1 = 2 * ekin_baro(c) - c[C_BNDOF] * kT;
-      factor = nhc_call(c, p, g1, G1, kT);
+      if (THERMO == TH_NHC) {
+        double G1 = 0.0;
+        if (g1) G1 = 2 * ekin_baro(c) - c[C_BNDOF] * kT;
+        const double f = nhc_call(c, p, g1, G1, kT);
+        for (int i = 0; i < 9; ++i) c[C_KT + i] *= f * f;
+        if (call == 1) c[C_ECT] = nhc_econs(c, p, kT);
+        sh.scal[0] = f;
+      } else {
+        sh.scal[0] = csvr_call(c, p, sys, a.nsys, step);
+      }
     }
     __syncthreads();
-    const double f = factor;
+    const double f = sh.scal[0];
     for (int n = threadIdx.x; n < sy.M; n += blockDim.x)
       for (int x = 0; x < 3; ++x) a.v[x * N3 + sy.off + n] *= f;
-    // the chain scales ekin by f^2 (NHChain.__call__, nvt.py:441-446); the kinetic
-    // tensor the barostat reads next scales the same way
+    __syncthreads();
+  } else if (THERMO == TH_BERENDSEN) {
+    // v <- f v, ekin from the scaled velocities, correction (1 - f^2) ekin_before (nvt.py:152-159)
     if (threadIdx.x == 0) {
-      for (int i = 0; i < 9; ++i) c[C_KT + i] *= f * f;
-      if (call == 1) c[C_ECT] = nhc_econs(c, p, kT);
+      const double f = berendsen_factor(c, p);
+      c[C_SAVE] = c[C_EKIN];
+      sh.scal[0] = f;
+      for (int i = 0; i < 9; ++i) sh.mat[i] = (i % 4 == 0) ? f : 0.0;
     }
+    __syncthreads();
+    kinetic<T>(a, c, red, sy, KV_SCALE, sh.mat);
+    if (threadIdx.x == 0) c[C_ECT] += (1 - sh.scal[0] * sh.scal[0]) * c[C_SAVE];
     __syncthreads();
   }
 }
 
 // MTK half step (MTKBarostat.baro, npt.py:653-736): barostat velocity, position and
-// domain scaling, force evaluation, velocity scaling, barostat velocity again.
+// domain scaling, force evaluation, velocity scaling, barostat velocity again. With
+// BA_LANGEVIN the barostat-velocity updates carry the Langevin barostat's friction and
+// random force (LangevinBarostat.baro, npt.py:402-486; draws `call0`, `call0 + 1`).
 template <typename T, int MODEL>
-__device__ void baro_half(const BArgs& a, Shared<T>& sh, const BSys& sy, const BMD& p, bool chain, double* cv0p) {
+__device__ void baro_half(const BArgs& a, Shared<T>& sh, const BSys& sy, const BMD& p, bool chain, double* cv0p,
+                          unsigned sys, long long step, int call0) {
   double* c = sh.ctl;
   const long long N3 = a.Ntot;
+  const bool lang = p.baro == BA_LANGEVIN;
   if (threadIdx.x == 0) {
-    update_baro_vel(c, p, chain, chain ? *cv0p : 0.0);
+    double z6[6];
+    if (lang) lbaro_draws(p, sys, a.nsys, step, call0, z6);
+    update_baro_vel(c, p, chain, chain ? *cv0p : 0.0, lang ? z6 : nullptr);
     sym_exp(c + C_VP, p.dt / 2, sh.mat);
-    double Ln[9], Rn[9];
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) {
-        double sl = 0.0, sr = 0.0;
-        for (int k = 0; k < 3; ++k) {
-          sl += c[C_L + i * 3 + k] * sh.mat[k * 3 + j];
-          sr += c[C_RV + i * 3 + k] * sh.mat[k * 3 + j];
-        }
-        Ln[i * 3 + j] = sl;
-        Rn[i * 3 + j] = sr;
-      }
-    for (int i = 0; i < 9; ++i) {
-      c[C_L + i] = Ln[i];
-      c[C_RV + i] = Rn[i];
-    }
-    const double* r = c + C_RV;
-    c[C_VOL] = fabs(r[0] * (r[4] * r[8] - r[5] * r[7]) + r[1] * (r[5] * r[6] - r[3] * r[8]) +
-                    r[2] * (r[3] * r[7] - r[4] * r[6]));
+    scale_domain(c, sh.mat);
   }
   __syncthreads();
   positions<T>(a, sy, sh.mat, 0.0);
@@ -488,7 +502,49 @@ __device__ void baro_half(const BArgs& a, Shared<T>& sh, const BSys& sy, const B
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) c[C_KT + i * 3 + j] = 0.5 * (K2[i * 3 + j] + K2[j * 3 + i]);
     c[C_EKIN] = 0.5 * (c[C_KT + 0] + c[C_KT + 4] + c[C_KT + 8]);
-    update_baro_vel(c, p, chain, chain ? *cv0p : 0.0);
+    double z6[6];
+    if (lang) lbaro_draws(p, sys, a.nsys, step, call0 + 1, z6);
+    update_baro_vel(c, p, chain, chain ? *cv0p : 0.0, lang ? z6 : nullptr);
+  }
+  __syncthreads();
+}
+
+// Berendsen barostat post call (BerendsenBarostat.post, npt.py:262-292): positions and
+// domain times mu, forces again, correction += epot before - epot after.
+template <typename T, int MODEL>
+__device__ void berendsen_baro(const BArgs& a, Shared<T>& sh, const BSys& sy, const BMD& p) {
+  double* c = sh.ctl;
+  if (threadIdx.x == 0) {
+    c[C_SAVE] = c[C_EPOT];
+    berendsen_mu(c, p, sh.mat);
+    scale_domain(c, sh.mat);
+  }
+  __syncthreads();
+  positions<T>(a, sy, sh.mat, 0.0);
+  refresh_B<T>(sh, a.tt, a.ntypes, c + C_L);
+  __syncthreads();
+  forces<T, MODEL>(a, sh, sy);
+  if (threadIdx.x == 0) c[C_ECB] += c[C_SAVE] - c[C_EPOT];
+  __syncthreads();
+}
+
+// Barostat pre/post call of the MTK or Langevin barostat (the Berendsen barostat acts in
+// post only). The Langevin barostat adds the change of epot + ekin over its call to its
+// correction (npt.py:375-395); the MTK barostat sets its correction after post.
+template <typename T, int MODEL>
+__device__ void baro_call(const BArgs& a, Shared<T>& sh, const BSys& sy, const BMD& p, double* cv0p,
+                          unsigned sys, long long step, int call0) {
+  double* c = sh.ctl;
+  const bool chain = p.thermo == TH_NHC;
+  if (threadIdx.x == 0) {
+    *cv0p = c[C_CVEL + 0];
+    c[C_SAVE] = c[C_EPOT] + c[C_EKIN];
+  }
+  __syncthreads();
+  baro_half<T, MODEL>(a, sh, sy, p, chain, cv0p, sys, step, call0);
+  if (threadIdx.x == 0) {
+    if (p.baro == BA_LANGEVIN) c[C_ECB] += c[C_SAVE] - c[C_EPOT] - c[C_EKIN];
+    else if (call0 != 0) c[C_ECB] = ekin_baro(c) + p.press * c[C_VOL];
   }
   __syncthreads();
 }
@@ -498,7 +554,6 @@ __global__ void __launch_bounds__(BT, (sizeof(T) == 4 && MODEL >= 1) ? 512 / BT 
   const int THERMO = p.thermo, BARO = p.baro;
   __shared__ Shared<T> sh;
   __shared__ double cv0;
-  const long long N3 = a.Ntot;
   for (int w = a.work_off[blockIdx.x]; w < a.work_off[blockIdx.x + 1]; ++w) {
     const int b = a.work[w];
     const BSys sy = a.sys[b];
@@ -507,7 +562,7 @@ __global__ void __launch_bounds__(BT, (sizeof(T) == 4 && MODEL >= 1) ? 512 / BT 
     double* c = sh.ctl;
     load_tables<T>(sh, a.tt, a.ntypes, c + C_L);
     __syncthreads();
-    const double kT = (1.3806505e-23 / 4.35974381e-18) * p.temp;  // boltzmann (Hartree / K) x T
+    const double kT = kBoltzmannHa * p.temp;
     write_disp<T>(a, sy);
     __syncthreads();
     forces<T, MODEL>(a, sh, sy);
@@ -515,31 +570,25 @@ __global__ void __launch_bounds__(BT, (sizeof(T) == 4 && MODEL >= 1) ? 512 / BT 
     for (int st = 1; st <= p.nsteps; ++st) {
       const long long step = p.step0 + st;
       // ---- pre hooks: barostat, then thermostat (TBCombination.pre)
-      if (BARO == 1) {
-        if (threadIdx.x == 0) cv0 = c[C_CVEL + 0];
-        __syncthreads();
-        baro_half<T, MODEL>(a, sh, sy, p, THERMO == 2, &cv0);
-      }
-      if (THERMO == 1) thermostat<T, 1>(a, c, sh.red, sy, p, step, 0u, BARO == 1, kT);
-      if (THERMO == 2) thermostat<T, 2>(a, c, sh.red, sy, p, step, 0u, BARO == 1, kT);
+      if (BARO == BA_MTK || BARO == BA_LANGEVIN) baro_call<T, MODEL>(a, sh, sy, p, &cv0, b, step, 0);
+      if (THERMO == TH_LANGEVIN) thermostat<T, TH_LANGEVIN>(a, sh, sy, p, step, 0u, false, kT, b);
+      if (THERMO == TH_NHC) thermostat<T, TH_NHC>(a, sh, sy, p, step, 0u, BARO == BA_MTK, kT, b);
+      if (THERMO == TH_BERENDSEN) thermostat<T, TH_BERENDSEN>(a, sh, sy, p, step, 0u, false, kT, b);
+      if (THERMO == TH_CSVR) thermostat<T, TH_CSVR>(a, sh, sy, p, step, 0u, false, kT, b);
       // ---- velocity Verlet
       positions<T>(a, sy, nullptr, p.dt);
       __syncthreads();
       forces<T, MODEL>(a, sh, sy);
       kinetic<T>(a, c, sh.red, sy, KV_KICK, nullptr, p.dt);
       // ---- post hooks: thermostat, then barostat
-      if (THERMO == 1) thermostat<T, 1>(a, c, sh.red, sy, p, step, 1u, BARO == 1, kT);
-      if (THERMO == 2) thermostat<T, 2>(a, c, sh.red, sy, p, step, 1u, BARO == 1, kT);
-      if (BARO == 1) {
-        if (threadIdx.x == 0) cv0 = c[C_CVEL + 0];
-        __syncthreads();
-        baro_half<T, MODEL>(a, sh, sy, p, THERMO == 2, &cv0);
-        if (threadIdx.x == 0) c[C_ECB] = ekin_baro(c) + p.press * c[C_VOL];
-      }
+      if (THERMO == TH_LANGEVIN) thermostat<T, TH_LANGEVIN>(a, sh, sy, p, step, 1u, false, kT, b);
+      if (THERMO == TH_NHC) thermostat<T, TH_NHC>(a, sh, sy, p, step, 1u, BARO == BA_MTK, kT, b);
+      if (BARO == BA_MTK || BARO == BA_LANGEVIN) baro_call<T, MODEL>(a, sh, sy, p, &cv0, b, step, 2);
+      if (BARO == BA_BERENDSEN) berendsen_baro<T, MODEL>(a, sh, sy, p);
       if (threadIdx.x == 0 && p.rec) {
         double* r = p.rec + ((size_t)b * p.nsteps + (st - 1)) * BR_LEN;
         double corr = c[C_ECT] + c[C_ECB];
-        if (THERMO == 2 && BARO == 1) corr += c[C_BNDOF] * kT * c[C_CPOS + 0];
+        if (THERMO == TH_NHC && BARO != BA_NONE) corr += c[C_BNDOF] * kT * c[C_CPOS + 0];
         r[BR_EPOT] = c[C_EPOT];
         r[BR_EKIN] = c[C_EKIN];
         r[BR_ECORR] = corr;

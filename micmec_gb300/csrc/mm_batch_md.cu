@@ -1,13 +1,7 @@
-// Batched MD kernel instantiations (device code in mm_batch_dev.cuh).
+// Batched MD launch dispatch; the kernel instantiations live in mm_batch_md_*.cu.
 #include "mm_batch_dev.cuh"
 
 namespace mmb {
-
-template <typename T, int MODEL>
-static void launch_md_t(const BatchLaunch& L, const BMD& p, cudaStream_t st) {
-  if (L.bt == 128) k_batch_md<T, MODEL, 128><<<L.nctas, 128, 0, st>>>(L.a, p);
-  else k_batch_md<T, MODEL, 256><<<L.nctas, 256, 0, st>>>(L.a, p);
-}
 
 void launch_md(const BatchLaunch& L, const BMD& p, cudaStream_t st) {
   if (L.prec == MM_PREC_FP32) {

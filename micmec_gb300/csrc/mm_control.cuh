@@ -1,11 +1,16 @@
 // Controller state and one-thread FP64 algebra of the thermostat/barostat hooks,
 // shared by the batch kernels and the lattice MD engine: the per-system control
-// block layout, the MTK barostat velocity update (micmec/sampling/npt.py:654-681),
-// symmetric 3x3 matrix exponentials for the MTK scalings (npt.py:686-720), and the
-// Nose-Hoover chain (micmec/sampling/nvt.py:410-458).
+// block layout, the MTK and Langevin barostat velocity updates
+// (micmec/sampling/npt.py:654-681, 404-439), symmetric 3x3 matrix exponentials for
+// their scalings (npt.py:686-720), the Berendsen barostat's scaling matrix
+// (npt.py:266-282), the Nose-Hoover chain (micmec/sampling/nvt.py:410-458), the
+// Berendsen thermostat's factor (nvt.py:152-159) and the CSVR thermostat's factor
+// (nvt.py:257-270) with its random draws.
 #pragma once
 
 #include <cuda_runtime.h>
+
+#include "mm_device.cuh"
 
 namespace mmc {
 
@@ -30,8 +35,19 @@ enum {
   C_GMAX = 62,        // relaxation: largest node gradient norm
   C_ITER = 63,        // relaxation: iterations used
   C_ALPHA = 64,       // relaxation: last step length
+  C_CNDOF = 65,       // degrees of freedom the chain thermostats (0: C_NDOF)
+  C_BTAU = 66,        // Langevin barostat: time constant
+  C_BTEMP = 67,       // Langevin barostat: temperature
+  C_SAVE = 68,        // scratch of the hook bookkeeping (energy before a hook call)
   C_LEN = 72
 };
+// thermostat / barostat kinds
+enum { TH_NONE = 0, TH_LANGEVIN = 1, TH_NHC = 2, TH_BERENDSEN = 3, TH_CSVR = 4 };
+enum { BA_NONE = 0, BA_MTK = 1, BA_BERENDSEN = 2, BA_LANGEVIN = 3 };
+// per-system replayed draws of one step (hook noise): the CSVR thermostat's normal R and
+// chi-squared S, then the lower triangles (00, 10, 11, 20, 21, 22) of the Langevin
+// barostat's four unit-normal tensors
+enum { HN_R = 0, HN_S = 1, HN_B = 2, HN_LEN = 26 };
 enum { BR_EPOT = 0, BR_EKIN = 1, BR_ECORR = 2, BR_VOL = 3, BR_VT = 4, BR_KT = 13, BR_RV = 22, BR_LEN = 31 };
 
 struct BMD {
@@ -40,8 +56,87 @@ struct BMD {
   unsigned long long seed;
   long long step0;
   const double* noise;   // replay: [nsteps][2][Ntot][3] or null
+  const double* hnoise;  // replay: [nsteps][nsys][HN_LEN] or null
   double* rec;           // [nsys][nsteps][BR_LEN] or null
 };
+
+constexpr double kBoltzmannHa = 1.3806505e-23 / 4.35974381e-18;  // Hartree / K
+
+// Hook kinds the step kernels run: thermostats none / Langevin / NHC (chain 1..3) /
+// Berendsen / CSVR, barostats none / MTK / Berendsen / Langevin; CSVR alone (the
+// reference's TBCombination does not pair it with a barostat, npt.py:163-177).
+inline bool hooks_valid(int thermo, double timecon, int baro, int chain) {
+  if (thermo < TH_NONE || thermo > TH_CSVR || baro < BA_NONE || baro > BA_LANGEVIN) return false;
+  if (thermo == TH_NHC && (chain < 1 || chain > 3)) return false;
+  if ((thermo == TH_LANGEVIN || thermo == TH_BERENDSEN || thermo == TH_CSVR) && !(timecon > 0.0)) return false;
+  if (thermo == TH_CSVR && baro != BA_NONE) return false;
+  return true;
+}
+
+// ------------------------------------------------------------ per-system random draws
+// Philox stream of the hook draws, keyed by (system, step, tag): disjoint from the
+// per-node Langevin stream (whose last counter word is a different constant).
+__device__ inline void hook_uniform4(unsigned long long seed, unsigned sys, long long step, unsigned tag,
+                                     double (&u)[4]) {
+  const mm::U4 r = mm::philox4x32_10(mm::U4{sys, (uint32_t)step, tag, 0x484f4f4bu}, (uint32_t)seed,
+                                     (uint32_t)(seed >> 32));
+  const double s = 2.3283064365386963e-10;  // 2^-32: uniforms in (0, 1)
+  u[0] = ((double)r.x + 0.5) * s;
+  u[1] = ((double)r.y + 0.5) * s;
+  u[2] = ((double)r.z + 0.5) * s;
+  u[3] = ((double)r.w + 0.5) * s;
+}
+
+// Two standard normals from two uniforms (Box-Muller, FP64).
+__device__ inline void box_muller(double u1, double u2, double& z0, double& z1) {
+  const double r = sqrt(-2.0 * log(u1));
+  double sn, cs;
+  sincospi(2.0 * u2, &sn, &cs);
+  z0 = r * cs;
+  z1 = r * sn;
+}
+
+// n standard normals for (system, step, tag): four per generator call.
+__device__ inline void hook_normals(unsigned long long seed, unsigned sys, long long step, unsigned tag, int n,
+                                    double* z) {
+  for (int q = 0; 4 * q < n; ++q) {
+    double u[4], v[4];
+    hook_uniform4(seed, sys, step, (tag << 8) | (unsigned)q, u);
+    box_muller(u[0], u[1], v[0], v[1]);
+    box_muller(u[2], u[3], v[2], v[3]);
+    for (int i = 0; i < 4 && 4 * q + i < n; ++i) z[4 * q + i] = v[i];
+  }
+}
+
+// Gamma(a, 1) variate by Marsaglia and Tsang, "A simple method for generating gamma
+// variables", ACM TOMS 26 (2000) 363-372: d = a - 1/3, c = 1 / sqrt(9 d); draw a normal
+// x until v = (1 + c x)^3 > 0 and log(u) < x^2/2 + d - d v + d log v, return d v. For
+// a < 1 the result for a + 1 is multiplied by u^(1/a). Each try accepts with probability
+// above 0.95; the loop is bounded (64 tries) and returns d if every try was rejected.
+__device__ inline double gamma_mt(double a, unsigned long long seed, unsigned sys, long long step, unsigned tag) {
+  double boost = 1.0;
+  if (a < 1.0) {
+    double u[4];
+    hook_uniform4(seed, sys, step, (tag << 8) | 255u, u);
+    boost = pow(u[0], 1.0 / a);
+    a += 1.0;
+  }
+  const double d = a - 1.0 / 3.0, cc = 1.0 / sqrt(9.0 * d);
+  for (unsigned k = 0; k < 64; ++k) {
+    double u[4];
+    hook_uniform4(seed, sys, step, (tag << 8) | k, u);
+    double x, unused;
+    box_muller(u[0], u[1], x, unused);
+    double v = 1.0 + cc * x;
+    if (v <= 0.0) continue;
+    v = v * v * v;
+    if (log(u[2]) < 0.5 * x * x + d - d * v + d * log(v)) return boost * d * v;
+  }
+  return boost * d;
+}
+
+// tags of the hook draws
+enum { TAG_CSVR_R = 1, TAG_CSVR_S = 2, TAG_LBARO = 8 };
 
 // ------------------------------------------------------------ small 3x3 helpers (thread 0, FP64)
 
@@ -92,9 +187,15 @@ __device__ inline void sym_exp(const double* S, double f, double* R) {
   }
 }
 
-// MTK: update of the barostat velocity tensor (npt.py:654-681), thread 0
-__device__ inline void update_baro_vel(double* c, const BMD& p, bool chain, double cv0) {
+// Update of the barostat velocity tensor, thread 0: MTK (npt.py:654-681) when z6 is null;
+// Langevin barostat (npt.py:404-439) with z6 = the lower triangle (00, 10, 11, 20, 21, 22)
+// of a unit-normal tensor: friction exp(-dt / (8 timecon)) before and after, and the
+// random force R = z sqrt(2 W kT / (dt timecon)) (symmetric) in the update.
+__device__ inline void update_baro_vel(double* c, const BMD& p, bool chain, double cv0, const double* z6 = nullptr) {
   const double dt = p.dt;
+  const double fric = z6 ? exp(-dt / (8 * c[C_BTAU])) : 1.0;
+  if (z6)
+    for (int i = 0; i < 9; ++i) c[C_VP + i] *= fric;
   if (chain)
     for (int i = 0; i < 9; ++i) c[C_VP + i] *= exp(-dt * cv0 / 8);
   double pt[9];
@@ -104,12 +205,100 @@ __device__ inline void update_baro_vel(double* c, const BMD& p, bool chain, doub
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) ps[i * 3 + j] = 0.5 * (pt[j * 3 + i] + pt[i * 3 + j]);
   const double diag = 2.0 * c[C_EKIN] / c[C_NDOF] - p.press * c[C_VOL];
+  double R[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  if (z6) {
+    const double sc = sqrt(2 * c[C_MPRESS] * kBoltzmannHa * c[C_BTEMP] / (dt * c[C_BTAU]));
+    const int tri[9] = {0, 1, 3, 1, 2, 4, 3, 4, 5};  // (i, j) -> lower-triangle slot of (max, min)
+    for (int i = 0; i < 9; ++i) R[i] = z6[tri[i]] * sc;
+  }
   for (int i = 0; i < 9; ++i) {
     const double Gi = (ps[i] + ((i % 4 == 0) ? diag : 0.0)) / c[C_MPRESS];
-    c[C_VP + i] += Gi * dt / 4;
+    if (z6) c[C_VP + i] += (Gi - R[i] / c[C_MPRESS]) * dt / 4;
+    else c[C_VP + i] += Gi * dt / 4;
   }
+  if (z6)
+    for (int i = 0; i < 9; ++i) c[C_VP + i] *= fric;
   if (chain)
     for (int i = 0; i < 9; ++i) c[C_VP + i] *= exp(-dt * cv0 / 8);
+}
+
+// The six unit normals of Langevin-barostat call `call` (0..3) of step `step`, system `sys`.
+__device__ inline void lbaro_draws(const BMD& p, unsigned sys, int nsys, long long step, int call, double* z6) {
+  if (p.hnoise) {
+    const double* h = p.hnoise + ((size_t)(step - p.step0 - 1) * nsys + sys) * HN_LEN + HN_B + 6 * call;
+    for (int i = 0; i < 6; ++i) z6[i] = h[i];
+  } else {
+    hook_normals(p.seed, sys, step, TAG_LBARO + call, 6, z6);
+  }
+}
+
+// Domain update of a barostat: L <- L M, domain vectors <- rv M, volume from them.
+__device__ inline void scale_domain(double* c, const double* M) {
+  double Ln[9], Rn[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double sl = 0.0, sr = 0.0;
+      for (int k = 0; k < 3; ++k) {
+        sl += c[C_L + i * 3 + k] * M[k * 3 + j];
+        sr += c[C_RV + i * 3 + k] * M[k * 3 + j];
+      }
+      Ln[i * 3 + j] = sl;
+      Rn[i * 3 + j] = sr;
+    }
+  for (int i = 0; i < 9; ++i) {
+    c[C_L + i] = Ln[i];
+    c[C_RV + i] = Rn[i];
+  }
+  const double* r = c + C_RV;
+  c[C_VOL] = fabs(r[0] * (r[4] * r[8] - r[5] * r[7]) + r[1] * (r[5] * r[6] - r[3] * r[8]) +
+                  r[2] * (r[3] * r[7] - r[4] * r[6]));
+}
+
+// Berendsen barostat scaling matrix (npt.py:266-277), anisotropic, no volume constraint:
+// mu = sym(I - dt / W (P I - (K - V) / vol)), K = sum m v (x) v, V the virial.
+__device__ inline void berendsen_mu(const double* c, const BMD& p, double* mu) {
+  double m[9];
+  for (int i = 0; i < 9; ++i) {
+    const double ptens = (c[C_KT + i] - c[C_VT + i]) / c[C_VOL];
+    const double dmu = p.dt / c[C_MPRESS] * (((i % 4 == 0) ? p.press : 0.0) - ptens);
+    m[i] = ((i % 4 == 0) ? 1.0 : 0.0) - dmu;
+  }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) mu[i * 3 + j] = 0.5 * (m[i * 3 + j] + m[j * 3 + i]);
+}
+
+// Berendsen thermostat factor (nvt.py:152-159): sqrt(1 + dt / timecon (T / T_inst - 1)).
+__device__ inline double berendsen_factor(const double* c, const BMD& p) {
+  const double temp_inst = 2.0 * c[C_EKIN] / (kBoltzmannHa * c[C_NDOF]);
+  return sqrt(1 + p.dt / p.timecon * (p.temp / temp_inst - 1));
+}
+
+// CSVR thermostat (nvt.py:257-270), thread 0: draws R and S (replayed or generated),
+// returns alpha and applies its effect on ekin, the kinetic tensor and the correction.
+__device__ inline double csvr_call(double* c, const BMD& p, unsigned sys, int nsys, long long step) {
+  double R, S;
+  if (p.hnoise) {
+    const double* h = p.hnoise + ((size_t)(step - p.step0 - 1) * nsys + sys) * HN_LEN;
+    R = h[HN_R];
+    S = h[HN_S];
+  } else {
+    double z[2];
+    hook_normals(p.seed, sys, step, TAG_CSVR_R, 2, z);
+    R = z[0];
+    const double n1 = c[C_NDOF] - 1.0;
+    S = n1 > 0.0 ? 2.0 * gamma_mt(0.5 * n1, p.seed, sys, step, TAG_CSVR_S) : 0.0;
+  }
+  const double cc = exp(-p.dt / p.timecon);
+  const double kin = 0.5 * c[C_NDOF] * kBoltzmannHa * p.temp;
+  const double ekin = c[C_EKIN];
+  const double fact = (1 - cc) * kin / c[C_NDOF] / ekin;
+  const double x = R + sqrt(cc / fact);
+  const double sgn = (x > 0.0) - (x < 0.0);
+  const double alpha = sgn * sqrt(cc + (S + R * R) * fact + 2 * R * sqrt(cc * fact));
+  c[C_ECT] += (1 - alpha * alpha) * ekin;
+  c[C_EKIN] = alpha * alpha * ekin;
+  for (int i = 0; i < 9; ++i) c[C_KT + i] *= alpha * alpha;
+  return alpha;
 }
 
 __device__ inline double ekin_baro(const double* c) {
@@ -118,12 +307,16 @@ __device__ inline double ekin_baro(const double* c) {
   return 0.5 * c[C_MPRESS] * s;
 }
 
+// degrees of freedom the chain thermostats: those of the thermostat's own init, which
+// differ from the integrator's when a Langevin barostat later widens them (npt.py:86-90)
+__device__ inline double chain_ndof(const double* c) { return c[C_CNDOF] > 0.0 ? c[C_CNDOF] : c[C_NDOF]; }
+
 // one bead update of the Nose-Hoover chain (nvt.py:411-435), thread 0
 __device__ inline void nhc_bead(double* c, const BMD& p, int k, double ekin, bool g1, double G1_add, double kT) {
   const int L = p.chain;
   double g;
   if (k == 0) {
-    g = 2 * ekin - c[C_NDOF] * kT;
+    g = 2 * ekin - chain_ndof(c) * kT;
     if (g1) g += G1_add;
   } else {
     g = c[C_CMASS + k - 1] * c[C_CVEL + k - 1] * c[C_CVEL + k - 1] - kT;
@@ -154,7 +347,7 @@ __device__ inline double nhc_econs(const double* c, const BMD& p, double kT) {
   double s = 0.0, sp = 0.0;
   for (int k = 0; k < p.chain; ++k) s += c[C_CVEL + k] * c[C_CVEL + k] * c[C_CMASS + k];
   for (int k = 1; k < p.chain; ++k) sp += c[C_CPOS + k];
-  return 0.5 * s + kT * (c[C_NDOF] * c[C_CPOS + 0] + sp);
+  return 0.5 * s + kT * (chain_ndof(c) * c[C_CPOS + 0] + sp);
 }
 
 

@@ -340,45 +340,32 @@ __global__ void __launch_bounds__(kEN, 1) k_eng_nodes32(ETopo32 t, NodeOp o, con
 }
 
 enum { CT_CV0, CT_BARO_VEL, CT_BARO_POS, CT_BARO_VSCALE, CT_NHC, CT_NHC_ECONS, CT_SAVE_EKIN, CT_LANG_CORR, CT_ECB,
-       CT_RECORD };
+       CT_RECORD, CT_BER_T, CT_BER_T_CORR, CT_CSVR, CT_BBARO, CT_BBARO_CORR, CT_LBARO_SAVE, CT_LBARO_CORR };
 
-// One-thread controller: barostat / chain algebra on the control block (FP64).
-__global__ void k_eng_ctl(int op, BMD p, int g1, double* __restrict__ ctl, double* __restrict__ mat,
+// One-thread controller: barostat / chain algebra on the control block (FP64). `arg` is
+// the G1 flag of CT_NHC and the draw index (0..3 within the step) of CT_BARO_VEL.
+__global__ void k_eng_ctl(int op, BMD p, int arg, long long step, double* __restrict__ ctl, double* __restrict__ mat,
                           double* __restrict__ box, double* __restrict__ scal, double* __restrict__ rec) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   double* c = ctl;
-  const double kT = (1.3806505e-23 / 4.35974381e-18) * p.temp;
-  const bool chain = p.thermo == 2;
+  const double kT = kBoltzmannHa * p.temp;
+  const bool chain = p.thermo == TH_NHC;
   switch (op) {
     case CT_CV0:
       scal[0] = c[C_CVEL + 0];
       break;
-    case CT_BARO_VEL:
-      update_baro_vel(c, p, chain, scal[0]);
-      break;
-    case CT_BARO_POS: {
-      sym_exp(c + C_VP, p.dt / 2, mat);
-      double Ln[9], Rn[9];
-      for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) {
-          double sl = 0.0, sr = 0.0;
-          for (int k = 0; k < 3; ++k) {
-            sl += c[C_L + i * 3 + k] * mat[k * 3 + j];
-            sr += c[C_RV + i * 3 + k] * mat[k * 3 + j];
-          }
-          Ln[i * 3 + j] = sl;
-          Rn[i * 3 + j] = sr;
-        }
-      for (int i = 0; i < 9; ++i) {
-        c[C_L + i] = Ln[i];
-        c[C_RV + i] = Rn[i];
-        box[i] = Ln[i];
-      }
-      const double* r = c + C_RV;
-      c[C_VOL] = fabs(r[0] * (r[4] * r[8] - r[5] * r[7]) + r[1] * (r[5] * r[6] - r[3] * r[8]) +
-                      r[2] * (r[3] * r[7] - r[4] * r[6]));
+    case CT_BARO_VEL: {
+      double z6[6];
+      const bool lang = p.baro == BA_LANGEVIN;
+      if (lang) lbaro_draws(p, 0u, 1, step, arg, z6);
+      update_baro_vel(c, p, chain, scal[0], lang ? z6 : nullptr);
       break;
     }
+    case CT_BARO_POS:
+      sym_exp(c + C_VP, p.dt / 2, mat);
+      scale_domain(c, mat);
+      for (int i = 0; i < 9; ++i) box[i] = c[C_L + i];
+      break;
     case CT_BARO_VSCALE: {
       double S[9];
       const double tr = c[C_VP + 0] + c[C_VP + 4] + c[C_VP + 8];
@@ -387,8 +374,8 @@ __global__ void k_eng_ctl(int op, BMD p, int g1, double* __restrict__ ctl, doubl
       break;
     }
     case CT_NHC: {
-      const double G1 = g1 ? 2 * ekin_baro(c) - c[C_BNDOF] * kT : 0.0;
-      mat[0] = nhc_call(c, p, g1 != 0, G1, kT);
+      const double G1 = arg ? 2 * ekin_baro(c) - c[C_BNDOF] * kT : 0.0;
+      mat[0] = nhc_call(c, p, arg != 0, G1, kT);
       break;
     }
     case CT_NHC_ECONS:
@@ -403,10 +390,35 @@ __global__ void k_eng_ctl(int op, BMD p, int g1, double* __restrict__ ctl, doubl
     case CT_ECB:
       c[C_ECB] = ekin_baro(c) + p.press * c[C_VOL];
       break;
+    case CT_BER_T:  // Berendsen thermostat factor; ekin before the scaling kept
+      scal[1] = c[C_EKIN];
+      mat[0] = berendsen_factor(c, p);
+      break;
+    case CT_BER_T_CORR:
+      c[C_ECT] += (1 - mat[0] * mat[0]) * scal[1];
+      break;
+    case CT_CSVR:  // updates ekin, the kinetic tensor and the correction itself
+      mat[0] = csvr_call(c, p, 0u, 1, step);
+      break;
+    case CT_BBARO:  // Berendsen barostat: scaling matrix and domain; epot before kept
+      scal[2] = c[C_EPOT];
+      berendsen_mu(c, p, mat);
+      scale_domain(c, mat);
+      for (int i = 0; i < 9; ++i) box[i] = c[C_L + i];
+      break;
+    case CT_BBARO_CORR:
+      c[C_ECB] += scal[2] - c[C_EPOT];
+      break;
+    case CT_LBARO_SAVE:
+      scal[3] = c[C_EPOT] + c[C_EKIN];
+      break;
+    case CT_LBARO_CORR:
+      c[C_ECB] += scal[3] - c[C_EPOT] - c[C_EKIN];
+      break;
     case CT_RECORD: {
       if (!rec) break;
       double corr = c[C_ECT] + c[C_ECB];
-      if (p.thermo == 2 && p.baro == 1) corr += c[C_BNDOF] * kT * c[C_CPOS + 0];
+      if (p.thermo == TH_NHC && p.baro != BA_NONE) corr += c[C_BNDOF] * kT * c[C_CPOS + 0];
       rec[BR_EPOT] = c[C_EPOT];
       rec[BR_EKIN] = c[C_EKIN];
       rec[BR_ECORR] = corr;
@@ -434,8 +446,8 @@ struct Engine {
   unsigned* ticket;
   int nb;
 
-  void ctlop(int op, int g1 = 0, double* rec = nullptr) {
-    k_eng_ctl<<<1, 32, 0, st>>>(op, p, g1, ctl, mat, h->d_box, scal, rec);
+  void ctlop(int op, int arg = 0, double* rec = nullptr, long long step = 0) {
+    k_eng_ctl<<<1, 32, 0, st>>>(op, p, arg, step, ctl, mat, h->d_box, scal, rec);
   }
   template <typename T>
   void nodes_t(NodeOp o) {
@@ -475,24 +487,46 @@ struct Engine {
     if (h->prec == MM_PREC_FP32) k_eng_energy<true><<<1, kET, 0, st>>>(h->d_cpart, cell_grid(h), ctl);
     else k_eng_energy<false><<<1, kET, 0, st>>>(h->d_cpart, cell_grid(h), ctl);
   }
-  void baro_half() {
-    ctlop(CT_BARO_VEL);
+  // MTK / Langevin barostat half step (draws call0, call0 + 1 of the step)
+  void baro_half(long long step, int call0) {
+    ctlop(CT_BARO_VEL, call0, nullptr, step);
     ctlop(CT_BARO_POS);
     nodes(OP_SCALE_U, 0);
     forces();
     ctlop(CT_BARO_VSCALE);
     nodes(OP_SCALE_V, 1);
-    ctlop(CT_BARO_VEL);
+    ctlop(CT_BARO_VEL, call0 + 1, nullptr, step);
+  }
+  // barostat pre (call0 = 0) or post (call0 = 2) call of the MTK or Langevin barostat
+  void baro(long long step, int call0) {
+    if (p.thermo == TH_NHC) ctlop(CT_CV0);
+    if (p.baro == BA_LANGEVIN) ctlop(CT_LBARO_SAVE);
+    baro_half(step, call0);
+    if (p.baro == BA_LANGEVIN) ctlop(CT_LBARO_CORR);
+    else if (call0 != 0) ctlop(CT_ECB);
+  }
+  void berendsen_baro() {
+    ctlop(CT_BBARO);
+    nodes(OP_SCALE_U, 0);
+    forces();
+    ctlop(CT_BBARO_CORR);
   }
   void thermo(long long step, unsigned call) {
-    if (p.thermo == 1) {
+    if (p.thermo == TH_LANGEVIN) {
       ctlop(CT_SAVE_EKIN);
       nodes(OP_LANGEVIN, 1, step, call);
       ctlop(CT_LANG_CORR);
-    } else if (p.thermo == 2) {
-      ctlop(CT_NHC, p.baro == 1);
+    } else if (p.thermo == TH_NHC) {
+      ctlop(CT_NHC, p.baro == BA_MTK);
       nodes(OP_SCALE_VS, 1);
       if (call == 1) ctlop(CT_NHC_ECONS);
+    } else if (p.thermo == TH_BERENDSEN && call == 0) {
+      ctlop(CT_BER_T);
+      nodes(OP_SCALE_VS, 1);
+      ctlop(CT_BER_T_CORR);
+    } else if (p.thermo == TH_CSVR && call == 0) {
+      ctlop(CT_CSVR, 0, nullptr, step);
+      nodes(OP_SCALE_VS, 0);
     }
   }
 };
@@ -501,10 +535,10 @@ struct Engine {
 
 extern "C" mm_status mm_md_engine(mm_handle* h, double* pos, double* vel, int nsteps, double timestep, int thermo,
                                   double temp, double timecon, int baro, double press, int chain, uint64_t seed,
-                                  const double* noise, double* ctl_host, double* records, int64_t step0,
-                                  void* stream) {
-  if (!h || !pos || !vel || !ctl_host || nsteps < 0 || !(timestep > 0.0) || thermo < 0 || thermo > 2 || baro < 0 ||
-      baro > 1 || (thermo == 2 && chain != 3) || (thermo == 1 && !(timecon > 0.0)) || (baro == 1 && !h->pbc)) {
+                                  const double* noise, const double* hook_noise, double* ctl_host, double* records,
+                                  int64_t step0, void* stream) {
+  if (!h || !pos || !vel || !ctl_host || nsteps < 0 || !(timestep > 0.0) || !hooks_valid(thermo, timecon, baro, chain) ||
+      (thermo == TH_NHC && chain != 3) || (baro != BA_NONE && !h->pbc)) {
     mm::set_error("mm_md_engine: bad argument");
     return MM_ERR_ARG;
   }
@@ -550,7 +584,7 @@ extern "C" mm_status mm_md_engine(mm_handle* h, double* pos, double* vel, int ns
   BMD& p = E.p;
   p.dt = timestep;
   p.temp = temp;
-  p.timecon = thermo == 1 ? timecon : (timecon > 0 ? timecon : 1.0);
+  p.timecon = timecon > 0 ? timecon : 1.0;
   p.press = press;
   p.nsteps = nsteps;
   p.thermo = thermo;
@@ -559,6 +593,7 @@ extern "C" mm_status mm_md_engine(mm_handle* h, double* pos, double* vel, int ns
   p.seed = seed;
   p.step0 = step0;
   p.noise = noise;
+  p.hnoise = hook_noise;
   p.rec = nullptr;
   // Langevin amplitudes (same cache as mm_md_run)
   if (thermo == 1) {
@@ -586,20 +621,14 @@ extern "C" mm_status mm_md_engine(mm_handle* h, double* pos, double* vel, int ns
   E.nodes(OP_KINETIC, 1);  // kinetic totals of the initial velocities
   for (int s = 1; s <= nsteps; ++s) {
     const long long step = step0 + s;
-    if (baro) {
-      if (thermo == 2) E.ctlop(CT_CV0);
-      E.baro_half();
-    }
+    if (baro == BA_MTK || baro == BA_LANGEVIN) E.baro(step, 0);
     E.thermo(step, 0);
     E.nodes(OP_KICK_DRIFT, 0);
     E.forces();
     E.nodes(OP_KICK, 1);
     E.thermo(step, 1);
-    if (baro) {
-      if (thermo == 2) E.ctlop(CT_CV0);
-      E.baro_half();
-      E.ctlop(CT_ECB);
-    }
+    if (baro == BA_MTK || baro == BA_LANGEVIN) E.baro(step, 2);
+    if (baro == BA_BERENDSEN) E.berendsen_baro();
     E.ctlop(CT_RECORD, 0, records ? records + (size_t)(s - 1) * BR_LEN : nullptr);
   }
   launch_state_to_pos(h, pos, st);

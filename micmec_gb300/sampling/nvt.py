@@ -136,15 +136,30 @@ class LangevinThermostat(VerletHook):
 
 
 class CSVRThermostat(VerletHook):
-    """Canonical sampling through velocity rescaling (Bussi, Donadio, Parrinello 2007); nvt.py:221-274."""
+    """Canonical sampling through velocity rescaling (Bussi, Donadio, Parrinello, J. Chem. Phys.
+    126, 014101 (2007)); nvt.py:221-274.
+
+    Before every step the velocities are scaled by alpha with
+    alpha^2 = c + (S + R^2) f + 2 R sqrt(c f), c = exp(-dt / timecon),
+    f = (1 - c) K / (ndof ekin), K = ndof kT / 2, R a standard normal and S a chi-squared
+    variate with ndof - 1 degrees of freedom; the kinetic-energy change goes into the
+    conserved-quantity correction.
+
+    Extra, for validation: ``seed`` keys the device generator; ``replay_noise`` (shape
+    (nsteps, 2): R and S of each step, first row for step ``replay_offset + 1``) makes both
+    execution paths use given draws.
+    """
 
     name = "CSVR"
     kind = "stochastic"
     method = "thermostat"
 
-    def __init__(self, temp, start=0, timecon=100 * femtosecond):
+    def __init__(self, temp, start=0, timecon=100 * femtosecond, seed=None, replay_noise=None, replay_offset=0):
         self.temp = temp
         self.timecon = timecon
+        self.seed = int(np.random.randint(0, 2**62)) if seed is None else int(seed)
+        self.replay_noise = None if replay_noise is None else np.asarray(replay_noise, dtype=float)
+        self.replay_offset = replay_offset
         VerletHook.__init__(self, start, 1)
 
     def init(self, iterative):
@@ -153,10 +168,17 @@ class CSVRThermostat(VerletHook):
             iterative.ndof = get_ndof_internal_md(iterative.pos.shape[0], iterative.mmf.system.domain.nvec)
         self.kin = 0.5 * iterative.ndof * boltzmann * self.temp
 
-    def pre(self, iterative, G1_add=None):
-        c = np.exp(-iterative.timestep / self.timecon)
+    def _draws(self, iterative):
+        if self.replay_noise is not None:
+            r = self.replay_noise[iterative.counter - self.replay_offset]
+            return float(r[0]), float(r[1])
         R = np.random.normal(0, 1)
         S = (np.random.normal(0, 1, iterative.ndof - 1) ** 2).sum()
+        return R, S
+
+    def pre(self, iterative, G1_add=None):
+        c = np.exp(-iterative.timestep / self.timecon)
+        R, S = self._draws(iterative)
         iterative.ekin = iterative._compute_ekin()
         fact = (1 - c) * self.kin / iterative.ndof / iterative.ekin
         alpha = np.sign(R + np.sqrt(c / fact)) * np.sqrt(c + (S + R**2) * fact + 2 * R * np.sqrt(c * fact))

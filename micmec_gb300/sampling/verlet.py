@@ -5,15 +5,17 @@ Interface of micmec/sampling/verlet.py:49-374 (``VerletIntegrator``,
 
 Two execution paths with the same results:
 
-* device path (used by ``run`` when the force field is a single
-  ``ForcePartMechanical`` and the only Verlet hook is absent or a
-  ``LangevinThermostat``): the whole step loop runs on the GPU
-  (``mm_md_run``: one cell kernel and one fused gather/kick/thermostat/drift
-  kernel per step); positions and velocities stay in device memory and are
+* device paths (used by ``run`` when the force field is a single
+  ``ForcePartMechanical``): with no Verlet hook or a ``LangevinThermostat`` the whole
+  step loop runs on the GPU (``mm_md_run``: one cell kernel and one fused
+  gather/kick/thermostat/drift kernel per step); with a Nose-Hoover-chain, Berendsen or
+  CSVR thermostat and/or an anisotropic MTK, Berendsen or Langevin barostat (alone or in
+  a ``TBCombination``) the hooks run on the GPU too: in the one-CTA persistent batch
+  kernel for systems up to ``batch_max_cells`` cells, else in the grid-wide lattice
+  engine (``mm_md_engine``). Positions and velocities stay in device memory and are
   copied back only where a regular hook expects a call;
-* host path (any other combination, e.g. NHC thermostats and the MTK
-  barostat): the reference's step order on the host, with every force
-  evaluation on the GPU.
+* host path (any other combination): the reference's step order on the host, with
+  every force evaluation on the GPU.
 """
 
 import time
@@ -175,13 +177,14 @@ class VerletIntegrator(Iterative):
             return ("batch", spec)
         return False
 
-    # systems up to this many cells run NHC / MTK hooks in the one-CTA batch kernel
+    # systems up to this many cells run the thermostat / barostat hooks in the one-CTA batch kernel
     batch_max_cells = 32768
 
     def _batch_spec(self, vhooks, part):
-        """Hook set the persistent batch kernel runs: NHC and/or MTK (with NHC, Langevin or no thermostat)."""
-        from micmec_gb300.sampling.npt import MTKBarostat, TBCombination
-        from micmec_gb300.sampling.nvt import LangevinThermostat, NHCThermostat
+        """Hook set the persistent kernels run: a thermostat (NHC, Langevin, Berendsen, CSVR) and/or an
+        anisotropic barostat (MTK, Berendsen, Langevin), alone or in a TBCombination."""
+        from micmec_gb300.sampling.npt import BerendsenBarostat, LangevinBarostat, MTKBarostat, TBCombination
+        from micmec_gb300.sampling.nvt import BerendsenThermostat, CSVRThermostat, LangevinThermostat, NHCThermostat
 
         if len(vhooks) != 1 or not part.handle:
             return None
@@ -191,32 +194,116 @@ class VerletIntegrator(Iterative):
         thermo, baro = None, None
         if isinstance(h, TBCombination):
             thermo, baro = h.thermostat, h.barostat
-            if thermo.step != 1 or baro.step != 1:
+            if thermo.step != 1 or baro.step != 1 or thermo.start != 0 or baro.start != 0:
                 return None
-        elif type(h) is NHCThermostat:
+        elif type(h) in (NHCThermostat, BerendsenThermostat, CSVRThermostat):
             thermo = h
-        elif type(h) is MTKBarostat:
+        elif type(h) in (MTKBarostat, BerendsenBarostat, LangevinBarostat):
             baro = h
         else:
             return None
-        if thermo is not None and type(thermo) not in (NHCThermostat, LangevinThermostat):
+        if thermo is not None and type(thermo) not in (NHCThermostat, LangevinThermostat, BerendsenThermostat,
+                                                       CSVRThermostat):
             return None
-        if baro is not None and (type(baro) is not MTKBarostat or not baro.anisotropic or baro.vol_constraint
-                                 or baro.baro_thermo is not None):
+        if type(thermo) is CSVRThermostat and baro is not None:
             return None
+        if baro is not None:
+            if type(baro) not in (MTKBarostat, BerendsenBarostat, LangevinBarostat):
+                return None
+            if not baro.anisotropic or baro.vol_constraint or getattr(baro, "baro_thermo", None) is not None:
+                return None
+            if not part.pbc:
+                return None
         if type(thermo) is NHCThermostat and thermo.chain.length != 3:
-            return None
-        if baro is not None and not part.pbc:
             return None
         s = self.mmf.system
         grid = np.asarray(s.grid)
         small = (part.pbc and not (grid == 0).any() and s.nnodes == grid.size and s.ncells <= self.batch_max_cells)
         return dict(hook=h, thermo=thermo, baro=baro, engine="batch" if small else "lattice")
 
+    def _hook_control(self, thermo, baro):
+        """Control block (layout of the batch/engine kernels) and kernel arguments from the
+        initialised hooks: (ctl, thermostat kind, barostat kind, temp, timecon, seed)."""
+        from micmec_gb300.batch import CTL, CTL_LEN
+        from micmec_gb300.sampling.npt import BerendsenBarostat, LangevinBarostat, MTKBarostat
+        from micmec_gb300.sampling.nvt import BerendsenThermostat, CSVRThermostat, LangevinThermostat, NHCThermostat
+
+        c = np.zeros(CTL_LEN)
+        c[CTL["ndof"]] = self.ndof
+        kind, bkind, temp, timecon, seed = None, None, 0.0, 1.0, 0
+        if thermo is not None:
+            kind = {NHCThermostat: "nhc", LangevinThermostat: "langevin", BerendsenThermostat: "berendsen",
+                    CSVRThermostat: "csvr"}[type(thermo)]
+            temp = thermo.temp
+            timecon = thermo.chain.timecon if kind == "nhc" else thermo.timecon
+            c[CTL["econs_thermo"]] = thermo.econs_correction
+            seed = getattr(thermo, "seed", 0)
+        if type(thermo) is NHCThermostat:
+            c[CTL["chain_pos"]] = thermo.chain.pos
+            c[CTL["chain_vel"]] = thermo.chain.vel
+            c[CTL["chain_mass"]] = thermo.chain.masses
+            c[CTL["chain_ndof"]] = thermo.chain.ndof
+        if baro is not None:
+            bkind = {MTKBarostat: "mtk", BerendsenBarostat: "berendsen", LangevinBarostat: "langevin"}[type(baro)]
+            if getattr(baro, "vel_press", None) is not None:
+                c[CTL["vel_press"]] = np.asarray(baro.vel_press).ravel()
+            c[CTL["mass_press"]] = baro.mass_press
+            c[CTL["baro_ndof"]] = baro.baro_ndof
+            c[CTL["econs_baro"]] = baro.econs_correction
+            if bkind == "langevin":
+                c[CTL["timecon_press"]] = baro.timecon
+                c[CTL["temp_press"]] = baro.temp
+                if kind not in ("langevin", "csvr"):
+                    seed = baro.seed
+            if thermo is None:
+                temp = baro.temp
+        return c, kind, bkind, temp, timecon, seed
+
+    def _replays(self, thermo, baro, nsteps):
+        """Replayed draws of the stochastic hooks for the next nsteps steps: (Langevin thermostat
+        normals (2 nsteps, N, 3) or None, hook draws (nsteps, HOOK_NOISE_LEN) or None)."""
+        from micmec_gb300.batch import HOOK_NOISE_LEN
+        from micmec_gb300.sampling.npt import LangevinBarostat
+        from micmec_gb300.sampling.nvt import CSVRThermostat, LangevinThermostat
+
+        noise, hook = None, None
+        if type(thermo) is LangevinThermostat and thermo.replay_noise is not None:
+            i0 = 2 * (self.counter - thermo.replay_offset)
+            noise = np.ascontiguousarray(thermo.replay_noise[i0:i0 + 2 * nsteps])
+            if noise.shape[0] != 2 * nsteps:
+                raise ValueError("replay_noise is too short for this run")
+        sources = []
+        if type(thermo) is CSVRThermostat and thermo.replay_noise is not None:
+            sources.append((thermo, slice(0, 2), 2))
+        if type(baro) is LangevinBarostat and baro.replay_noise is not None:
+            sources.append((baro, slice(2, 26), 24))
+        stochastic = int(type(thermo) is CSVRThermostat) + int(type(baro) is LangevinBarostat)
+        if sources:
+            if len(sources) != stochastic:
+                raise ValueError("replay draws for some stochastic hooks but not for others")
+            hook = np.zeros((nsteps, HOOK_NOISE_LEN))
+            for h, cols, n in sources:
+                i0 = self.counter - h.replay_offset
+                rows = np.asarray(h.replay_noise[i0:i0 + nsteps]).reshape(-1, n)
+                if rows.shape[0] != nsteps:
+                    raise ValueError("replay_noise is too short for this run")
+                hook[:, cols] = rows
+        return noise, hook
+
+    def _hook_back(self, thermo, baro, c):
+        """Hook state after a device run, from the returned control block."""
+        from micmec_gb300.batch import CTL
+        from micmec_gb300.sampling.nvt import NHCThermostat
+
+        if type(thermo) is NHCThermostat:
+            thermo.chain.pos[:] = c[CTL["chain_pos"]]
+            thermo.chain.vel[:] = c[CTL["chain_vel"]]
+        if baro is not None and getattr(baro, "vel_press", None) is not None:
+            baro.vel_press = c[CTL["vel_press"]].reshape(3, 3).copy()
+
     def _run_batch(self, nsteps, spec):
-        """NHC / MTK hooks on the device: the system as a one-element batch (one persistent CTA)."""
-        from micmec_gb300.batch import BatchSystems, CTL, REC
-        from micmec_gb300.sampling.nvt import LangevinThermostat, NHCThermostat
+        """Thermostat / barostat hooks on the device: the system as a one-element batch (one persistent CTA)."""
+        from micmec_gb300.batch import CTL, BatchSystems
 
         part = self.mmf.parts[0]
         thermo, baro, hook = spec["thermo"], spec["baro"], spec["hook"]
@@ -224,107 +311,57 @@ class VerletIntegrator(Iterative):
         if b is None:
             b = self._batch = BatchSystems([self.mmf.system], model=part.model, precision=part.precision)
         b.set_state([self.pos], [self.vel], [self.mmf.system.domain.rvecs])
-        c = b.control()
-        c[0, CTL["ndof"]] = self.ndof
-        kind, temp, timecon, noise = None, 0.0, 1.0, None
-        if type(thermo) is NHCThermostat:
-            kind, temp, timecon = "nhc", thermo.temp, thermo.chain.timecon
-            c[0, CTL["chain_pos"]] = thermo.chain.pos
-            c[0, CTL["chain_vel"]] = thermo.chain.vel
-            c[0, CTL["chain_mass"]] = thermo.chain.masses
-            c[0, CTL["econs_thermo"]] = thermo.econs_correction
-        elif type(thermo) is LangevinThermostat:
-            kind, temp, timecon = "langevin", thermo.temp, thermo.timecon
-            c[0, CTL["econs_thermo"]] = thermo.econs_correction
-        if baro is not None:
-            c[0, CTL["vel_press"]] = np.asarray(baro.vel_press).ravel()
-            c[0, CTL["mass_press"]] = baro.mass_press
-            c[0, CTL["baro_ndof"]] = baro.baro_ndof
-            c[0, CTL["econs_baro"]] = baro.econs_correction
-            temp = temp if thermo is not None else baro.temp
-        c[0, CTL["epot"]] = self.epot
-        c[0, CTL["vtens"]] = self.vtens.ravel()
-        b.set_control(c)
-        seed = 0
-        if type(thermo) is LangevinThermostat:
-            seed = thermo.seed
-            if thermo.replay_noise is not None:
-                i0 = 2 * (self.counter - thermo.replay_offset)
-                noise = np.asarray(thermo.replay_noise[i0:i0 + 2 * nsteps]).reshape(nsteps, 2, -1, 3)
-        rec = b.md(nsteps, timestep=self.timestep, thermostat=kind, temp=temp, timecon=timecon,
-                   barostat="mtk" if baro is not None else None, press=0.0 if baro is None else baro.press,
-                   seed=seed, step0=self.counter, noise=noise, record=True, use_graph=False)[0]
+        c, kind, bkind, temp, timecon, seed = self._hook_control(thermo, baro)
+        c0 = b.control()[0]
+        for key in ("L", "rvecs", "volume"):  # lattice matrix and domain as set_state left them
+            c[CTL[key]] = c0[CTL[key]]
+        c[CTL["epot"]] = self.epot
+        c[CTL["vtens"]] = self.vtens.ravel()
+        b.set_control(c[None, :])
+        noise, hook_noise = self._replays(thermo, baro, nsteps)
+        if noise is not None:
+            noise = noise.reshape(nsteps, 2, -1, 3)
+        if hook_noise is not None:
+            hook_noise = hook_noise[:, None, :]
+        rec = b.md(nsteps, timestep=self.timestep, thermostat=kind, temp=temp, timecon=timecon, barostat=bkind,
+                   press=0.0 if baro is None else baro.press, seed=seed, step0=self.counter, noise=noise,
+                   hook_noise=hook_noise, record=True, use_graph=False)[0]
         if not np.isfinite(rec[:, :3]).all():
             raise ValueError("The energy is not-a-number (``nan``).")
         pos, vel, rv = b.get_state()
-        c = b.control()
-        if type(thermo) is NHCThermostat:
-            thermo.chain.pos[:] = c[0, CTL["chain_pos"]]
-            thermo.chain.vel[:] = c[0, CTL["chain_vel"]]
-        if baro is not None:
-            baro.vel_press = c[0, CTL["vel_press"]].reshape(3, 3).copy()
-        return rec, pos[0], vel[0], rv[0], c[0], (thermo, baro, hook)
-
-    def _hook_control(self, thermo, baro):
-        """Control block (layout of the batch/engine kernels) from the initialised hooks."""
-        from micmec_gb300.batch import CTL, CTL_LEN
-        from micmec_gb300.sampling.nvt import LangevinThermostat, NHCThermostat
-
-        c = np.zeros(CTL_LEN)
-        c[CTL["ndof"]] = self.ndof
-        kind, temp, timecon = None, 0.0, 1.0
-        if type(thermo) is NHCThermostat:
-            kind, temp, timecon = "nhc", thermo.temp, thermo.chain.timecon
-            c[CTL["chain_pos"]] = thermo.chain.pos
-            c[CTL["chain_vel"]] = thermo.chain.vel
-            c[CTL["chain_mass"]] = thermo.chain.masses
-            c[CTL["econs_thermo"]] = thermo.econs_correction
-        elif type(thermo) is LangevinThermostat:
-            kind, temp, timecon = "langevin", thermo.temp, thermo.timecon
-            c[CTL["econs_thermo"]] = thermo.econs_correction
-        if baro is not None:
-            c[CTL["vel_press"]] = np.asarray(baro.vel_press).ravel()
-            c[CTL["mass_press"]] = baro.mass_press
-            c[CTL["baro_ndof"]] = baro.baro_ndof
-            c[CTL["econs_baro"]] = baro.econs_correction
-            temp = temp if thermo is not None else baro.temp
-        return c, kind, temp, timecon
+        c = b.control()[0]
+        self._hook_back(thermo, baro, c)
+        return rec, pos[0], vel[0], rv[0], c, (thermo, baro, hook)
 
     def _run_engine(self, nsteps, spec):
-        """NHC / MTK hooks on the device for a system spread over the whole GPU (mm_md_engine)."""
+        """Thermostat / barostat hooks on the device for a system spread over the whole GPU (mm_md_engine)."""
         import torch
 
         from micmec_gb300 import _native as nat
-        from micmec_gb300.batch import CTL, REC_LEN
-        from micmec_gb300.sampling.nvt import LangevinThermostat, NHCThermostat
+        from micmec_gb300.batch import CTL, REC_LEN, _BARO, _THERMO
 
         part = self.mmf.parts[0]
         thermo, baro, hook = spec["thermo"], spec["baro"], spec["hook"]
-        c, kind, temp, timecon = self._hook_control(thermo, baro)
+        c, kind, bkind, temp, timecon, seed = self._hook_control(thermo, baro)
+        c[CTL["epot"]] = self.epot
+        c[CTL["vtens"]] = self.vtens.ravel()
         dev = part.device
         pos_d = torch.from_numpy(np.ascontiguousarray(self.pos)).to(dev)
         vel_d = torch.from_numpy(np.ascontiguousarray(self.vel)).to(dev)
         rec = torch.zeros((nsteps, REC_LEN), dtype=torch.float64, device=dev)
-        noise, seed = None, 0
-        if type(thermo) is LangevinThermostat:
-            seed = thermo.seed
-            if thermo.replay_noise is not None:
-                i0 = 2 * (self.counter - thermo.replay_offset)
-                noise = torch.from_numpy(np.ascontiguousarray(thermo.replay_noise[i0:i0 + 2 * nsteps])).to(dev)
+        noise, hook_noise = self._replays(thermo, baro, nsteps)
+        noise = None if noise is None else torch.from_numpy(noise).to(dev)
+        hook_noise = None if hook_noise is None else torch.from_numpy(np.ascontiguousarray(hook_noise)).to(dev)
         st = nat.lib().mm_md_engine(part.handle, pos_d.data_ptr(), vel_d.data_ptr(), int(nsteps), float(self.timestep),
-                                    {None: 0, "langevin": 1, "nhc": 2}[kind], float(temp), float(timecon),
-                                    1 if baro is not None else 0, 0.0 if baro is None else float(baro.press), 3,
-                                    int(seed), nat.ptr(noise), c.ctypes.data, rec.data_ptr(), int(self.counter),
+                                    _THERMO[kind], float(temp), float(timecon), _BARO[bkind],
+                                    0.0 if baro is None else float(baro.press), 3, int(seed), nat.ptr(noise),
+                                    nat.ptr(hook_noise), c.ctypes.data, rec.data_ptr(), int(self.counter),
                                     torch.cuda.current_stream().cuda_stream)
         nat.check(st, "mm_md_engine")
         rec = rec.cpu().numpy()
         if not np.isfinite(rec[:, :3]).all():
             raise ValueError("The energy is not-a-number (``nan``).")
-        if type(thermo) is NHCThermostat:
-            thermo.chain.pos[:] = c[CTL["chain_pos"]]
-            thermo.chain.vel[:] = c[CTL["chain_vel"]]
-        if baro is not None:
-            baro.vel_press = c[CTL["vel_press"]].reshape(3, 3).copy()
+        self._hook_back(thermo, baro, c)
         rv = c[CTL["rvecs"]].reshape(3, 3).copy()
         return rec, pos_d.cpu().numpy(), vel_d.cpu().numpy(), rv, c, (thermo, baro, hook)
 

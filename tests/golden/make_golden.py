@@ -12,8 +12,9 @@ barostat, builder and ``QNOptimizer`` on small seeded inputs, and writes the
 inputs and outputs as compressed ``.npz`` files next to this script. The tests
 read only those files; they never touch the reference at run time.
 
-Random draws the reference makes with ``np.random.normal`` (Langevin noise) are
-recorded into the fixtures so the GPU path can replay them.
+Random draws the reference makes with ``np.random.normal`` (Langevin noise, the CSVR
+thermostat's scalars, the Langevin barostat's random tensors) are recorded into the
+fixtures so the GPU path can replay them.
 """
 
 import os
@@ -36,8 +37,8 @@ from micmec.system import System  # noqa: E402
 from micmec.pes.mmff import MicMecForceField, ForcePartMechanical  # noqa: E402
 from micmec.sampling.verlet import VerletIntegrator  # noqa: E402
 from micmec.sampling.iterative import Hook  # noqa: E402
-from micmec.sampling.nvt import LangevinThermostat, NHCThermostat  # noqa: E402
-from micmec.sampling.npt import MTKBarostat  # noqa: E402
+from micmec.sampling.nvt import BerendsenThermostat, CSVRThermostat, LangevinThermostat, NHCThermostat  # noqa: E402
+from micmec.sampling.npt import BerendsenBarostat, LangevinBarostat, MTKBarostat, TBCombination  # noqa: E402
 from micmec.sampling.dof import CartesianDOF  # noqa: E402
 from micmec.sampling.opt import QNOptimizer  # noqa: E402
 from micmec import utils as rutils  # noqa: E402
@@ -248,6 +249,7 @@ def run_md(tag, model, nsteps, hooks_fn, every_pos, seed=1, dt_fs=1.0, record_no
     if record_noise:
         arrays["noise"] = np.array([d for d in nl.draws if d.shape == s.pos.shape])
     if extra:
+        vi.noise_draws = nl.draws
         extra(arrays, vi)
     save("md_" + tag, **arrays)
 
@@ -317,6 +319,84 @@ def make_md_fixtures():
     run_md("langevin_mtk_nanocell", "nanocell", 50, lang_mtk, 25, record_noise=True, extra=mtk_extra)
 
 
+def make_hook_fixtures():
+    """The rest of the hook set TBCombination accepts (npt.py:163-177) and the CSVR thermostat."""
+    T = 300.0 * units.kelvin
+    fs = units.femtosecond
+    press = 100e6 * units.pascal
+    rng = np.random.default_rng(6)
+    chain_vel0 = rng.normal(0, 1e-5, 3)
+    vp = rng.normal(0, 1e-6, (3, 3))
+    vp = 0.5 * (vp + vp.T)
+    tril = [(i, j) for i in range(3) for j in range(i + 1)]
+
+    def end_state(arrays, vi):
+        hook = [h for h in vi.hooks if h.name in ("TBCombination", "Langevin", "Berendsen", "MTTK", "CSVR")][0]
+        baro = getattr(hook, "barostat", hook if getattr(hook, "method", "") == "barostat" else None)
+        thermo = getattr(hook, "thermostat", hook if getattr(hook, "method", "") == "thermostat" else None)
+        arrays["rvecs_end"] = vi.mmf.system.domain.rvecs
+        if baro is not None and getattr(baro, "vel_press", None) is not None:
+            arrays["vel_press_end"] = np.asarray(baro.vel_press)
+        if thermo is not None and hasattr(thermo, "chain"):
+            arrays["chain_pos_end"] = thermo.chain.pos
+            arrays["chain_vel_end"] = thermo.chain.vel
+        draws = vi.noise_draws
+        if isinstance(baro, LangevinBarostat):
+            # first (3, 3) draw: the initial barostat velocity (get_random_vel_press); then
+            # four unit-normal tensors per step (getR, lower triangle used)
+            mats = [d for d in draws if d.shape == (3, 3)]
+            arrays["vel_press0"] = baro.vel_press0
+            arrays["baro_noise"] = np.array([[m[i, j] for (i, j) in tril] for m in mats[1:]]).reshape(-1, 4, 6)
+        if isinstance(thermo, CSVRThermostat):
+            R = [float(d) for d in draws if d.shape == ()]
+            S = [float((d ** 2).sum()) for d in draws if d.ndim == 1]
+            arrays["csvr_noise"] = np.array([R, S]).T
+
+    class LB(LangevinBarostat):
+        def init(self, iterative):
+            LangevinBarostat.init(self, iterative)
+            self.vel_press0 = np.array(self.vel_press, dtype=float).copy()
+
+    def berendsen(ff):
+        return [BerendsenThermostat(2 * T, timecon=50 * fs)], {"temp": 2 * T, "timecon": 50 * fs}
+
+    run_md("berendsen_nanocell", "nanocell", 200, berendsen, 50, extra=end_state)
+
+    def csvr(ff):
+        return [CSVRThermostat(2 * T, timecon=50 * fs)], {"temp": 2 * T, "timecon": 50 * fs}
+
+    run_md("csvr_nanocell", "nanocell", 200, csvr, 50, extra=end_state)
+
+    def berendsen_mtk(ff):
+        b = MTKBarostat(ff, T, press, timecon=1000 * fs, vel_press0=vp.copy())
+        t = BerendsenThermostat(T, timecon=100 * fs)
+        return [TBCombination(t, b)], {"temp": T, "press": press, "timecon_baro": 1000 * fs,
+                                       "timecon_thermo": 100 * fs, "vel_press0": vp}
+
+    run_md("berendsen_mtk_nanocell", "nanocell", 100, berendsen_mtk, 25, extra=end_state)
+
+    def nhc_bbaro(ff):
+        b = BerendsenBarostat(ff, T, press, timecon=1000 * fs)
+        t = NHCThermostat(T, timecon=100 * fs, chainlength=3, chain_vel0=chain_vel0.copy())
+        return [TBCombination(t, b)], {"temp": T, "press": press, "timecon_baro": 1000 * fs,
+                                       "timecon_thermo": 100 * fs, "chain_vel0": chain_vel0}
+
+    run_md("nhc_bbaro_nanocell", "nanocell", 100, nhc_bbaro, 25, extra=end_state)
+
+    def lbaro(ff):
+        return [LB(ff, T, press, timecon=1000 * fs)], {"temp": T, "press": press, "timecon": 1000 * fs}
+
+    run_md("lbaro_nanocell", "nanocell", 100, lbaro, 25, extra=end_state)
+
+    def nhc_lbaro(ff):
+        b = LB(ff, T, press, timecon=1000 * fs)
+        t = NHCThermostat(T, timecon=100 * fs, chainlength=3, chain_vel0=chain_vel0.copy())
+        return [TBCombination(t, b)], {"temp": T, "press": press, "timecon_baro": 1000 * fs,
+                                       "timecon_thermo": 100 * fs, "chain_vel0": chain_vel0}
+
+    run_md("nhc_lbaro_nanocell", "nanocell", 100, nhc_lbaro, 25, extra=end_state)
+
+
 # ------------------------------------------------------------------ optimiser
 
 
@@ -340,12 +420,14 @@ def make_opt_fixture():
 
 
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["forces", "builder", "md", "opt"]
+    which = sys.argv[1:] or ["forces", "builder", "md", "hooks", "opt"]
     if "forces" in which:
         make_force_fixtures()
     if "builder" in which:
         make_builder_fixture()
     if "md" in which:
         make_md_fixtures()
+    if "hooks" in which:
+        make_hook_fixtures()
     if "opt" in which:
         make_opt_fixture()

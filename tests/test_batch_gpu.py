@@ -79,6 +79,48 @@ def test_batch_mtk_matches_reference(name):
     assert np.allclose(rv[0], g["rvecs_end"], rtol=1e-9)
 
 
+@pytest.mark.parametrize("name", ["md_berendsen_nanocell", "md_csvr_nanocell", "md_berendsen_mtk_nanocell",
+                                  "md_nhc_bbaro_nanocell", "md_lbaro_nanocell", "md_nhc_lbaro_nanocell"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_batch_hooks_match_reference(name, precision):
+    """Berendsen / CSVR thermostats, Berendsen / Langevin barostats through the batch API
+    (hook constants from setup_md, replayed draws as hook noise)."""
+    from micmec_gb300.batch import HOOK_NOISE_LEN
+
+    g, b = _golden_batch(name, precision=precision)
+    T = float(g["meta/temp"])
+    n = len(g["records"]) - 1
+    tag = name[3:-9]
+    thermo = {"berendsen": "berendsen", "csvr": "csvr", "berendsen_mtk": "berendsen", "nhc_bbaro": "nhc",
+              "lbaro": None, "nhc_lbaro": "nhc"}[tag]
+    baro = {"berendsen": None, "csvr": None, "berendsen_mtk": "mtk", "nhc_bbaro": "berendsen", "lbaro": "langevin",
+            "nhc_lbaro": "langevin"}[tag]
+    tt = float(g["meta/timecon_thermo"]) if "meta/timecon_thermo" in g.files else float(g["meta/timecon"])
+    tb = float(g["meta/timecon_baro"]) if "meta/timecon_baro" in g.files else float(g["meta/timecon"])
+    P = float(g["meta/press"]) if baro else 0.0
+    vp0 = None
+    if baro == "mtk":
+        vp0 = [g["meta/vel_press0"]]
+    elif baro == "langevin":
+        vp0 = [g["vel_press0"]]
+    chain0 = [g["meta/chain_vel0"]] if thermo == "nhc" else None
+    b.setup_md(vel=[g["vel0"]], thermostat=thermo, temp=T, timecon=tt, chain_vel0=chain0, barostat=baro,
+               baro_timecon=tb, vel_press0=vp0)
+    hook = None
+    if thermo == "csvr" or baro == "langevin":
+        hook = np.zeros((n, 1, HOOK_NOISE_LEN))
+        if thermo == "csvr":
+            hook[:, 0, 0:2] = g["csvr_noise"][:n]
+        if baro == "langevin":
+            hook[:, 0, 2:26] = g["baro_noise"][:n].reshape(n, 24)
+    rec = b.md(n, timestep=float(g["timestep"]), thermostat=thermo, temp=T, timecon=tt, barostat=baro, press=P,
+               hook_noise=hook, record=True)
+    _check(g, rec[0], n, 1e-7 if precision == "fp64" else 2e-5)
+    _, _, rv = b.get_state()
+    ref = g["rvecs_end"]
+    assert np.abs(rv[0] - ref).max() <= (1e-9 if precision == "fp64" else 1e-7) * np.abs(ref).max()
+
+
 def _mixed_batch(ns, precision, seed=0, sigma=0.1, strains=None):
     from micmec_gb300 import lattices, units
     from micmec_gb300.batch import BatchSystems

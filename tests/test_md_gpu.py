@@ -278,3 +278,84 @@ def test_engine_on_lattice_with_vacancies_follows_host_path():
         scale = np.abs(h[:, col]).max()
         assert np.abs(e64[:, col] - h[:, col]).max() <= 1e-9 * scale
         assert np.abs(e32[:, col] - h[:, col]).max() <= 1e-5 * scale
+
+
+HOOK_NAMES = ["md_berendsen_nanocell", "md_csvr_nanocell", "md_berendsen_mtk_nanocell", "md_nhc_bbaro_nanocell",
+              "md_lbaro_nanocell", "md_nhc_lbaro_nanocell"]
+
+
+@pytest.mark.parametrize("device", ["batch", "engine", "host"])
+@pytest.mark.parametrize("name", HOOK_NAMES)
+def test_hooks_match_reference(name, device):
+    """Berendsen / CSVR thermostats and Berendsen / Langevin barostats on the device paths."""
+    from test_hooks_cpu import hooks_for
+
+    from micmec_gb300.sampling.verlet import VerletIntegrator
+
+    g, s, ff = _setup(name)
+    rec = Rec()
+    n = len(g["records"]) - 1
+    vi = VerletIntegrator(ff, float(g["timestep"]), hooks=hooks_for(name, g, ff) + [rec.hook], vel0=g["vel0"].copy(),
+                          device=device != "host")
+    if device == "engine":
+        vi.batch_max_cells = 0
+    if device != "host":
+        assert vi._device_plan()[1]["engine"] == ("batch" if device == "batch" else "lattice")
+    vi.run(n)
+    _compare(g, rec, n, 1e-7)
+    assert np.allclose(s.domain.rvecs, g["rvecs_end"], rtol=1e-9)
+    if "chain_pos_end" in g.files:
+        hook = [h for h in vi.hooks if hasattr(h, "thermostat")][0]
+        assert np.allclose(hook.thermostat.chain.pos, g["chain_pos_end"], rtol=1e-6, atol=1e-12)
+
+
+@pytest.mark.parametrize("hooks", ["csvr", "nhc_lbaro"])
+def test_generated_hook_draws_agree_between_batch_and_engine(hooks):
+    """Without replay, the batch kernel and the lattice engine draw the same CSVR and
+    Langevin-barostat numbers (the same generator stream keyed by system, step and call)."""
+    from micmec_gb300 import units
+    from micmec_gb300.pes.mmff import ForcePartMechanical, MicMecForceField
+    from micmec_gb300.sampling.npt import LangevinBarostat
+    from micmec_gb300.sampling.nvt import CSVRThermostat, NHCThermostat
+    from micmec_gb300.sampling.verlet import VerletIntegrator
+
+    rows = {}
+    for engine in ("batch", "lattice"):
+        s, vel = _lattice(4, 2, 12)
+        ff = MicMecForceField(s, [ForcePartMechanical(s, model="nanocell", precision="fp64")])
+        if hooks == "csvr":
+            hs = [CSVRThermostat(600.0, timecon=50 * units.femtosecond, seed=11)]
+        else:
+            hs = [NHCThermostat(300.0, timecon=100 * units.femtosecond, chain_vel0=np.zeros(3)),
+                  LangevinBarostat(ff, 300.0, 1e8 * units.pascal, timecon=2000 * units.femtosecond,
+                                   vel_press0=np.zeros((3, 3)), seed=11)]
+        rec = Rec()
+        vi = VerletIntegrator(ff, 1.0 * units.femtosecond, hooks=hs + [rec.hook], vel0=vel, device=True)
+        if engine == "lattice":
+            vi.batch_max_cells = 0
+        assert vi._device_plan()[1]["engine"] == engine
+        vi.run(60)
+        rows[engine] = np.array(rec.rows)
+    a, b = rows["batch"], rows["lattice"]
+    assert np.isfinite(a).all()
+    for col in (1, 2, 3):
+        assert np.abs(a[:, col] - b[:, col]).max() <= 1e-7 * np.abs(b[:, col]).max()
+
+
+def test_csvr_generator_samples_canonical_kinetic_energy():
+    """CSVR with the device generator (normal R, chi-squared S by Marsaglia-Tsang): the
+    kinetic energy follows the canonical Gamma(ndof/2, kT) law in mean and variance."""
+    from micmec_gb300 import units
+    from micmec_gb300.batch import REC, BatchSystems
+
+    systems = [_lattice(4, 1, 20 + i)[0] for i in range(48)]
+    b = BatchSystems(systems, model="nanocell", precision="fp64")
+    T = 600.0
+    b.setup_md(temp=300.0, thermostat="csvr", seed=3)
+    rec = b.md(4000, timestep=1.0 * units.femtosecond, thermostat="csvr", temp=T,
+               timecon=50 * units.femtosecond, seed=5, record=True)
+    ndof = 3 * systems[0].nnodes - 3
+    kT = units.boltzmann * T
+    ek = rec[:, 1000:, REC["ekin"]].ravel()
+    assert abs(ek.mean() / (0.5 * ndof * kT) - 1.0) < 0.02
+    assert abs(ek.var() / (0.5 * ndof * kT ** 2) - 1.0) < 0.15
