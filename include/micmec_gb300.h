@@ -267,6 +267,17 @@ mm_status mm_batch_md(mm_batch* b, int nsteps, double timestep, int thermo, doub
                       const double* hook_noise, double* records, int use_graph, void* stream);
 /* Relax node positions of every system (domain fixed) until max |gradient| < gtol. */
 mm_status mm_batch_relax(mm_batch* b, int max_iter, double gtol, void* stream);
+/*
+ * Relax node positions and domain of every system together (the reference's
+ * BaseCellDOF with CG/QN, micmec/sampling/dof.py:199-697, opt.py:147-443): full = 0
+ * StrainCellDOF (rvecs = A rvecs0, A symmetric), full = 1 FullCellDOF (all nine domain
+ * components); external pressure `press` adds E = P V (ForcePartPressure). Stops when
+ * max |node gradient| < gtol and max |vtens / V + P I| < stol, or after max_iter
+ * iterations; the controller block then holds the domain, energy, virial, the largest
+ * gradient (62), iterations (63) and the largest residual stress (69).
+ */
+mm_status mm_batch_relax_cell(mm_batch* b, int max_iter, double gtol, double stol, double press, int full,
+                              void* stream);
 /* Choose CTA size and persistent CTA count by timing probe_steps MD steps (state restored). */
 mm_status mm_batch_autotune(mm_batch* b, int probe_steps, double timestep, int thermo, double temp, double timecon,
                             int baro, double press, int chain, double* best_ms);

@@ -27,7 +27,7 @@ __all__ = ["BatchSystems", "CTL", "REC", "HOOK_NOISE_LEN"]
 CTL = dict(L=slice(0, 9), rvecs=slice(9, 18), volume=18, epot=19, ekin=20, vtens=slice(21, 30), ktens=slice(30, 39),
            vel_press=slice(39, 48), chain_pos=slice(48, 51), chain_vel=slice(51, 54), chain_mass=slice(54, 57),
            ndof=57, mass_press=58, baro_ndof=59, econs_thermo=60, econs_baro=61, gmax=62, iters=63, alpha=64,
-           chain_ndof=65, timecon_press=66, temp_press=67)
+           chain_ndof=65, timecon_press=66, temp_press=67, stress_res=69)
 CTL_LEN = 72
 REC = dict(epot=0, ekin=1, ecorr=2, volume=3, vtens=slice(4, 13), ktens=slice(13, 22), rvecs=slice(22, 31))
 REC_LEN = 31
@@ -50,11 +50,13 @@ def _declare(L):
                               ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_uint64, ctypes.c_int64, P, P, P,
                               ctypes.c_int, P]
     L.mm_batch_relax.argtypes = [P, ctypes.c_int, ctypes.c_double, P]
+    L.mm_batch_relax_cell.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                      ctypes.c_int, P]
     L.mm_batch_autotune.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_int, ctypes.c_double, ctypes.c_int, P]
     L.mm_batch_config.argtypes = [P, P, P]
     for n in ("mm_batch_create", "mm_batch_destroy", "mm_batch_set_state", "mm_batch_get_state", "mm_batch_control",
-              "mm_batch_md", "mm_batch_relax", "mm_batch_autotune", "mm_batch_config"):
+              "mm_batch_md", "mm_batch_relax", "mm_batch_relax_cell", "mm_batch_autotune", "mm_batch_config"):
         getattr(L, n).restype = ctypes.c_int
     L._batch_declared = True
 
@@ -248,13 +250,27 @@ class BatchSystems(object):
             return rec.cpu().numpy()
         return None
 
-    def relax(self, max_iter=2000, gtol=1e-6):
-        """CG relaxation of node positions; returns (largest gradient norm, iterations) per system."""
+    def relax(self, max_iter=2000, gtol=1e-6, cell=None, press=0.0, stress_tol=1e-9):
+        """CG relaxation of every system; returns (largest gradient norm, iterations) per system.
+
+        cell=None: node positions only (the domain is fixed). cell="strain" / "full": positions
+        and domain together, as StrainCellDOF / FullCellDOF (dof.py:492-697), at external
+        pressure ``press`` (E + P V); converged when max |gpos| < gtol and the largest residual
+        stress component |vtens / V + P I| < stress_tol (atomic units)."""
         torch = self.torch
-        nat.check(self.L.mm_batch_relax(self._h, int(max_iter), float(gtol), torch.cuda.current_stream().cuda_stream),
-                  "mm_batch_relax")
+        stream = torch.cuda.current_stream().cuda_stream
+        if cell is None:
+            nat.check(self.L.mm_batch_relax(self._h, int(max_iter), float(gtol), stream), "mm_batch_relax")
+        else:
+            full = {"strain": 0, "full": 1}[cell]
+            nat.check(self.L.mm_batch_relax_cell(self._h, int(max_iter), float(gtol), float(stress_tol), float(press),
+                                                 full, stream), "mm_batch_relax_cell")
         c = self.control()
         return c[:, CTL["gmax"]], c[:, CTL["iters"]]
+
+    def residual_stress(self):
+        """Largest residual stress component of the last cell relaxation, per system."""
+        return self.control()[:, CTL["stress_res"]]
 
     def autotune(self, probe_steps=5, timestep=1.0 * femtosecond, thermostat=None, temp=300.0,
                  timecon=100 * femtosecond, barostat=None, press=0.0, chainlength=3):

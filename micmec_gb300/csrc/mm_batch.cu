@@ -150,6 +150,9 @@ void launch_md(mm_batch* b, const BMD& p, cudaStream_t st) { mmb::launch_md(batc
 void launch_relax(mm_batch* b, int max_iter, double gtol, cudaStream_t st) {
   mmb::launch_relax(batch_launch(b), max_iter, gtol, st);
 }
+void launch_relax_cell(mm_batch* b, const CellRelax& r, cudaStream_t st) {
+  mmb::launch_relax_cell(batch_launch(b), r, st);
+}
 
 bool same_key(const BMD& x, const BMD& y) {
   return x.dt == y.dt && x.temp == y.temp && x.timecon == y.timecon && x.press == y.press && x.nsteps == y.nsteps &&
@@ -380,6 +383,23 @@ mm_status mm_batch_md(mm_batch* b, int nsteps, double timestep, int thermo, doub
 mm_status mm_batch_relax(mm_batch* b, int max_iter, double gtol, void* stream) {
   if (!b || max_iter < 0 || !(gtol > 0.0)) return MM_ERR_ARG;
   launch_relax(b, max_iter, gtol, (cudaStream_t)stream);
+  BCUDA(cudaGetLastError());
+  return MM_OK;
+}
+
+mm_status mm_batch_relax_cell(mm_batch* b, int max_iter, double gtol, double stol, double press, int full,
+                              void* stream) {
+  if (!b || max_iter < 0 || !(gtol > 0.0) || !(stol > 0.0) || !(press == press) || (full != 0 && full != 1)) {
+    mm::set_error("mm_batch_relax_cell: bad argument");
+    return MM_ERR_ARG;
+  }
+  CellRelax r;
+  r.max_iter = max_iter;
+  r.gtol = gtol;
+  r.stol = stol;
+  r.press = press;
+  r.full = full;
+  launch_relax_cell(b, r, (cudaStream_t)stream);
   BCUDA(cudaGetLastError());
   return MM_OK;
 }

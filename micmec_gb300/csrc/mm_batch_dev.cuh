@@ -73,6 +73,13 @@ struct BatchLaunch {
 };
 void launch_md(const BatchLaunch& L, const BMD& p, cudaStream_t st);                     // mm_batch_md.cu
 void launch_relax(const BatchLaunch& L, int max_iter, double gtol, cudaStream_t st);    // mm_batch_relax.cu
+// Relaxation of positions and domain (k_batch_relax_cell).
+struct CellRelax {
+  int max_iter;
+  double gtol, stol, press;
+  int full;  // 1: FullCellDOF, 0: StrainCellDOF
+};
+void launch_relax_cell(const BatchLaunch& L, const CellRelax& r, cudaStream_t st);       // mm_batch_relax_cell.cu
 // MD launch of one (cell precision, model) pair: each is instantiated in its own
 // translation unit (mm_batch_md_<precision><model>.cu) so that they compile in parallel.
 template <typename T, int MODEL>
@@ -777,6 +784,321 @@ __global__ void __launch_bounds__(BT) k_batch_relax(BArgs a, int max_iter, doubl
       __syncthreads();
     }
     if (threadIdx.x == 0) c[C_ITER] = it;
+    __syncthreads();
+    for (int i = threadIdx.x; i < C_LEN; i += blockDim.x) a.ctl[(size_t)b * C_LEN + i] = sh.ctl[i];
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------ relaxation with cell DOFs
+// Positions and domain together, as the reference's BaseCellDOF does (dof.py:199-470):
+// x = (cell variables, fractional coordinates). StrainCellDOF (dof.py:522-697): six
+// variables [A00, A11, A22, 2 A12, 2 A20, 2 A01] of a symmetric A, rvecs = A rvecs0;
+// FullCellDOF (dof.py:492-519): the nine components of rvecs / V0^(1/3). The gradient is
+// (J^T grvecs, gpos rvecs^T) with grvecs = gvecs (vtens + P V I) (dof.py:370-384; the
+// pressure term is ForcePartPressure's E = P V). Polak-Ribiere+ CG with the secant line
+// search of k_batch_relax along the joint direction; converged when the largest node
+// gradient is below gtol and the largest residual stress component |vtens / V + P I| is
+// below stol. Fractional displacements w (pos = (grid fraction + w) rvecs) are the
+// position variables; u = w rvecs is rebuilt at every evaluation.
+__device__ inline void inv3(const double* m, double* r) {
+  const double c00 = m[4] * m[8] - m[5] * m[7], c01 = m[5] * m[6] - m[3] * m[8], c02 = m[3] * m[7] - m[4] * m[6];
+  const double id = 1.0 / (m[0] * c00 + m[1] * c01 + m[2] * c02);
+  r[0] = c00 * id;
+  r[1] = (m[2] * m[7] - m[1] * m[8]) * id;
+  r[2] = (m[1] * m[5] - m[2] * m[4]) * id;
+  r[3] = c01 * id;
+  r[4] = (m[0] * m[8] - m[2] * m[6]) * id;
+  r[5] = (m[2] * m[3] - m[0] * m[5]) * id;
+  r[6] = c02 * id;
+  r[7] = (m[1] * m[6] - m[0] * m[7]) * id;
+  r[8] = (m[0] * m[4] - m[1] * m[3]) * id;
+}
+
+// rvecs from the cell variables (thread 0)
+__device__ inline void cell_to_rvecs(const double* xc, const double* rv0, double scale, int full, double* rv) {
+  if (full) {
+    for (int i = 0; i < 9; ++i) rv[i] = xc[i] * scale;
+  } else {
+    const double A[9] = {xc[0], 0.5 * xc[5], 0.5 * xc[4], 0.5 * xc[5], xc[1], 0.5 * xc[3],
+                         0.5 * xc[4], 0.5 * xc[3], xc[2]};
+    matmul3(A, rv0, rv);
+  }
+}
+
+// gradient of the cell variables from grvecs (thread 0): J^T grvecs
+__device__ inline void cell_gradient(const double* grv, const double* rv0, double scale, int full, double* gx) {
+  if (full) {
+    for (int i = 0; i < 9; ++i) gx[i] = grv[i] * scale;
+  } else {
+    double gA[9];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        gA[i * 3 + j] = grv[i * 3] * rv0[j * 3] + grv[i * 3 + 1] * rv0[j * 3 + 1] + grv[i * 3 + 2] * rv0[j * 3 + 2];
+    gx[0] = gA[0];
+    gx[1] = gA[4];
+    gx[2] = gA[8];
+    gx[3] = 0.5 * (gA[5] + gA[7]);
+    gx[4] = 0.5 * (gA[6] + gA[2]);
+    gx[5] = 0.5 * (gA[1] + gA[3]);
+  }
+}
+
+struct CellShared {
+  double rv0[9], rv[9], xc0[9], dc[9], gc[9], gco[9];
+  double scale;
+  double s, gg, gmax;  // reduction results of the last evaluation
+  double alpha, beta;
+  int mode, done, ncv;
+};
+
+// One evaluation at x0 + alpha d: domain, displacements, forces, gradients in x space
+// (node part written over gpos), node max |gpos|^2, g.d and g.g (cell parts included).
+template <typename T, int MODEL, int BT>
+__device__ __noinline__ void cell_eval(const BArgs& a, Shared<T>& sh, CellShared& cs, const BSys& sy, const CellRelax& r,
+                          double alpha, double* gm) {
+  double* c = sh.ctl;
+  const long long N3 = a.Ntot;
+  if (threadIdx.x == 0) {
+    double xc[9];
+    for (int i = 0; i < cs.ncv; ++i) xc[i] = cs.xc0[i] + alpha * cs.dc[i];
+    cell_to_rvecs(xc, cs.rv0, cs.scale, r.full, cs.rv);
+    const int n[3] = {sy.nx, sy.ny, sy.nz};
+    for (int d = 0; d < 3; ++d)
+      for (int x = 0; x < 3; ++x) {
+        c[C_RV + 3 * d + x] = cs.rv[3 * d + x];
+        c[C_L + 3 * d + x] = cs.rv[3 * d + x] / n[d];
+      }
+    const double* q = cs.rv;
+    c[C_VOL] = fabs(q[0] * (q[4] * q[8] - q[5] * q[7]) + q[1] * (q[5] * q[6] - q[3] * q[8]) +
+                    q[2] * (q[3] * q[7] - q[4] * q[6]));
+  }
+  __syncthreads();
+  refresh_B<T>(sh, a.tt, a.ntypes, c + C_L);
+  T* disp = (T*)a.disp;
+  for (int n = threadIdx.x; n < sy.M; n += blockDim.x) {
+    const long long g = sy.off + n;
+    double w[3];
+    for (int x = 0; x < 3; ++x) w[x] = a.cgu[x * N3 + g] + alpha * a.cgd[x * N3 + g];
+    for (int x = 0; x < 3; ++x) {
+      const double ux = w[0] * cs.rv[x] + w[1] * cs.rv[3 + x] + w[2] * cs.rv[6 + x];
+      a.u[x * N3 + g] = ux;
+      disp[x * N3 + g] = from_double<T>(ux);
+    }
+  }
+  __syncthreads();
+  forces<T, MODEL>(a, sh, sy);
+  // node gradient in fractional coordinates gw = gpos rvecs^T, with max |gpos|^2, gw.d, gw.gw
+  double acc[2] = {0.0, 0.0};
+  double gmx = 0.0;
+  for (int n = threadIdx.x; n < sy.M; n += blockDim.x) {
+    const long long g = sy.off + n;
+    const double gp[3] = {a.gpos[g], a.gpos[N3 + g], a.gpos[2 * N3 + g]};
+    gmx = fmax(gmx, gp[0] * gp[0] + gp[1] * gp[1] + gp[2] * gp[2]);
+    for (int i = 0; i < 3; ++i) {
+      const double gw = gp[0] * cs.rv[3 * i] + gp[1] * cs.rv[3 * i + 1] + gp[2] * cs.rv[3 * i + 2];
+      a.gpos[i * N3 + g] = gw;
+      acc[0] += gw * a.cgd[i * N3 + g];
+      acc[1] += gw * gw;
+    }
+  }
+  gm[threadIdx.x] = gmx;
+  block_sum<2>(acc, sh.red);
+  for (int off = BT / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off) gm[threadIdx.x] = fmax(gm[threadIdx.x], gm[threadIdx.x + off]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    // cell gradient: grvecs = gvecs (vtens + P V I), gvecs = rvecs^-T
+    double vt[9], inv[9], gv[9], grv[9];
+    double smax = 0.0;
+    for (int i = 0; i < 9; ++i) {
+      vt[i] = c[C_VT + i] + ((i % 4 == 0) ? r.press * c[C_VOL] : 0.0);
+      smax = fmax(smax, fabs(vt[i]) / c[C_VOL]);
+    }
+    inv3(cs.rv, inv);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) gv[i * 3 + j] = inv[j * 3 + i];
+    matmul3(gv, vt, grv);
+    cell_gradient(grv, cs.rv0, cs.scale, r.full, cs.gc);
+    double sd = acc[0], g2 = acc[1];
+    for (int i = 0; i < cs.ncv; ++i) {
+      sd += cs.gc[i] * cs.dc[i];
+      g2 += cs.gc[i] * cs.gc[i];
+    }
+    cs.s = sd;
+    cs.gg = g2;
+    cs.gmax = sqrt(gm[0]);
+    c[C_GMAX] = cs.gmax;
+    c[C_SRES] = smax;
+  }
+  __syncthreads();
+}
+
+template <typename T, int MODEL, int BT>
+__global__ void __launch_bounds__(BT) k_batch_relax_cell(BArgs a, CellRelax r) {
+  __shared__ Shared<T> sh;
+  __shared__ CellShared cs;
+  __shared__ double gm[BT];
+  const long long N3 = a.Ntot;
+  for (int w = a.work_off[blockIdx.x]; w < a.work_off[blockIdx.x + 1]; ++w) {
+    const int b = a.work[w];
+    const BSys sy = a.sys[b];
+    for (int i = threadIdx.x; i < C_LEN; i += blockDim.x) sh.ctl[i] = a.ctl[(size_t)b * C_LEN + i];
+    __syncthreads();
+    double* c = sh.ctl;
+    load_tables<T>(sh, a.tt, a.ntypes, c + C_L);
+    if (threadIdx.x == 0) {
+      for (int i = 0; i < 9; ++i) cs.rv0[i] = c[C_RV + i];
+      cs.scale = cbrt(c[C_VOL]);
+      cs.ncv = r.full ? 9 : 6;
+      if (r.full) {
+        for (int i = 0; i < 9; ++i) cs.xc0[i] = cs.rv0[i] / cs.scale;
+      } else {
+        const double x0[6] = {1.0, 1.0, 1.0, 0.0, 0.0, 0.0};
+        for (int i = 0; i < 6; ++i) cs.xc0[i] = x0[i];
+      }
+      for (int i = 0; i < 9; ++i) cs.dc[i] = 0.0;
+      inv3(cs.rv0, sh.mat);
+      cs.done = 0;
+      if (!(c[C_ALPHA] > 0.0)) c[C_ALPHA] = 1e-3;
+    }
+    __syncthreads();
+    // fractional displacements w = u rvecs^-1 (saved point), zero direction
+    for (int n = threadIdx.x; n < sy.M; n += blockDim.x) {
+      const long long g = sy.off + n;
+      const double u[3] = {a.u[g], a.u[N3 + g], a.u[2 * N3 + g]};
+      for (int x = 0; x < 3; ++x) {
+        a.cgu[x * N3 + g] = u[0] * sh.mat[x] + u[1] * sh.mat[3 + x] + u[2] * sh.mat[6 + x];
+        a.cgd[x * N3 + g] = 0.0;
+      }
+    }
+    __syncthreads();
+    cell_eval<T, MODEL, BT>(a, sh, cs, sy, r, 0.0, gm);
+    // d = -g
+    for (int n = threadIdx.x; n < sy.M; n += blockDim.x)
+      for (int x = 0; x < 3; ++x) a.cgd[x * N3 + sy.off + n] = -a.gpos[x * N3 + sy.off + n];
+    if (threadIdx.x == 0) {
+      for (int i = 0; i < cs.ncv; ++i) cs.dc[i] = -cs.gc[i];
+      cs.s = -cs.gg;
+    }
+    __syncthreads();
+    int it = 0;
+    for (; it < r.max_iter; ++it) {
+      if (threadIdx.x == 0) cs.done = (cs.gmax < r.gtol && c[C_SRES] < r.stol) ? 1 : 0;
+      __syncthreads();
+      if (cs.done) break;
+      if (cs.s >= 0.0) {  // not a descent direction: steepest descent
+        for (int n = threadIdx.x; n < sy.M; n += blockDim.x)
+          for (int x = 0; x < 3; ++x) a.cgd[x * N3 + sy.off + n] = -a.gpos[x * N3 + sy.off + n];
+        if (threadIdx.x == 0) {
+          for (int i = 0; i < cs.ncv; ++i) cs.dc[i] = -cs.gc[i];
+          cs.s = -cs.gg;
+        }
+        __syncthreads();
+      }
+      const double s0 = cs.s, e0 = c[C_EPOT] + r.press * c[C_VOL];
+      // keep the gradient at the line-search start (cgg, gco)
+      for (int n = threadIdx.x; n < sy.M; n += blockDim.x)
+        for (int x = 0; x < 3; ++x) a.cgg[x * N3 + sy.off + n] = a.gpos[x * N3 + sy.off + n];
+      if (threadIdx.x == 0)
+        for (int i = 0; i < cs.ncv; ++i) cs.gco[i] = cs.gc[i];
+      __syncthreads();
+      const double noise = (sizeof(T) == 4 ? 1e-6 : 1e-12) * fabs(e0);
+      double alpha = c[C_ALPHA];
+      bool accepted = false;
+      for (int ls = 0; ls < 16 && !accepted; ++ls) {
+        cell_eval<T, MODEL, BT>(a, sh, cs, sy, r, alpha, gm);
+        if (threadIdx.x == 0) {
+          const double s1 = cs.s, e1 = c[C_EPOT] + r.press * c[C_VOL];
+          int mode = 0;
+          double anew = alpha;
+          if (e1 > e0 + noise && s1 < 0.0) {
+            anew = 0.25 * alpha;
+          } else if (s1 >= 0.0) {
+            anew = alpha * (-s0) / (s1 - s0);
+            mode = 2;
+          } else if (fabs(s1) <= 0.5 * fabs(s0)) {
+            mode = 1;
+          } else {
+            anew = (s1 > s0) ? fmin(alpha * (-s0) / (s1 - s0), 8.0 * alpha) : 4.0 * alpha;
+          }
+          cs.alpha = anew;
+          cs.mode = mode;
+        }
+        __syncthreads();
+        if (cs.mode == 1) {
+          accepted = true;
+        } else if (cs.mode == 2) {
+          alpha = cs.alpha;
+          cell_eval<T, MODEL, BT>(a, sh, cs, sy, r, alpha, gm);
+          accepted = true;
+        } else {
+          alpha = cs.alpha;
+        }
+        __syncthreads();
+      }
+      if (!accepted) {  // restore the start point and stop
+        cell_eval<T, MODEL, BT>(a, sh, cs, sy, r, 0.0, gm);
+        break;
+      }
+      // move the saved point to the accepted one: w0 += alpha d, xc0 += alpha dc
+      for (int n = threadIdx.x; n < sy.M; n += blockDim.x)
+        for (int x = 0; x < 3; ++x) {
+          const long long g = x * N3 + sy.off + n;
+          a.cgu[g] += alpha * a.cgd[g];
+        }
+      // Polak-Ribiere+: beta = max(0, g.(g - g_old) / g_old.g_old)
+      double bb[2] = {0.0, 0.0};
+      for (int n = threadIdx.x; n < sy.M; n += blockDim.x)
+        for (int x = 0; x < 3; ++x) {
+          const long long g = x * N3 + sy.off + n;
+          bb[0] += a.gpos[g] * (a.gpos[g] - a.cgg[g]);
+          bb[1] += a.cgg[g] * a.cgg[g];
+        }
+      block_sum<2>(bb, sh.red);
+      if (threadIdx.x == 0) {
+        c[C_ALPHA] = alpha;
+        for (int i = 0; i < cs.ncv; ++i) {
+          cs.xc0[i] += alpha * cs.dc[i];
+          bb[0] += cs.gc[i] * (cs.gc[i] - cs.gco[i]);
+          bb[1] += cs.gco[i] * cs.gco[i];
+        }
+        cs.beta = fmax(0.0, bb[0] / fmax(bb[1], 1e-300));
+      }
+      __syncthreads();
+      const double beta = cs.beta;
+      double sv[1] = {0.0};
+      for (int n = threadIdx.x; n < sy.M; n += blockDim.x)
+        for (int x = 0; x < 3; ++x) {
+          const long long g = x * N3 + sy.off + n;
+          const double d = -a.gpos[g] + beta * a.cgd[g];
+          a.cgd[g] = d;
+          sv[0] += a.gpos[g] * d;
+        }
+      block_sum<1>(sv, sh.red);
+      if (threadIdx.x == 0) {
+        double sd = sv[0];
+        for (int i = 0; i < cs.ncv; ++i) {
+          cs.dc[i] = -cs.gc[i] + beta * cs.dc[i];
+          sd += cs.gc[i] * cs.dc[i];
+        }
+        cs.s = sd;
+      }
+      __syncthreads();
+    }
+    // positions gradient back to Cartesian (gpos = gw rvecs^-T) for the caller
+    if (threadIdx.x == 0) {
+      c[C_ITER] = it;
+      inv3(cs.rv, sh.mat);
+    }
+    __syncthreads();
+    for (int n = threadIdx.x; n < sy.M; n += blockDim.x) {
+      const long long g = sy.off + n;
+      const double gw[3] = {a.gpos[g], a.gpos[N3 + g], a.gpos[2 * N3 + g]};
+      for (int x = 0; x < 3; ++x)
+        a.gpos[x * N3 + g] = gw[0] * sh.mat[x * 3] + gw[1] * sh.mat[x * 3 + 1] + gw[2] * sh.mat[x * 3 + 2];
+    }
     __syncthreads();
     for (int i = threadIdx.x; i < C_LEN; i += blockDim.x) a.ctl[(size_t)b * C_LEN + i] = sh.ctl[i];
     __syncthreads();

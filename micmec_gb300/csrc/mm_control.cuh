@@ -39,6 +39,7 @@ enum {
   C_BTAU = 66,        // Langevin barostat: time constant
   C_BTEMP = 67,       // Langevin barostat: temperature
   C_SAVE = 68,        // scratch of the hook bookkeeping (energy before a hook call)
+  C_SRES = 69,        // cell relaxation: largest residual stress component
   C_LEN = 72
 };
 // thermostat / barostat kinds

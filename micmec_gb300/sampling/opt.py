@@ -75,9 +75,76 @@ class CGOptimizer(BaseOptimizer):
 
     log_name = "CGOPT"
 
-    def __init__(self, dof, state=None, hooks=None, counter0=0, max_line=8):
+    def __init__(self, dof, state=None, hooks=None, counter0=0, max_line=8, device=False):
         self.max_line = max_line
+        self.device = device
         BaseOptimizer.__init__(self, dof, state, hooks, counter0)
+
+    # ------------------------------------------------------------ device route
+    def _device_kind(self):
+        """None (positions), "strain" or "full" when the batched device relaxation applies, else False.
+
+        It applies to a force field of one ``ForcePartMechanical`` (plus optionally one
+        ``ForcePartPressure``) on a full periodic lattice, with a CartesianDOF without
+        selection, or a StrainCellDOF / FullCellDOF without freemask or frozen positions."""
+        from micmec_gb300.pes.mmff import ForcePartMechanical, ForcePartPressure
+        from micmec_gb300.sampling.dof import CartesianDOF, FullCellDOF, StrainCellDOF
+
+        if not self.device:
+            return False
+        parts = getattr(self.mmf, "parts", [])
+        mech = [p for p in parts if isinstance(p, ForcePartMechanical)]
+        if len(mech) != 1 or any(not isinstance(p, (ForcePartMechanical, ForcePartPressure)) for p in parts):
+            return False
+        if sum(isinstance(p, ForcePartPressure) for p in parts) > 1:
+            return False
+        s, part = self.mmf.system, mech[0]
+        grid = np.asarray(s.grid)
+        if not part.pbc or (grid == 0).any() or s.nnodes != grid.size:
+            return False
+        dof = self.dof
+        if type(dof) is CartesianDOF and dof.select is None:
+            return None
+        if type(dof) in (StrainCellDOF, FullCellDOF) and dof.freemask is None and not dof.do_frozen:
+            return "strain" if type(dof) is StrainCellDOF else "full"
+        return False
+
+    def run(self, nsteps=None):
+        kind = self._device_kind() if nsteps is not None else False
+        if kind is False:
+            return BaseOptimizer.run(self, nsteps)
+        return self._run_device(int(nsteps), kind)
+
+    def _run_device(self, nsteps, kind):
+        """All iterations in the batched CG kernel (mm_batch_relax / mm_batch_relax_cell). The
+        convergence test is the kernel's: max |gpos| below 3 gpos_rms (the DOF's gpos_max
+        criterion, dof.py:155-193) and, for cell DOFs, the residual stress below the stress
+        that the grvecs_rms threshold allows on this domain."""
+        from micmec_gb300.batch import BatchSystems
+        from micmec_gb300.pes.mmff import ForcePartMechanical, ForcePartPressure
+
+        s = self.mmf.system
+        part = [p for p in self.mmf.parts if isinstance(p, ForcePartMechanical)][0]
+        press = sum(p.pext for p in self.mmf.parts if isinstance(p, ForcePartPressure))
+        b = BatchSystems([s], model=part.model, precision=part.precision)
+        b.set_state([s.pos], None, [s.domain.rvecs])
+        gtol = 3.0 * self.dof.th_gpos_rms
+        if kind is None:
+            gmax, iters = b.relax(max_iter=nsteps, gtol=gtol)
+        else:
+            rv = np.asarray(s.domain.rvecs)
+            stol = self.dof.th_grvecs_rms * np.linalg.norm(rv, axis=1).max() / s.domain.volume
+            gmax, iters = b.relax(max_iter=nsteps, gtol=gtol, cell=kind, press=press, stress_tol=stol)
+        pos, _, rvecs = b.get_state()
+        if kind is not None:
+            self.mmf.update_rvecs(rvecs[0])
+        self.mmf.update_pos(pos[0])
+        self.counter += int(iters[0])
+        self.epot = self.mmf.compute()
+        self.dof.converged = bool(iters[0] < nsteps)
+        self.call_hooks()
+        self.finalize()
+        return self.dof.converged
 
     def initialize(self):
         self.x = self.dof.x0.copy()

@@ -39,7 +39,7 @@ from micmec.sampling.verlet import VerletIntegrator  # noqa: E402
 from micmec.sampling.iterative import Hook  # noqa: E402
 from micmec.sampling.nvt import BerendsenThermostat, CSVRThermostat, LangevinThermostat, NHCThermostat  # noqa: E402
 from micmec.sampling.npt import BerendsenBarostat, LangevinBarostat, MTKBarostat, TBCombination  # noqa: E402
-from micmec.sampling.dof import CartesianDOF  # noqa: E402
+from micmec.sampling.dof import CartesianDOF, FullCellDOF, StrainCellDOF  # noqa: E402
 from micmec.sampling.opt import QNOptimizer  # noqa: E402
 from micmec import utils as rutils  # noqa: E402
 
@@ -419,8 +419,33 @@ def make_opt_fixture():
     save("opt_qn_nanocell", **arrays)
 
 
+def make_cell_opt_fixtures():
+    """Relaxation of positions and domain (StrainCellDOF / FullCellDOF with QNOptimizer,
+    opt.py:258-443, dof.py:199-697) to a tight tolerance: the minimum a device relaxation
+    must reach."""
+    set_model("nanocell")
+    for tag, cls in (("strain", StrainCellDOF), ("full", FullCellDOF)):
+        s = synthetic_system(3, 2, 23, 0.1, 0.3)
+        arrays = system_arrays(s, prefix="sys/")
+        ff = MicMecForceField(s, [ForcePartMechanical(s)])
+        dof = cls(ff, gpos_rms=1e-8, dpos_rms=1e-6, grvecs_rms=1e-8, drvecs_rms=1e-6)
+        opt = QNOptimizer(dof)
+        opt.run(2000)
+        gpos = np.zeros(s.pos.shape)
+        vtens = np.zeros((3, 3))
+        arrays["epot_end"] = np.array(ff.compute(gpos, vtens))
+        arrays["vtens_end"] = vtens
+        arrays["gpos_end"] = gpos
+        arrays["pos_end"] = s.pos.copy()
+        arrays["rvecs_end"] = s.domain.rvecs.copy()
+        arrays["converged"] = np.array(bool(dof.converged))
+        arrays["iterations"] = np.array(opt.counter)
+        arrays["model"] = np.array("nanocell")
+        save("opt_cell_%s_nanocell" % tag, **arrays)
+
+
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["forces", "builder", "md", "hooks", "opt"]
+    which = sys.argv[1:] or ["forces", "builder", "md", "hooks", "opt", "cellopt"]
     if "forces" in which:
         make_force_fixtures()
     if "builder" in which:
@@ -431,3 +456,5 @@ if __name__ == "__main__":
         make_hook_fixtures()
     if "opt" in which:
         make_opt_fixture()
+    if "cellopt" in which:
+        make_cell_opt_fixtures()

@@ -190,3 +190,51 @@ def test_autotune_and_graph_replay_keep_results():
         got = b.md(20, record=True, use_graph=use_graph)
         for col in (REC["epot"], REC["ekin"]):
             assert np.abs(got[:, :, col] - ref[:, :, col]).max() <= 1e-6 * np.abs(ref[:, :, col]).max()
+
+
+@pytest.mark.parametrize("kind", ["strain", "full"])
+def test_batch_cell_relax_reaches_reference_minimum(kind):
+    """Positions and domain relaxed together (StrainCellDOF / FullCellDOF) reach the minimum
+    the reference's QNOptimizer found from the same start (energy, domain metric, stress)."""
+    g, b = _golden_batch("opt_cell_%s_nanocell" % kind, copies=2)
+    d = system_dict(g, "sys/")
+    b.set_state([d["pos"]] * 2, None, [d["rvecs"]] * 2)
+    gmax, iters = b.relax(max_iter=3000, gtol=1e-7, cell=kind, stress_tol=1e-11)
+    assert (gmax < 1e-7).all() and (b.residual_stress() < 1e-11).all(), (gmax, iters)
+    E = b.energies()
+    assert np.abs(E - float(g["epot_end"])).max() <= 1e-10 * abs(float(g["epot_end"]))
+    _, _, rv = b.get_state()
+    ref = g["rvecs_end"]
+    for r in rv:
+        if kind == "strain":
+            assert np.abs(r - ref).max() <= 1e-6 * np.abs(ref).max()
+        else:  # a rigid rotation of the domain is a zero mode: compare the metric
+            assert np.abs(r @ r.T - ref @ ref.T).max() <= 2e-6 * np.abs(ref @ ref.T).max()
+
+
+def test_batch_cell_relax_under_pressure_and_fp32():
+    """At 1 GPa the relaxed domain shrinks and the residual stress vtens / V + P I vanishes;
+    FP32 cells reach the FP64 minimum to the FP32 force resolution."""
+    from micmec_gb300 import units
+    from micmec_gb300.batch import CTL
+
+    P = 1e9 * units.pascal
+    out = {}
+    for prec in ("fp64", "fp32"):
+        systems, b = _mixed_batch([3, 4, 5], prec, seed=8, sigma=0.05)
+        vol0 = b.control()[:, CTL["volume"]].copy()
+        gmax, iters = b.relax(max_iter=4000, gtol=1e-6 if prec == "fp64" else 1e-4, cell="strain", press=P,
+                              stress_tol=1e-10 if prec == "fp64" else 1e-8)
+        c = b.control()
+        out[prec] = (c[:, CTL["epot"]] + P * c[:, CTL["volume"]], c[:, CTL["volume"]])
+        if prec == "fp64":
+            assert (gmax < 1e-6).all(), (gmax, iters)
+            assert (b.residual_stress() < 1e-10).all()
+            assert (c[:, CTL["volume"]] < vol0).all()
+            for i in range(len(systems)):
+                vt = c[i, CTL["vtens"]].reshape(3, 3) / c[i, CTL["volume"]] + P * np.eye(3)
+                assert np.abs(vt).max() < 1e-10
+    h64, v64 = out["fp64"]
+    h32, v32 = out["fp32"]
+    assert np.abs(h32 - h64).max() <= 1e-5 * np.abs(h64).max()
+    assert np.abs(v32 / v64 - 1).max() < 1e-4

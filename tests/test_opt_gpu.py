@@ -58,3 +58,41 @@ def test_strain_cell_dof_gradient():
     for cls in (StrainCellDOF, FullCellDOF):
         dof = cls(ff)
         assert dof.check_delta(eps=1e-6) < 1e-3
+
+
+@pytest.mark.parametrize("kind", ["strain", "full", "host-strain"])
+def test_cell_relaxation_reaches_reference_minimum(kind):
+    """CGOptimizer with StrainCellDOF / FullCellDOF: on the device (batched cell-relaxation
+    kernel) and on the host (GPU forces) it reaches the minimum of the reference's
+    QNOptimizer run from the same start."""
+    from micmec_gb300.sampling.dof import FullCellDOF, StrainCellDOF
+    from micmec_gb300.sampling.opt import CGOptimizer
+
+    tag = "full" if kind == "full" else "strain"
+    g = load_golden("opt_cell_%s_nanocell" % tag)
+    s, ff = _ff(g)
+    cls = FullCellDOF if tag == "full" else StrainCellDOF
+    dof = cls(ff, gpos_rms=1e-8, dpos_rms=1e-6, grvecs_rms=1e-8, drvecs_rms=1e-6)
+    opt = CGOptimizer(dof, device=not kind.startswith("host"))
+    if opt.device:
+        assert opt._device_kind() == tag
+    opt.run(3000)
+    e = ff.compute()
+    assert abs(e - float(g["epot_end"])) <= 1e-9 * abs(float(g["epot_end"]))
+    rv, ref = np.asarray(s.domain.rvecs), g["rvecs_end"]
+    assert np.abs(rv @ rv.T - ref @ ref.T).max() <= 1e-5 * np.abs(ref @ ref.T).max()
+
+
+def test_device_cg_positions_reach_reference_minimum():
+    from micmec_gb300.sampling.dof import CartesianDOF
+    from micmec_gb300.sampling.opt import CGOptimizer
+
+    g = load_golden("opt_qn_nanocell")
+    s, ff = _ff(g)
+    opt = CGOptimizer(CartesianDOF(ff, gpos_rms=1e-7, dpos_rms=1e-5), device=True)
+    assert opt._device_kind() is None
+    opt.run(2000)
+    assert opt.dof.converged
+    e = ff.compute()
+    assert e <= g["energies"][-1] + 1e-9 * abs(g["energies"][-1])
+    assert np.abs(s.pos - g["pos_end"]).max() < 1e-3
