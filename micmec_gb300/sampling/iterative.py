@@ -162,6 +162,9 @@ class Hook(object):
     name = None
     kind = None
     method = None
+    # False for hooks that only read the iterative's state (writers, logs): the device MD
+    # paths then run the next steps while such a hook runs on a snapshot
+    modifies_state = True
 
     def __init__(self, start=0, step=1):
         self.start = start

@@ -412,20 +412,35 @@ class VerletIntegrator(Iterative):
             self._run_device(int(nsteps), plan)
         self.finalize()
 
-    def _next_hook_gap(self, remaining):
+    def _next_hook_gap(self, remaining, counter=None):
+        counter = self.counter if counter is None else counter
         gap = remaining
         for hook in self.hooks:
             if isinstance(hook, VerletHook) or (isinstance(hook, VerletScreenLog) and not hook.verbose):
                 continue
-            c = self.counter + 1
+            c = counter + 1
             if c < hook.start:
                 c = hook.start
             else:
                 c = c + (-(c - hook.start)) % hook.step
-            gap = min(gap, c - self.counter)
+            gap = min(gap, c - counter)
         return max(1, min(gap, self.chunk))
 
+    def _hooks_read_only(self, counter):
+        """True when every hook due at ``counter`` only reads the state."""
+        return all(isinstance(h, VerletHook) or not h.modifies_state or not h.expects_call(counter)
+                   for h in self.hooks)
+
     def _run_device(self, nsteps, thermo):
+        """NVE / Langevin steps in ``mm_md_run`` chunks that end where a regular hook is due.
+
+        The state stays on the device. After each chunk the positions, velocities and
+        per-step records are copied into pinned host buffers (two slots, alternating); when
+        every hook due at the chunk's end only reads the state (writers, logs), the next
+        chunk is launched before the host processes the records and runs the hooks on the
+        snapshot, so the GPU keeps stepping while they write. A hook that may change the
+        state runs before the next launch, and its changes to ``pos`` / ``vel`` are uploaded.
+        """
         import torch
 
         from micmec_gb300 import _native as nat
@@ -437,42 +452,72 @@ class VerletIntegrator(Iterative):
         kind, temp, timecon = 0, 0.0, 1.0
         if thermo is not None:
             kind, temp, timecon = 1, float(thermo.temp), float(thermo.timecon)
-        stream = torch.cuda.current_stream().cuda_stream
-        remaining = nsteps
-        while remaining > 0:
-            k = self._next_hook_gap(remaining)
-            rec = torch.empty((k, nat.MM_REC_LEN), dtype=torch.float64, device=dev)
+        seed = 0 if thermo is None else thermo.seed
+        stream = torch.cuda.current_stream()
+        chunks, c, rem = [], self.counter, nsteps
+        while rem > 0:
+            k = self._next_hook_gap(rem, c)
+            chunks.append((c, k))
+            c += k
+            rem -= k
+        kmax = max(k for _, k in chunks)
+        slots = [dict(rec_d=torch.empty((kmax, nat.MM_REC_LEN), dtype=torch.float64, device=dev),
+                      rec=torch.empty((kmax, nat.MM_REC_LEN), dtype=torch.float64).pin_memory(),
+                      pos=torch.empty(pos_d.shape, dtype=torch.float64).pin_memory(),
+                      vel=torch.empty(vel_d.shape, dtype=torch.float64).pin_memory(),
+                      ev=torch.cuda.Event()) for _ in range(2)]
+        pending = None
+        for i, (c0, k) in enumerate(chunks):
+            sl = slots[i % 2]
             noise = None
             if thermo is not None and thermo.replay_noise is not None:
-                i0 = 2 * (self.counter - thermo.replay_offset)
+                i0 = 2 * (c0 - thermo.replay_offset)
                 noise = torch.from_numpy(np.ascontiguousarray(thermo.replay_noise[i0:i0 + 2 * k])).to(dev)
                 if noise.shape[0] != 2 * k:
                     raise ValueError("replay_noise is too short for this run")
-            seed = 0 if thermo is None else thermo.seed
             st = nat.lib().mm_md_run(fp.handle, pos_d.data_ptr(), vel_d.data_ptr(), k, float(self.timestep), kind,
-                                     temp, timecon, seed, nat.ptr(noise), rec.data_ptr(), int(self.counter), stream)
+                                     temp, timecon, seed, nat.ptr(noise), sl["rec_d"].data_ptr(), int(c0),
+                                     stream.cuda_stream)
             nat.check(st, "mm_md_run")
-            recs = rec.cpu().numpy()
-            if not np.isfinite(recs[:, :3]).all():
-                raise ValueError("The energy is not-a-number (``nan``).")
-            self.pos[:] = pos_d.cpu().numpy()
-            self.vel[:] = vel_d.cpu().numpy()
-            for i in range(k):
-                r = recs[i]
-                self.counter += 1
-                self.time += self.timestep
-                self.epot = r[nat.REC["epot"]]
-                self.ekin = r[nat.REC["ekin"]]
-                if thermo is not None:
-                    thermo.econs_correction += r[nat.REC["decons"]]
-                self.vtens = r[nat.REC["vtens"]].reshape(3, 3).copy()
-                self._finish_properties(ktens=r[nat.REC["ktens"]].reshape(3, 3))
-            self.mmf.update_pos(self.pos)
-            self.delta[:] = self.pos - self.posold
-            self.posold[:] = self.pos
-            self.rmsd_delta = np.sqrt(np.mean(self.delta**2))
-            remaining -= k
-            self.call_hooks()
+            sl["rec"][:k].copy_(sl["rec_d"][:k], non_blocking=True)
+            sl["pos"].copy_(pos_d, non_blocking=True)
+            sl["vel"].copy_(vel_d, non_blocking=True)
+            sl["ev"].record(stream)
+            if pending is not None:  # the previous chunk's hooks run while this chunk steps
+                self._finish_device_chunk(*pending, thermo)
+            pending = (sl, k)
+            if not self._hooks_read_only(c0 + k):
+                self._finish_device_chunk(sl, k, thermo)
+                pending = None
+                pos_d.copy_(torch.from_numpy(np.ascontiguousarray(self.pos)))
+                vel_d.copy_(torch.from_numpy(np.ascontiguousarray(self.vel)))
+        if pending is not None:
+            self._finish_device_chunk(*pending, thermo)
+
+    def _finish_device_chunk(self, sl, k, thermo):
+        from micmec_gb300 import _native as nat
+
+        sl["ev"].synchronize()
+        recs = sl["rec"][:k].numpy()
+        if not np.isfinite(recs[:, :3]).all():
+            raise ValueError("The energy is not-a-number (``nan``).")
+        self.pos[:] = sl["pos"].numpy()
+        self.vel[:] = sl["vel"].numpy()
+        for i in range(k):
+            r = recs[i]
+            self.counter += 1
+            self.time += self.timestep
+            self.epot = r[nat.REC["epot"]]
+            self.ekin = r[nat.REC["ekin"]]
+            if thermo is not None:
+                thermo.econs_correction += r[nat.REC["decons"]]
+            self.vtens = r[nat.REC["vtens"]].reshape(3, 3).copy()
+            self._finish_properties(ktens=r[nat.REC["ktens"]].reshape(3, 3))
+        self.mmf.update_pos(self.pos)
+        self.delta[:] = self.pos - self.posold
+        self.posold[:] = self.pos
+        self.rmsd_delta = np.sqrt(np.mean(self.delta**2))
+        self.call_hooks()
 
 
 class ConsErrTracker(object):
@@ -523,6 +568,8 @@ class VerletHook(Hook):
 
 class VerletScreenLog(Hook):
     """Screen logger (silent unless ``verbose``)."""
+
+    modifies_state = False
 
     def __init__(self, start=0, step=1, verbose=False):
         Hook.__init__(self, start, step)

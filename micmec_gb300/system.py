@@ -1,8 +1,9 @@
 """``System``: a micromechanical system (nodes, cells, types, domain).
 
-Same constructor, attributes and CHK I/O as the reference's ``System``
-(micmec/system.py:38-316). HDF5 and XYZ output are left out: they need h5py /
-molmod, which are not part of this build.
+Same constructor, attributes and file I/O as the reference's ``System``
+(micmec/system.py:38-370): CHK text files, "HDF5" system groups (through any
+``h5py.File``-like object; ``.h5`` file names use ``micmec_gb300.h5lite``, a NumPy-archive
+stand-in for h5py, which is not installed) and XYZ snapshots.
 """
 
 import numpy as np
@@ -36,7 +37,12 @@ class System(object):
 
     @classmethod
     def from_file(cls, fn, **user_kwargs):
-        """Construct a system from a CHK file (micmec/system.py:213-259)."""
+        """Construct a system from a CHK or .h5 file (micmec/system.py:213-259)."""
+        if fn.endswith(".h5"):
+            from micmec_gb300 import h5lite
+
+            with h5lite.File(fn, "r") as f:
+                return cls.from_hdf5(f, **user_kwargs)
         if not fn.endswith(".chk"):
             raise IOError('Cannot read from file "%s".' % fn)
         allowed = ["pos", "masses", "rvecs", "surrounding_cells", "surrounding_nodes", "boundary_nodes", "grid",
@@ -59,8 +65,57 @@ class System(object):
         kw["params"] = {k: v for k, v in data.items() if "/" in k}
         return cls(**kw)
 
+    @classmethod
+    def from_hdf5(cls, f, **user_kwargs):
+        """Construct a system from the ``system`` group of an h5py-like file (micmec/system.py:383-420)."""
+        sgrp = f["system"]
+        kwargs = {}
+        for key in ("pos", "masses", "rvecs", "surrounding_cells", "surrounding_nodes", "boundary_nodes", "grid",
+                    "types"):
+            if key in sgrp:
+                kwargs[key] = np.asarray(sgrp[key][:])
+        params = {}
+        if "params" in sgrp:
+            for name, item in sgrp["params"].items():
+                for key, ds in item.items():
+                    params["%s/%s" % (name, key)] = np.asarray(ds[()]) if len(ds.shape) else ds[()]
+        kwargs["params"] = params
+        kwargs.update(user_kwargs)
+        return cls(**kwargs)
+
+    def to_hdf5(self, f):
+        """Write the system to the ``system`` group of an h5py-like file (micmec/system.py:352-370);
+        the topology, domain and parameters are written too, so that ``from_hdf5`` restores it."""
+        if "system" in f:
+            raise ValueError("The HDF5 file already contains a system description.")
+        sgrp = f.create_group("system")
+        sgrp.create_dataset("pos", data=self.pos)
+        if self.masses is not None:
+            sgrp.create_dataset("masses", data=self.masses)
+        sgrp.create_dataset("rvecs", data=self.domain.rvecs)
+        sgrp.create_dataset("surrounding_cells", data=self.surrounding_cells)
+        sgrp.create_dataset("surrounding_nodes", data=self.surrounding_nodes)
+        for key in ("boundary_nodes", "grid", "types"):
+            value = getattr(self, key)
+            if value is not None:
+                sgrp.create_dataset(key, data=np.asarray(value))
+        for key, value in (self.params or {}).items():
+            sgrp.create_dataset("params/" + key, data=np.asarray(value))
+
     def to_file(self, fn):
-        """Write the system to a CHK file."""
+        """Write the system to a CHK, .h5 or XYZ file (micmec/system.py:298-350)."""
+        if fn.endswith(".h5"):
+            from micmec_gb300 import h5lite
+
+            with h5lite.File(fn, "w") as f:
+                self.to_hdf5(f)
+            return
+        if fn.endswith(".xyz"):
+            from micmec_gb300.sampling.trajectory import write_xyz_frame
+
+            with open(fn, "w") as fh:
+                write_xyz_frame(fh, str(self), self.pos)
+            return
         if not fn.endswith(".chk"):
             raise NotImplementedError("The extension of %s does not correspond to any known format." % fn)
         output = {

@@ -46,8 +46,8 @@ def _host_steps(fp, pos, vel, nsteps, thermo, pinned, seed=11):
     for i in range(nsteps):
         nat.check(nat.lib().mm_md_step_host(fp.handle, ptrs[0], ptrs[1], ptrs[2], ptrs[3], dt, thermo, temp, tau,
                                             seed, 1 + i), "mm_md_step_host")
-        recs.append(np.array(arrays[3]).copy())
-    out = [np.array(a, copy=True) for a in arrays[:3]]
+        recs.append(arrays[3].numpy().copy() if pinned else arrays[3].copy())
+    out = [a.numpy().copy() if pinned else a.copy() for a in arrays[:3]]
     return out[0], out[1], out[2], np.array(recs)
 
 

@@ -359,3 +359,70 @@ def test_csvr_generator_samples_canonical_kinetic_energy():
     ek = rec[:, 1000:, REC["ekin"]].ravel()
     assert abs(ek.mean() / (0.5 * ndof * kT) - 1.0) < 0.02
     assert abs(ek.var() / (0.5 * ndof * kT ** 2) - 1.0) < 0.15
+
+
+def test_device_writers_run_on_snapshots_while_the_gpu_steps(tmp_path):
+    """Writers (read-only hooks) run on pinned snapshots while the next chunk steps; their
+    records equal those of a run whose hooks force synchronous chunks."""
+    from micmec_gb300 import h5lite, units
+    from micmec_gb300.pes.mmff import ForcePartMechanical, MicMecForceField
+    from micmec_gb300.sampling.iterative import Hook
+    from micmec_gb300.sampling.nvt import LangevinThermostat
+    from micmec_gb300.sampling.trajectory import HDF5Writer, XYZWriter
+    from micmec_gb300.sampling.verlet import VerletIntegrator
+
+    noise = np.random.default_rng(4).normal(size=(2 * 60, 6 ** 3, 3))
+
+    class Touch(Hook):  # may modify the state (the default): chunks run synchronously
+        def __call__(self, it):
+            pass
+
+    out = {}
+    for mode in ("overlap", "sync"):
+        s, vel = _lattice(6, 2, 5)
+        ff = MicMecForceField(s, [ForcePartMechanical(s, model="nanocell", precision="fp64")])
+        f = h5lite.File(str(tmp_path / ("%s.h5" % mode)), "w")
+        xyz = XYZWriter(str(tmp_path / ("%s.xyz" % mode)), step=10)
+        hooks = [LangevinThermostat(300.0, timecon=100 * units.femtosecond, replay_noise=noise),
+                 HDF5Writer(f, step=10), xyz]
+        if mode == "sync":
+            hooks.append(Touch(0, 10))
+        vi = VerletIntegrator(ff, 1.0 * units.femtosecond, hooks=hooks, vel0=vel)
+        assert vi._hooks_read_only(10) == (mode == "overlap")
+        vi.run(60)
+        f.close()
+        xyz.close()
+        with h5lite.File(str(tmp_path / ("%s.h5" % mode)), "r") as h:
+            out[mode] = {k: np.array(h["trajectory/" + k][:]) for k in ("counter", "pos", "vel", "epot", "econs")}
+        out[mode]["xyz"] = open(str(tmp_path / ("%s.xyz" % mode))).read()
+    a, b = out["overlap"], out["sync"]
+    assert list(a["counter"]) == [0, 10, 20, 30, 40, 50, 60]
+    for k in ("counter", "pos", "vel", "epot", "econs"):
+        assert np.array_equal(a[k], b[k]), k
+    assert a["xyz"] == b["xyz"]
+
+
+def test_state_changes_by_hooks_reach_the_device_path():
+    """A hook that changes the velocities between device chunks: the device path continues
+    from the changed state, as the host path does."""
+    from micmec_gb300 import units
+    from micmec_gb300.pes.mmff import ForcePartMechanical, MicMecForceField
+    from micmec_gb300.sampling.iterative import Hook
+    from micmec_gb300.sampling.verlet import VerletIntegrator
+
+    class Cool(Hook):
+        def __call__(self, it):
+            it.vel[:] *= 0.5
+
+    rows = {}
+    for device in (True, False):
+        s, vel = _lattice(5, 2, 6)
+        ff = MicMecForceField(s, [ForcePartMechanical(s, model="nanocell", precision="fp64")])
+        rec = Rec()
+        vi = VerletIntegrator(ff, 1.0 * units.femtosecond, hooks=[Cool(20, 1000), rec.hook], vel0=vel, device=device)
+        vi.run(40)
+        rows[device] = np.array(rec.rows)
+    a, b = rows[True], rows[False]
+    assert a[30, 2] < 0.6 * a[19, 2]  # the cooling took effect
+    for col in (1, 2):
+        assert np.abs(a[:, col] - b[:, col]).max() <= 1e-9 * np.abs(b[:, col]).max()
