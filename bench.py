@@ -392,7 +392,7 @@ def measure_large_mtk(n=256, nsteps=100, cmp_steps=4):
 
     rng = np.random.default_rng(SEED + 5)
     t0 = time.perf_counter()
-    d = lattices.make_lattice(lattices.defect_grid(n, 0.2, rng, clustered=True), nstates=2)
+    d = lattices.make_lattice(lattices.defect_grid(n, 0.2, rng, clustered=True), nstates=2, device=True)
     d["pos"] = lattices.displace(d["pos"], 0.02 * units.angstrom, rng)
     t_setup = time.perf_counter() - t0
     kT = units.boltzmann * 300.0
@@ -451,6 +451,50 @@ def measure_large_mtk(n=256, nsteps=100, cmp_steps=4):
     return out
 
 
+def _error_text(exc):
+    """The exception and the innermost frame that raised it (file:line), for the JSON line."""
+    import traceback
+
+    tb = traceback.extract_tb(exc.__traceback__)
+    where = "%s:%d" % (os.path.basename(tb[-1].filename), tb[-1].lineno) if tb else "?"
+    return ("%r at %s" % (exc, where))[:300]
+
+
+def measure_builder(n_cmp=128, n_large=256):
+    """System construction: the device builder (mm_build_topology, tables copied back to host
+    arrays) against the vectorised host builder on the same grid, and the device builder alone
+    at 256^3 (20% clustered defects, two types, periodic)."""
+    import torch
+
+    from micmec_gb300 import lattices
+    from micmec_gb300.utils import build_system
+
+    rng = np.random.default_rng(5)
+    data = lattices.standard_types(nstates=2)
+    build_system(data, lattices.defect_grid(8, 0.2, rng), pbc=True, device=True)  # warm-up
+    grid = lattices.defect_grid(n_cmp, 0.2, rng, clustered=True)
+    t0 = time.perf_counter()
+    host = build_system(data, grid, pbc=True)
+    t_host = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    dev = build_system(data, grid, pbc=True, device=True)
+    t_dev = time.perf_counter() - t0
+    same = all(np.array_equal(np.asarray(host[k]), np.asarray(dev[k]))
+               for k in ("surrounding_cells", "surrounding_nodes", "boundary_nodes", "types", "masses", "pos"))
+    del host, dev
+    grid = lattices.defect_grid(n_large, 0.2, rng, clustered=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    big = build_system(data, grid, pbc=True, device=True)
+    t_big = time.perf_counter() - t0
+    ncells = len(big["types"])
+    del big
+    return {"lattice_cmp": [n_cmp] * 3, "host_s": t_host, "device_s": t_dev, "identical": bool(same),
+            "lattice_large": [n_large] * 3, "device_large_s": t_big, "large_cells": ncells,
+            "note": "wall time of build_system, device tables copied back into host arrays"}
+
+
 def measure_grad_over_fwd(n=16, reps=5):
     """Cost of the adjoint (backward of a force loss) relative to the forward force evaluation, 16^3 FP64."""
     import torch
@@ -486,8 +530,9 @@ def measure_grad_over_fwd(n=16, reps=5):
     gc, gh, gd = torch.autograd.grad((w * energy_and_gradient(pos, params)[1]).sum(),
                                      [params.c21, params.h0, params.free_energy])
     errs = []
-    # C11, C12 of the second state of type 1, a diagonal entry of h0 (all nonzero)
-    for tensor, grad, idx in ((params.c21, gc, (0, 0, 0)), (params.c21, gc, (1, 1, 1)), (params.h0, gh, (0, 0, 1, 1))):
+    # C11 of type 0 and C12 of type 1 in state 0, a diagonal entry of h0 (all nonzero; the
+    # lattice sits near state 0's rest cell, where the other states' weights are below rounding)
+    for tensor, grad, idx in ((params.c21, gc, (0, 0, 0)), (params.c21, gc, (1, 0, 1)), (params.h0, gh, (0, 0, 1, 1))):
         base = float(tensor.detach()[idx])
         if base == 0.0:
             raise ValueError("finite-difference probe on a zero parameter")
@@ -703,10 +748,14 @@ def run_gpu(args):
             line["batched"] = {"fp32": bf, "fp64": bd, "plain_fp64_per_system": plain,
                                "batched_fp32_over_plain_fp64_systems_per_s":
                                    bf["systems_steps_per_s"] / plain["systems_steps_per_s"]}
-            line["adjoint"] = measure_grad_over_fwd()
-            line["large_mtk"] = measure_large_mtk()
         except Exception as exc:  # extra measurements never block the main line
-            line["extra_error"] = repr(exc)[:300]
+            line["extra_error"] = _error_text(exc)
+        for key, fn in (("builder", measure_builder), ("adjoint", measure_grad_over_fwd),
+                        ("large_mtk", measure_large_mtk)):
+            try:
+                line[key] = fn()
+            except Exception as exc:
+                line[key] = {"error": _error_text(exc)}
     if rank == 0 and not args.no_cpu_baseline:
         nproc = 1
         sample_steps = 1
@@ -730,6 +779,9 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the FP64 / batched / adjoint side measurements")
     ap.add_argument("--large-only", type=int, default=0, metavar="N",
                     help="only the large single-system NHC + MTK run (lattice engine) on an N^3 lattice")
+    ap.add_argument("--builder-only", type=int, default=0, metavar="N",
+                    help="only the device system builder on an N^3 lattice with 20%% clustered defects, built "
+                         "--warmup + --steps times (for kernel profiles)")
     ap.add_argument("--batch-only", action="store_true",
                     help="only the batched workload (512 systems, NHC + MTK, FP32 cells): one warm-up launch of "
                          "--warmup steps and one launch of --steps steps, no autotuning or graph (for kernel profiles)")
@@ -743,7 +795,29 @@ def main():
     if args.large_only:
         print(json.dumps(measure_large_mtk(n=args.large_only, nsteps=args.steps)), flush=True)
         return 0
+    if args.builder_only:
+        return run_builder_only(args)
     return run_gpu(args)
+
+
+def run_builder_only(args):
+    import torch
+
+    from micmec_gb300 import lattices
+    from micmec_gb300.utils import build_system
+
+    n = args.builder_only
+    grid = lattices.defect_grid(n, 0.2, np.random.default_rng(5), clustered=True)
+    data = lattices.standard_types(nstates=2)
+    times = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d = build_system(data, grid, pbc=True, device=True)
+        times.append(time.perf_counter() - t0)
+    print(json.dumps({"builder_lattice": [n] * 3, "cells": len(d["types"]), "nodes": len(d["masses"]),
+                      "wall_s_median": float(np.median(times[args.warmup:]))}), flush=True)
+    return 0
 
 
 def run_batch_only(args):

@@ -212,6 +212,26 @@ mm_status mm_compute_noalloc(const int32_t* lattice_shape, const int32_t* cell_t
                              const double* pos, double* gpos, double* vtens, double* energy, void* stream);
 
 /*
+ * Topology of a system from its grid of cell types, built on the device (the tables of
+ * build_system, micmec/utils.py:164-263, with the reference's orderings: cells and nodes
+ * lexicographic over grid coordinates, corner k = neighbor_nodes[k], node masses summed
+ * in increasing cell order).
+ *  grid      : device int32 (nx, ny, nz), last index fastest; 0 = vacancy, else a type id
+ *              below ntype_ids (others: MM_ERR_ARG).
+ *  pbc       : host int32[3].  type_mass : host double[ntype_ids] (index = type id).
+ *  cell_size : host double[3], node spacing along x, y, z.
+ *  Outputs (device), sized for every grid point; the first counts[0] cells and
+ *  counts[1] nodes are valid: surrounding_nodes int64 (cells, 8), surrounding_cells
+ *  int64 (nodes, 8; -1 = no cell) (both 16-byte aligned), masses double (nodes), pos double (nodes, 3),
+ *  types int32 (cells), boundary uint8 (nodes; 1 on the node grid's faces).
+ *  counts    : host int64[2] = (number of cells, number of nodes).
+ */
+mm_status mm_build_topology(const int32_t* grid, int nx, int ny, int nz, const int32_t* pbc, const double* type_mass,
+                            int ntype_ids, const double* cell_size, int64_t* surrounding_nodes,
+                            int64_t* surrounding_cells, double* masses, double* pos, int32_t* types,
+                            uint8_t* boundary, int64_t* counts, void* stream);
+
+/*
  * Batched systems: nsys independent, fully periodic lattices (every lattice site a
  * node and a cell) of uneven size, evaluated and integrated in one persistent launch
  * (one CTA runs whole systems). No single reference function corresponds: the

@@ -104,13 +104,14 @@ def defect_grid(n, fraction, rng, clustered=False):
     return grid.reshape(shape)
 
 
-def make_lattice(grid, nstates=1, pbc=True):
-    """System dict (as ``build_system``) for a type grid with the standard types."""
+def make_lattice(grid, nstates=1, pbc=True, device=False):
+    """System dict (as ``build_system``) for a type grid with the standard types
+    (``device=True``: topology built on the GPU)."""
     grid = np.asarray(grid)
     data = standard_types(nstates=nstates, with_reo=bool((grid == 2).any()))
     if 2 not in data:
         data = {1: data[1]}
-    return build_system(data, grid, pbc=pbc)
+    return build_system(data, grid, pbc=pbc, device=device)
 
 
 def displace(pos, sigma, rng):

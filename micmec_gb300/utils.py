@@ -129,9 +129,14 @@ class Grid(object):
         return idx
 
 
-def build_system(data, grid, pbc=None):
-    """Micromechanical system as a ``dict`` ready for ``dump_chk`` (micmec/utils.py:164-263)."""
+def build_system(data, grid, pbc=None, device=False):
+    """Micromechanical system as a ``dict`` ready for ``dump_chk`` (micmec/utils.py:164-263).
+
+    ``device=True`` builds the topology, masses and positions on the GPU
+    (``mm_build_topology``; the same tables, bit for bit) and copies them back."""
     grid = np.asarray(grid)
+    if device:
+        return _build_system_device(data, grid, pbc)
     g = Grid(grid, pbc=pbc)
     nodes = g.node_coords
     cells = g.cell_coords
@@ -155,9 +160,7 @@ def build_system(data, grid, pbc=None):
     # cell-major order: each node accumulates in increasing cell index
     np.add.at(masses, surrounding_nodes.ravel(), np.repeat(cell_mass, 8))
 
-    counts = np.bincount(np.array(grid.ravel(), dtype=np.int64))[1:]
-    maj = int(np.argmax(counts)) + 1
-    dx, dy, dz = np.diag(np.asarray(data[maj]["cell"][0]))
+    dx, dy, dz = _majority_cell_size(data, grid)
     pos = nodes.astype(np.float64) * np.array([dx, dy, dz])
 
     rvecs = []
@@ -179,6 +182,70 @@ def build_system(data, grid, pbc=None):
         "surrounding_nodes": surrounding_nodes,
         "boundary_nodes": g.boundary_nodes,
         "masses": masses,
+    }
+    for type_idx, type_data in data.items():
+        for key, value in type_data.items():
+            output[f"type{type_idx}/{key}"] = value
+    return output
+
+
+def _majority_cell_size(data, grid):
+    counts = np.bincount(np.array(grid.ravel(), dtype=np.int64))[1:]
+    maj = int(np.argmax(counts)) + 1
+    return np.diag(np.asarray(data[maj]["cell"][0])).astype(np.float64)
+
+
+def _build_system_device(data, grid, pbc):
+    import torch
+
+    from micmec_gb300 import _native as nat
+
+    if grid.ndim != 3 or grid.min() < 0:
+        raise ValueError("grid must be a 3-D array of type ids >= 0")
+    nx, ny, nz = grid.shape
+    flags = _pbc_list(pbc)
+    nn = [n + 1 - int(p) for n, p in zip(grid.shape, flags)]
+    ncg, nng = nx * ny * nz, nn[0] * nn[1] * nn[2]
+    ntype_ids = int(grid.max()) + 1
+    type_mass = np.zeros(ntype_ids)
+    for k, v in data.items():
+        if int(k) < ntype_ids:
+            type_mass[int(k)] = float(v["mass"])
+    dx, dy, dz = _majority_cell_size(data, grid)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    g_d = torch.from_numpy(np.ascontiguousarray(grid, dtype=np.int32)).to(dev)
+    snodes = torch.empty((ncg, 8), dtype=torch.int64, device=dev)
+    scells = torch.empty((nng, 8), dtype=torch.int64, device=dev)
+    masses = torch.empty(nng, dtype=torch.float64, device=dev)
+    pos = torch.empty((nng, 3), dtype=torch.float64, device=dev)
+    types = torch.empty(ncg, dtype=torch.int32, device=dev)
+    boundary = torch.empty(nng, dtype=torch.uint8, device=dev)
+    counts = np.zeros(2, dtype=np.int64)
+    pbc_a = np.array(flags, dtype=np.int32)
+    size = np.array([dx, dy, dz], dtype=np.float64)
+    nat.check(nat.lib().mm_build_topology(g_d.data_ptr(), nx, ny, nz, pbc_a.ctypes.data, type_mass.ctypes.data,
+                                          ntype_ids, size.ctypes.data, snodes.data_ptr(), scells.data_ptr(),
+                                          masses.data_ptr(), pos.data_ptr(), types.data_ptr(), boundary.data_ptr(),
+                                          counts.ctypes.data, torch.cuda.current_stream().cuda_stream),
+              "mm_build_topology")
+    M, N = int(counts[0]), int(counts[1])
+    rvecs = []
+    if flags[0]:
+        rvecs.append([nx * dx, 0.0, 0.0])
+    if flags[1]:
+        rvecs.append([0.0, ny * dy, 0.0])
+    if flags[2]:
+        rvecs.append([0.0, 0.0, nz * dz])
+    output = {
+        "pos": pos[:N].cpu().numpy(),
+        "rvecs": np.array(rvecs, dtype=np.float64).reshape(-1, 3),
+        "types": types[:M].cpu().numpy().astype(grid.dtype),
+        "grid": grid,
+        "pbc": flags,
+        "surrounding_cells": scells[:N].cpu().numpy(),
+        "surrounding_nodes": snodes[:M].cpu().numpy(),
+        "boundary_nodes": list(np.nonzero(boundary[:N].cpu().numpy())[0]),
+        "masses": masses[:N].cpu().numpy(),
     }
     for type_idx, type_data in data.items():
         for key, value in type_data.items():
