@@ -9,7 +9,9 @@ import os
 
 __all__ = ["lib", "check", "MMError", "LIB_PATH", "MM_REC_LEN", "REC"]
 
-LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libmicmec_gb300.so")
+# MICMEC_GB300_LIB selects another build of the library (e.g. one with different compile flags)
+LIB_PATH = os.environ.get("MICMEC_GB300_LIB") or os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib",
+                                                              "libmicmec_gb300.so")
 
 MM_OK, MM_ERR_NAN, MM_ERR_ARG, MM_ERR_CUDA, MM_ERR_TIMEOUT = range(5)
 MM_REC_LEN = 21

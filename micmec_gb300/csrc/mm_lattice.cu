@@ -264,7 +264,7 @@ constexpr int kCell8Cells = kCell8Threads / 8;
 static_assert(kCell8Threads == 256 && kCellPart == 10, "component ownership assumes 8 warps and 10 components");
 
 template <typename T, bool STRUCT, bool SIMPLE>
-__global__ void __launch_bounds__(kCell8Threads, sizeof(T) == 4 ? (SIMPLE ? 4 : 3) : 2) k_cells8(Topo t, const TypeTable* __restrict__ tt, int ntypes,
+__global__ void __launch_bounds__(kCell8Threads, sizeof(T) == 4 ? 3 : 2) k_cells8(Topo t, const TypeTable* __restrict__ tt, int ntypes,
                                                           const double* __restrict__ box, const T* __restrict__ disp,
                                                           T* __restrict__ G, double* __restrict__ ecell,
                                                           double* __restrict__ cpart) {
@@ -290,27 +290,40 @@ __global__ void __launch_bounds__(kCell8Threads, sizeof(T) == 4 ? (SIMPLE ? 4 : 
   typedef typename std::conditional<sizeof(T) == 8, double, F2>::type Acc;
   Acc acc0{}, acc1{};
   int parity = 0;
+  // software pipelining (FP32 cells): the next group's corner displacements and cell type
+  // are loaded before the current group is evaluated (FP64: no spare registers, loaded in turn)
+  constexpr bool kPrefetch = sizeof(T) == 4;
+  T du_n[3];
+  int ty_n;
+  auto load_group = [&](int gg) {
+    const int cc = gg * kCell8Cells + cl;
+    du_n[0] = du_n[1] = du_n[2] = T(0);
+    ty_n = 0;
+    if (gg < ngroups && cc < t.M) {
+      int node;
+      if (STRUCT) {
+        int i, j, k;
+        split_index(t, cc, i, j, k);
+        node = struct_corner_node(t, i, j, k, a);
+      } else {
+        node = t.cell_nodes[bits_to_corner(a) * t.M + cc];
+      }
+#pragma unroll
+      for (int x = 0; x < 3; ++x) du_n[x] = disp[x * t.N + node];
+      ty_n = t.cell_type[cc];
+    }
+  };
+  if constexpr (kPrefetch) load_group(blockIdx.x);
   for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x, parity ^= 1) {
   T* tile = buf0 + parity * kBuf;      // [24][kCell8Cells] corner gradients
   T* relt = tile + 24 * kCell8Cells;   // [24][kCell8Cells] vertex offsets r_a - r_0
   T* et = relt + 24 * kCell8Cells;     // [kCell8Cells] cell energies
   const int cell = grp * kCell8Cells + cl;
   const bool valid = cell < t.M;
-  T du[3] = {T(0), T(0), T(0)};
-  int ty = 0;
-  if (valid) {
-    int node;
-    if (STRUCT) {
-      int i, j, k;
-      split_index(t, cell, i, j, k);
-      node = struct_corner_node(t, i, j, k, a);
-    } else {
-      node = t.cell_nodes[bits_to_corner(a) * t.M + cell];
-    }
-#pragma unroll
-    for (int x = 0; x < 3; ++x) du[x] = disp[x * t.N + node];
-    ty = t.cell_type[cell];
-  }
+  if constexpr (!kPrefetch) load_group(grp);
+  T du[3] = {du_n[0], du_n[1], du_n[2]};
+  const int ty = ty_n;
+  if constexpr (kPrefetch) load_group(grp + gridDim.x);
   T g[3];
   const T Ecell = cell8_eval<T, SIMPLE>(du, a, tp[ty], valid, g);
   // stage corner gradients and vertex offsets r_a - r_0 = offset(a) . L + du_a - du_0
