@@ -17,6 +17,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 #define MM_MAX_TYPES 8
@@ -99,7 +100,8 @@ __device__ __forceinline__ void fill_type_scalars(TypeParams<T>& dst, const Type
   dst.nstates = src.nstates;
 }
 
-// Elastic energy of one state and its gradient with respect to the rows of W.
+// Elastic energy of one state (state_energy, which also returns D and the stress s) and
+// its gradient with respect to the rows of W (state_gradient, from D and s).
 // W = M - h0 (rows: edge deviations). F = M^T h0^-T = I + D with
 // D[i][k] = sum_j W[j][i] hinv[k][j]; eps = (D + D^T + D^T D)/2;
 // s = A eps; E = scale * eps:s / 2; dE/dW[j][i] = scale * sum_k (F S)[i][k] hinv[k][j].
@@ -110,9 +112,7 @@ __device__ __forceinline__ void fill_type_scalars(TypeParams<T>& dst, const Type
 // (A00 = A11 = A22, A01 = A02 = A12 and symmetric, A33 = A44 = A55, all else 0); the
 // products with h0^-1 and A then reduce to scalings (detected exactly on the host).
 template <typename T, bool SIMPLE = false, typename P = StateParams<T>>
-__device__ __forceinline__ T state_energy_grad(const T* __restrict__ W, const P& p, T scale,
-                                               T* __restrict__ GW) {
-  T D[9];
+__device__ __forceinline__ T state_energy(const T* __restrict__ W, const P& p, T scale, T (&D)[9], T (&s)[6]) {
   if constexpr (SIMPLE) {
     const T h[3] = {p.hd[0], p.hd[1], p.hd[2]};
 #pragma unroll
@@ -134,7 +134,6 @@ __device__ __forceinline__ T state_energy_grad(const T* __restrict__ W, const P&
   e[3] = h * (D[5] + D[7] + D[1] * D[2] + D[4] * D[5] + D[7] * D[8]);
   e[4] = h * (D[2] + D[6] + D[0] * D[2] + D[3] * D[5] + D[6] * D[8]);
   e[5] = h * (D[1] + D[3] + D[0] * D[1] + D[3] * D[4] + D[6] * D[7]);
-  T s[6];
   if constexpr (SIMPLE) {
     const T amb = p.cub[0], b = p.cub[1], c = p.cub[2];
     const T tr = e[0] + e[1] + e[2];
@@ -153,7 +152,14 @@ __device__ __forceinline__ T state_energy_grad(const T* __restrict__ W, const P&
     s[q] = acc;
   }
   }
-  T dens = e[0] * s[0] + e[1] * s[1] + e[2] * s[2] + T(2) * (e[3] * s[3] + e[4] * s[4] + e[5] * s[5]);
+  const T dens = e[0] * s[0] + e[1] * s[1] + e[2] * s[2] + T(2) * (e[3] * s[3] + e[4] * s[4] + e[5] * s[5]);
+  return h * scale * dens;
+}
+
+// Gradient with respect to the rows of W from the D and stress s of state_energy.
+template <typename T, bool SIMPLE = false, typename P = StateParams<T>>
+__device__ __forceinline__ void state_gradient(const T (&D)[9], const T (&s)[6], const P& p, T scale,
+                                               T* __restrict__ GW) {
   // S symmetric 3x3 from s
   const T S[9] = {s[0], s[5], s[4], s[5], s[1], s[3], s[4], s[3], s[2]};
   // GF = (I + D) S
@@ -178,7 +184,15 @@ __device__ __forceinline__ T state_energy_grad(const T* __restrict__ W, const P&
     for (int i = 0; i < 3; ++i)
       GW[j * 3 + i] = scale * (GF[i * 3 + 0] * p.hinv[0 * 3 + j] + GF[i * 3 + 1] * p.hinv[1 * 3 + j] + GF[i * 3 + 2] * p.hinv[2 * 3 + j]);
   }
-  return h * scale * dens;
+}
+
+template <typename T, bool SIMPLE = false, typename P = StateParams<T>>
+__device__ __forceinline__ T state_energy_grad(const T* __restrict__ W, const P& p, T scale,
+                                               T* __restrict__ GW) {
+  T D[9], s[6];
+  const T E = state_energy<T, SIMPLE, P>(W, p, scale, D, s);
+  state_gradient<T, SIMPLE, P>(D, s, p, scale, GW);
+  return E;
 }
 
 // Per-cell evaluation. du[b][c]: displacement of the corner with offset bits b.
@@ -545,29 +559,37 @@ __device__ __forceinline__ T cell8_eval(const T (&du)[3], int a, const TypeParam
   for (int s = 0; s < ns; ++s) {
     const bool active = s < ns_lane;
     const StateParams<T>& p = tpl.s[active ? s : 0];
-    T W[9], GW[9], Es, df;
+    T W[9], Dm[9], sv[6], Es, df;
+    const T sc = T(0.125) * p.v0;
+    struct NoView {};
+    typename std::conditional<SIMPLE && sizeof(T) == 4, CubicView<float>, NoView>::type cv;
     if constexpr (SIMPLE && sizeof(T) == 4) {
-      CubicView<float> cv;
       load_cubic(p, cv);
 #pragma unroll
       for (int d = 0; d < 3; ++d)
 #pragma unroll
         for (int x = 0; x < 3; ++x) W[d * 3 + x] = cv.B[d * 3 + x] + ed[d][x];
-      Es = state_energy_grad<T, true, CubicView<float>>(W, cv, T(0.125) * cv.v0, GW);
+      Es = state_energy<T, true, CubicView<float>>(W, cv, sc, Dm, sv);
       df = cv.df;
     } else {
 #pragma unroll
       for (int d = 0; d < 3; ++d)
 #pragma unroll
         for (int x = 0; x < 3; ++x) W[d * 3 + x] = p.B[d * 3 + x] + ed[d][x];
-      Es = state_energy_grad<T, SIMPLE>(W, p, T(0.125) * p.v0, GW);
+      Es = state_energy<T, SIMPLE>(W, p, sc, Dm, sv);
       df = p.df;
     }
     Es += __shfl_xor_sync(0xffffffffu, Es, 1);
     Es += __shfl_xor_sync(0xffffffffu, Es, 2);
     Es += __shfl_xor_sync(0xffffffffu, Es, 4);
-    if (active) {
-      const T E = Es + df;
+    const T E = Es + df;
+    // A state whose weight against the lowest energy so far is below e^-50 adds nothing
+    // representable to the weighted gradient (nor to the weight sum): its gradient is not
+    // formed. The lowest energy can only fall later, so the weight stays below e^-50.
+    if (active && (s == 0 || !(E - m >= T(50) * kT))) {
+      T GW[9];
+      if constexpr (SIMPLE && sizeof(T) == 4) state_gradient<T, true, CubicView<float>>(Dm, sv, cv, sc, GW);
+      else state_gradient<T, SIMPLE>(Dm, sv, p, sc, GW);
       if (s == 0) {
         m = E;
         wsum = T(1);
