@@ -524,16 +524,23 @@ mm_status mm_md_step_host(mm_handle* h, double* pos, double* vel, double* gpos, 
     if (s != MM_OK) return s;
   }
   mm::launch_md_host_begin(h, h->md.dt, h->md.c1, seed, step, thermo, d_pos, d_vel, d_gpos, st);
+  // the new positions are final after the drift: copy them back while the forces run
+  MM_CUDA(cudaEventRecord(h->copy_ev[0], st));
+  MM_CUDA(cudaStreamWaitEvent(h->copy_st[0], h->copy_ev[0], 0));
+  MM_CUDA(cudaMemcpyAsync(pos, d_pos, bytes, cudaMemcpyDeviceToHost, h->copy_st[0]));
+  MM_CUDA(cudaEventRecord(h->copy_ev[1], h->copy_st[0]));
   mm::launch_cells(h, st, nullptr);
   mm::launch_md_nodes(h, h->md.dt, h->md.c1, seed, step, step, 1, 0, thermo, nullptr, d_rec, d_gpos, st);
-  mm::launch_md_host_end(h, d_pos, d_vel, st);
+  mm::launch_md_host_end(h, d_vel, st);
   MM_CUDA(cudaGetLastError());
-  {
-    void* dst[3] = {pos, vel, gpos};
-    const void* src[3] = {d_pos, d_vel, d_gpos};
-    s = copy3(h, dst, src, bytes, cudaMemcpyDeviceToHost, st);
-    if (s != MM_OK) return s;
-  }
+  // velocities and gradient on two streams; the step ends when all three copies are done
+  MM_CUDA(cudaEventRecord(h->copy_ev[0], st));
+  MM_CUDA(cudaStreamWaitEvent(h->copy_st[1], h->copy_ev[0], 0));
+  MM_CUDA(cudaMemcpyAsync(gpos, d_gpos, bytes, cudaMemcpyDeviceToHost, h->copy_st[1]));
+  MM_CUDA(cudaEventRecord(h->copy_ev[2], h->copy_st[1]));
+  MM_CUDA(cudaMemcpyAsync(vel, d_vel, bytes, cudaMemcpyDeviceToHost, st));
+  MM_CUDA(cudaStreamWaitEvent(st, h->copy_ev[1], 0));
+  MM_CUDA(cudaStreamWaitEvent(st, h->copy_ev[2], 0));
   if (record) MM_CUDA(cudaMemcpyAsync(record, d_rec, MM_REC_LEN * sizeof(double), cudaMemcpyDeviceToHost, st));
   MM_CUDA(cudaStreamSynchronize(st));
   return MM_OK;

@@ -106,6 +106,6 @@ void launch_soa_to_aos(int N, const double* s, double* a, cudaStream_t st);
 void launch_md_nodes(mm_handle* h, double dt, double c1, uint64_t seed, int64_t step, int64_t noise_step0, int finish,
                      int start, int thermo, const double* noise, double* record, double* gpos_out, cudaStream_t st);
 void launch_md_host_begin(mm_handle* h, double dt, double c1, uint64_t seed, int64_t step, int thermo,
-                          const double* pos, const double* vel, const double* gpos, cudaStream_t st);
-void launch_md_host_end(mm_handle* h, double* pos, double* vel, cudaStream_t st);
+                          double* pos, const double* vel, const double* gpos, cudaStream_t st);
+void launch_md_host_end(mm_handle* h, double* vel, cudaStream_t st);
 }  // namespace mm

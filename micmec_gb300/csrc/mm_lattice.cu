@@ -797,9 +797,11 @@ __global__ void __launch_bounds__(kMDThreads, 1) k_md_nodes(Topo t, MDArgs p, co
 // Host-buffer step, first half in one pass: u = pos - X(L) and v from the caller's
 // AoS arrays, then the "pre" thermostat, kick with the caller's gradient, and drift
 // (u as k_pos_to_state forms it, then the arithmetic of the host step's first half);
-// pos / vel / gpos are the device copies of the caller's arrays.
+// pos / vel / gpos are the device copies of the caller's arrays. The step's final
+// positions X(L) + u are known after the drift: each thread writes them over its own
+// entries of pos, so their copy to the host overlaps the force evaluation.
 template <typename T, int THERMO>
-__global__ void k_md_host_begin(Topo t, MDArgs p, const double* __restrict__ pos, const double* __restrict__ vel,
+__global__ void k_md_host_begin(Topo t, MDArgs p, double* pos, const double* __restrict__ vel,
                                 const double* __restrict__ gpos, const double* __restrict__ box,
                                 double* __restrict__ u, double* __restrict__ v, T* __restrict__ disp,
                                 const double* __restrict__ invm, const double* __restrict__ c2) {
@@ -829,22 +831,17 @@ __global__ void k_md_host_begin(Topo t, MDArgs p, const double* __restrict__ pos
     u[x * t.N + n] = un;
     disp[x * t.N + n] = (T)un;
     v[x * t.N + n] = vv[x];
+    pos[3 * n + x] = (la * box[x] + lb * box[3 + x] + lc * box[6 + x]) + un;
   }
 }
 
-// Host-buffer step, output: pos = X(L) + u and vel in AoS (the arithmetic of
-// k_state_to_pos + k_soa_to_aos), into the device buffers copied back to the caller.
-__global__ void k_md_host_end(Topo t, const double* __restrict__ u, const double* __restrict__ v,
-                              const double* __restrict__ box, double* __restrict__ pos, double* __restrict__ vel) {
+// Host-buffer step, output: vel in AoS (the arithmetic of k_soa_to_aos), into the device
+// buffer copied back to the caller (positions come from k_md_host_begin).
+__global__ void k_md_host_end(Topo t, const double* __restrict__ v, double* __restrict__ vel) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= t.N) return;
-  int la, lb, lc;
-  lattice_of(t, n, la, lb, lc);
 #pragma unroll
-  for (int x = 0; x < 3; ++x) {
-    pos[3 * n + x] = (la * box[x] + lb * box[3 + x] + lc * box[6 + x]) + u[x * t.N + n];
-    vel[3 * n + x] = v[x * t.N + n];
-  }
+  for (int x = 0; x < 3; ++x) vel[3 * n + x] = v[x * t.N + n];
 }
 
 }  // namespace
@@ -1066,7 +1063,7 @@ void launch_md_nodes(mm_handle* h, double dt, double c1, uint64_t seed, int64_t 
 }
 
 void launch_md_host_begin(mm_handle* h, double dt, double c1, uint64_t seed, int64_t step, int thermo,
-                          const double* pos, const double* vel, const double* gpos, cudaStream_t st) {
+                          double* pos, const double* vel, const double* gpos, cudaStream_t st) {
   Topo t;
   topo_of(h, t);
   MDArgs a;
@@ -1092,10 +1089,10 @@ void launch_md_host_begin(mm_handle* h, double dt, double c1, uint64_t seed, int
   }
 }
 
-void launch_md_host_end(mm_handle* h, double* pos, double* vel, cudaStream_t st) {
+void launch_md_host_end(mm_handle* h, double* vel, cudaStream_t st) {
   Topo t;
   topo_of(h, t);
-  k_md_host_end<<<node_blocks(h), kNodeThreads, 0, st>>>(t, h->d_u, h->d_v, h->d_box, pos, vel);
+  k_md_host_end<<<node_blocks(h), kNodeThreads, 0, st>>>(t, h->d_v, vel);
 }
 
 }  // namespace mm
