@@ -495,6 +495,134 @@ def measure_builder(n_cmp=128, n_large=256):
             "note": "wall time of build_system, device tables copied back into host arrays"}
 
 
+def measure_config4(n=16, npts=11, nsteps=200, every=20):
+    """The differentiation workload end to end: a 16^3 two-type two-state lattice; loss =
+    MSE of the relaxed stress over 11 uniaxial strain points (0 .. 2.5%) + MSE of the mean
+    node forces over a 200-step Verlet trajectory (dt 1 fs, checkpoint every 20 steps)
+    against targets from a hidden parameter set (C per Voigt component x (1 + U[-0.2, 0.2]),
+    h0 x (1 + U[-0.01, 0.01])). The strain points are relaxed together by the batched device
+    relaxer (FP64, max |gradient| < 1e-9 Ha/bohr) for every parameter value; gradients with
+    respect to the 21 Voigt C components and h0 per type and state and the free energies come
+    from the adjoint (implicit differentiation through the relaxations, checkpointed
+    recomputation through the trajectory) and are checked against central differences
+    (h = 1e-4 relative) of the whole loss for three parameters."""
+    import torch
+
+    from micmec_gb300 import lattices, units
+    from micmec_gb300.autograd import MicMecParameters, relaxed_stress, verlet_trajectory
+    from micmec_gb300.batch import BatchSystems
+    from micmec_gb300.pes.mmff import ForcePartMechanical
+    from micmec_gb300.system import System
+
+    t_start = time.perf_counter()
+    rng = np.random.default_rng(41)
+    d = lattices.make_lattice(lattices.defect_grid(n, 0.2, rng), nstates=2)
+    s = System.from_dict(d)
+    part = ForcePartMechanical(s, model="nanocell", precision="fp64")
+    params = MicMecParameters(part)
+    base_rv = np.array(s.domain.rvecs)
+    pos0 = np.array(s.pos)
+    Fs = []
+    for e in np.linspace(0.0, 0.025, npts):
+        F = np.eye(3)
+        F[0, 0] += e
+        Fs.append(F)
+    batch = BatchSystems([System.from_dict(d) for _ in Fs], model="nanocell", precision="fp64")
+    dev = torch.device("cuda")
+    kT = units.boltzmann * 300.0
+    vel0 = rng.normal(0.0, 1.0, s.pos.shape) * np.sqrt(kT / s.masses)[:, None]
+    vel0 -= (s.masses @ vel0) / s.masses.sum()
+    x0 = torch.tensor(pos0, dtype=torch.float64, device=dev)
+    v0 = torch.tensor(vel0, dtype=torch.float64, device=dev)
+    m = torch.tensor(np.asarray(s.masses), dtype=torch.float64, device=dev)
+    dt = 1.0 * units.femtosecond
+    tensors = list(params.tensors())
+    relax_iters = []
+
+    def relax_all():
+        C, H, D = params.native_tables(*tensors)
+        batch.set_params(H, C, D, params.temp, params.nstates)
+        batch.set_state([pos0 @ F for F in Fs], None, [base_rv @ F for F in Fs])
+        gmax, iters = batch.relax(max_iter=50000, gtol=1e-9)
+        relax_iters.append(int(iters.max()))
+        if not (gmax < 1e-9).all():
+            raise RuntimeError("relaxation did not converge: %g" % float(gmax.max()))
+        return batch.get_state()[0]
+
+    def set_domain(rv):
+        s.domain.update_rvecs(rv)
+        part.update_rvecs(rv)
+
+    def evaluate(targets=None, grad=False):
+        """(loss, gradients or None, stresses, mean forces)."""
+        positions = relax_all()
+        total, sigmas = 0.0, []
+        grads = [torch.zeros_like(t) for t in tensors] if grad else None
+        for i, F in enumerate(Fs):
+            set_domain(base_rv @ F)
+            x = torch.tensor(positions[i], dtype=torch.float64, device=dev)
+            with torch.set_grad_enabled(grad):
+                sig = relaxed_stress(x, params)
+                sigmas.append(sig.detach())
+                if targets is not None:
+                    loss = ((sig - targets[0][i]) ** 2).sum()
+                    total += float(loss.detach())
+                    if grad:
+                        for acc, gr in zip(grads, torch.autograd.grad(loss, tensors)):
+                            acc += gr
+        set_domain(base_rv)
+        with torch.set_grad_enabled(grad):
+            gl, _, _ = verlet_trajectory(x0, v0, m, params, dt, nsteps, checkpoint_every=every)
+            fbar = -torch.stack(gl[1:]).mean(0)
+            if targets is not None:
+                loss = ((fbar - targets[1]) ** 2).mean()
+                total += float(loss.detach())
+                if grad:
+                    for acc, gr in zip(grads, torch.autograd.grad(loss, tensors)):
+                        acc += gr
+        return total, grads, sigmas, fbar.detach()
+
+    # targets from the hidden parameter set
+    hidden = np.random.default_rng(4242)
+    saved = [t.detach().clone() for t in tensors]
+    with torch.no_grad():
+        tensors[0].mul_(torch.tensor(1 + hidden.uniform(-0.2, 0.2, tuple(tensors[0].shape)), device=tensors[0].device))
+        tensors[1].mul_(torch.tensor(1 + hidden.uniform(-0.01, 0.01, tuple(tensors[1].shape)),
+                                     device=tensors[1].device))
+    _, _, sig_t, f_t = evaluate()
+    with torch.no_grad():
+        for t, v in zip(tensors, saved):
+            t.copy_(v)
+    t_setup = time.perf_counter() - t_start
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loss0, grads, _, _ = evaluate((sig_t, f_t), grad=True)
+    torch.cuda.synchronize()
+    t_grad = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    evaluate((sig_t, f_t))
+    t_loss = time.perf_counter() - t0
+    errs = []
+    picks = [(0, (0, 0, 0)), (0, (1, 0, 1)), (1, (0, 0, 1, 1))]
+    for which, idx in picks:
+        t = tensors[which]
+        base = float(t.detach()[idx])
+        h = 1e-4 * abs(base)
+        vals = []
+        for sgn in (1, -1):
+            with torch.no_grad():
+                t[idx] = base + sgn * h
+            vals.append(evaluate((sig_t, f_t))[0])
+        with torch.no_grad():
+            t[idx] = base
+        fd = (vals[0] - vals[1]) / (2 * h)
+        errs.append(abs(float(grads[which][idx]) - fd) / max(abs(fd), 1e-300))
+    return {"lattice": [n] * 3, "strain_points": npts, "trajectory_steps": nsteps, "checkpoint_every": every,
+            "loss": loss0, "loss_s": t_loss, "loss_and_gradient_s": t_grad, "setup_s": t_setup,
+            "relax_iterations_max": max(relax_iters), "fd_rel_err": errs, "fd_h": "1e-4 relative",
+            "fd_params": ["C11 type 0 state 0", "C12 type 1 state 0", "h0_yy type 0 state 0"]}
+
+
 def measure_grad_over_fwd(n=16, reps=5):
     """Cost of the adjoint (backward of a force loss) relative to the forward force evaluation, 16^3 FP64."""
     import torch
@@ -757,7 +885,7 @@ def run_gpu(args):
         except Exception as exc:  # extra measurements never block the main line
             line["extra_error"] = _error_text(exc)
         for key, fn in (("builder", measure_builder), ("adjoint", measure_grad_over_fwd),
-                        ("large_mtk", measure_large_mtk)):
+                        ("differentiation_16cubed", measure_config4), ("large_mtk", measure_large_mtk)):
             try:
                 line[key] = fn()
             except Exception as exc:
@@ -785,6 +913,8 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the FP64 / batched / adjoint side measurements")
     ap.add_argument("--large-only", type=int, default=0, metavar="N",
                     help="only the large single-system NHC + MTK run (lattice engine) on an N^3 lattice")
+    ap.add_argument("--config4", action="store_true",
+                    help="only the differentiation workload (16^3, 11 relaxed strain points + 200-step trajectory)")
     ap.add_argument("--builder-only", type=int, default=0, metavar="N",
                     help="only the device system builder on an N^3 lattice with 20%% clustered defects, built "
                          "--warmup + --steps times (for kernel profiles)")
@@ -803,6 +933,9 @@ def main():
         return 0
     if args.builder_only:
         return run_builder_only(args)
+    if args.config4:
+        print(json.dumps(measure_config4()), flush=True)
+        return 0
     return run_gpu(args)
 
 

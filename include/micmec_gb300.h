@@ -285,6 +285,13 @@ mm_status mm_batch_control(mm_batch* b, double* ctl, int write);
 mm_status mm_batch_md(mm_batch* b, int nsteps, double timestep, int thermo, double temp, double timecon, int baro,
                       double press, int chain, uint64_t seed, int64_t step0, const double* noise,
                       const double* hook_noise, double* records, int use_graph, void* stream);
+/*
+ * Replace the parameter tables of a batch (same layout as mm_batch_create): used by
+ * parameter fits that relax or run many systems per parameter value. No reference
+ * counterpart (the reference builds a new ForcePartMechanical, micmec/pes/mmff.py:207-245).
+ */
+mm_status mm_batch_set_params(mm_batch* b, const int32_t* nstates, const double* h0, const double* C,
+                              const double* free_energy, const double* temp_eff);
 /* Relax node positions of every system (domain fixed) until max |gradient| < gtol. */
 mm_status mm_batch_relax(mm_batch* b, int max_iter, double gtol, void* stream);
 /*

@@ -87,8 +87,9 @@ class MicMecParameters(object):
     def tensors(self):
         return self.c21, self.h0, self.free_energy
 
-    def upload(self, c21, h0, df):
-        """Push parameter values into the native handle (unused state slots repeat state 0)."""
+    def native_tables(self, c21, h0, df):
+        """(C (T*4, 81), h0 (T*4, 9), free energies (T*4,)) in the layout of the C ABI's
+        parameter tables; unused state slots repeat state 0."""
         T = c21.shape[0]
         C = voigt21_to_tensor(c21.detach()).cpu().numpy().reshape(T * 4, 81).copy()
         H = h0.detach().cpu().numpy().reshape(T * 4, 9).copy()
@@ -98,7 +99,11 @@ class MicMecParameters(object):
                 C[4 * t + s] = C[4 * t]
                 H[4 * t + s] = H[4 * t]
                 D[4 * t + s] = D[4 * t]
-        C, H, D = (np.ascontiguousarray(a) for a in (C, H, D))
+        return tuple(np.ascontiguousarray(a) for a in (C, H, D))
+
+    def upload(self, c21, h0, df):
+        """Push parameter values into the native handle."""
+        C, H, D = self.native_tables(c21, h0, df)
         nat.check(nat.lib().mm_set_params(self.part.handle, H.ctypes.data, C.ctypes.data, D.ctypes.data,
                                           self.temp.ctypes.data), "mm_set_params")
 

@@ -50,13 +50,15 @@ def _declare(L):
                               ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_uint64, ctypes.c_int64, P, P, P,
                               ctypes.c_int, P]
     L.mm_batch_relax.argtypes = [P, ctypes.c_int, ctypes.c_double, P]
+    L.mm_batch_set_params.argtypes = [P, P, P, P, P, P]
     L.mm_batch_relax_cell.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_int, P]
     L.mm_batch_autotune.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_int, ctypes.c_double, ctypes.c_int, P]
     L.mm_batch_config.argtypes = [P, P, P]
     for n in ("mm_batch_create", "mm_batch_destroy", "mm_batch_set_state", "mm_batch_get_state", "mm_batch_control",
-              "mm_batch_md", "mm_batch_relax", "mm_batch_relax_cell", "mm_batch_autotune", "mm_batch_config"):
+              "mm_batch_md", "mm_batch_relax", "mm_batch_relax_cell", "mm_batch_autotune", "mm_batch_config",
+              "mm_batch_set_params"):
         getattr(L, n).restype = ctypes.c_int
     L._batch_declared = True
 
@@ -141,6 +143,15 @@ class BatchSystems(object):
         nat.check(self.L.mm_batch_get_state(self._h, pos.ctypes.data, vel.ctypes.data, rv.ctypes.data), "get_state")
         split = lambda a: [a[self.offsets[i]:self.offsets[i + 1]] for i in range(len(self))]
         return split(pos), split(vel), list(rv)
+
+    def set_params(self, h0, C, free_energy, temp_eff, nstates):
+        """Replace the parameter tables: h0 (types*4, 9), C (types*4, 81), free energies (types*4,),
+        effective temperatures (types,), states per type (types,) -- the layout of
+        ``type_parameters`` and ``MicMecParameters.native_tables`` (types in increasing id order)."""
+        arrs = [np.ascontiguousarray(nstates, dtype=np.int32), np.ascontiguousarray(h0, dtype=np.float64),
+                np.ascontiguousarray(C, dtype=np.float64), np.ascontiguousarray(free_energy, dtype=np.float64),
+                np.ascontiguousarray(temp_eff, dtype=np.float64)]
+        nat.check(self.L.mm_batch_set_params(self._h, *[a.ctypes.data for a in arrs]), "mm_batch_set_params")
 
     def control(self):
         c = np.zeros((len(self), CTL_LEN))

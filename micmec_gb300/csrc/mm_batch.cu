@@ -154,6 +154,26 @@ void launch_relax_cell(mm_batch* b, const CellRelax& r, cudaStream_t st) {
   mmb::launch_relax_cell(batch_launch(b), r, st);
 }
 
+// Per-type parameter tables (rest matrices and their inverses, stress maps, free
+// energies, kT) in b->tt, and the cubic-specialisation flag.
+void fill_type_tables(mm_batch* b, const int32_t* nstates, const double* h0, const double* C,
+                      const double* free_energy, const double* temp_eff) {
+  for (int t = 0; t < b->ntypes; ++t) {
+    mm::TypeTable& tt = b->tt[t];
+    std::memset(&tt, 0, sizeof(tt));
+    tt.nstates = nstates[t];
+    tt.kT = kBoltz * temp_eff[t];
+    for (int st = 0; st < MM_MAX_STATES; ++st) {
+      const int slot = t * MM_MAX_STATES + (st < nstates[t] ? st : 0);
+      std::memcpy(tt.s[st].h0, h0 + 9 * slot, 9 * sizeof(double));
+      binv3(tt.s[st].h0, tt.s[st].hinv, &tt.s[st].v0);
+      bstress_map(C + 81 * slot, tt.s[st].A);
+      tt.s[st].df = free_energy[slot];
+    }
+  }
+  b->simple = mm::tables_are_simple(b->tt, b->ntypes);
+}
+
 bool same_key(const BMD& x, const BMD& y) {
   return x.dt == y.dt && x.temp == y.temp && x.timecon == y.timecon && x.press == y.press && x.nsteps == y.nsteps &&
          x.thermo == y.thermo && x.baro == y.baro && x.chain == y.chain && x.seed == y.seed && x.step0 == y.step0 &&
@@ -200,25 +220,13 @@ mm_status mm_batch_create(int nsys, const int32_t* shapes, const int32_t* cell_t
       mm::set_error("mm_batch_create: cell type out of range");
       return MM_ERR_ARG;
     }
-  for (int t = 0; t < ntypes; ++t) {
+  for (int t = 0; t < ntypes; ++t)
     if (nstates[t] < 1 || nstates[t] > MM_MAX_STATES) {
       batch_free(b);
       mm::set_error("mm_batch_create: nstates out of range");
       return MM_ERR_ARG;
     }
-    mm::TypeTable& tt = b->tt[t];
-    std::memset(&tt, 0, sizeof(tt));
-    tt.nstates = nstates[t];
-    tt.kT = kBoltz * temp_eff[t];
-    for (int st = 0; st < MM_MAX_STATES; ++st) {
-      const int slot = t * MM_MAX_STATES + (st < nstates[t] ? st : 0);
-      std::memcpy(tt.s[st].h0, h0 + 9 * slot, 9 * sizeof(double));
-      binv3(tt.s[st].h0, tt.s[st].hinv, &tt.s[st].v0);
-      bstress_map(C + 81 * slot, tt.s[st].A);
-      tt.s[st].df = free_energy[slot];
-    }
-  }
-  b->simple = mm::tables_are_simple(b->tt, ntypes);
+  fill_type_tables(b, nstates, h0, C, free_energy, temp_eff);
   int dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, dev);
@@ -377,6 +385,24 @@ mm_status mm_batch_md(mm_batch* b, int nsteps, double timestep, int thermo, doub
     b->graph_nctas = b->nctas;
   }
   BCUDA(cudaGraphLaunch(b->graph, st));
+  return MM_OK;
+}
+
+mm_status mm_batch_set_params(mm_batch* b, const int32_t* nstates, const double* h0, const double* C,
+                               const double* free_energy, const double* temp_eff) {
+  if (!b || !nstates || !h0 || !C || !free_energy || !temp_eff) return MM_ERR_ARG;
+  for (int t = 0; t < b->ntypes; ++t)
+    if (nstates[t] < 1 || nstates[t] > MM_MAX_STATES) {
+      mm::set_error("mm_batch_set_params: nstates out of range");
+      return MM_ERR_ARG;
+    }
+  BCUDA(cudaDeviceSynchronize());
+  fill_type_tables(b, nstates, h0, C, free_energy, temp_eff);
+  BCUDA(cudaMemcpy(b->d_tt, b->tt, sizeof(b->tt), cudaMemcpyHostToDevice));
+  if (b->graph) {  // a captured launch may have been built for the other specialisation
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
   return MM_OK;
 }
 
