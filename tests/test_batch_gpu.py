@@ -238,3 +238,33 @@ def test_batch_cell_relax_under_pressure_and_fp32():
     h32, v32 = out["fp32"]
     assert np.abs(h32 - h64).max() <= 1e-5 * np.abs(h64).max()
     assert np.abs(v32 / v64 - 1).max() < 1e-4
+
+
+def test_batch_set_params_matches_single_system_with_the_same_parameters():
+    """mm_batch_set_params: a batch evaluated with replaced tables gives the energy and
+    stress of a single-system handle carrying the same parameters (mm_set_params)."""
+    import torch
+
+    from micmec_gb300.autograd import MicMecParameters
+    from micmec_gb300.batch import BatchSystems
+    from micmec_gb300.pes.mmff import ForcePartMechanical, MicMecForceField
+
+    systems, _ = _mixed_batch([4], "fp64", seed=9, sigma=0.05)
+    s = systems[0]
+    part = ForcePartMechanical(s, model="nanocell", precision="fp64")
+    ff = MicMecForceField(s, [part])
+    params = MicMecParameters(part)
+    with torch.no_grad():
+        params.c21.mul_(1.1)
+        params.h0.mul_(1.002)
+        params.free_energy.add_(1e-4)
+    params.upload(*params.tensors())
+    vt = np.zeros((3, 3))
+    e_part = ff.compute(None, vt)
+    b = BatchSystems([s], model="nanocell", precision="fp64")
+    C, H, D = params.native_tables(*params.tensors())
+    b.set_params(H, C, D, params.temp, params.nstates)
+    b.set_state([s.pos], None, [s.domain.rvecs])
+    b.relax(max_iter=0, gtol=1e-3)  # one force evaluation, no step
+    assert abs(b.energies()[0] - e_part) <= 1e-11 * abs(e_part)
+    assert np.abs(b.stress()[0] - vt / s.domain.volume).max() <= 1e-10 * np.abs(vt / s.domain.volume).max()
