@@ -12,12 +12,12 @@ import numpy as np
 
 from micmec_gb300.units import boltzmann, femtosecond
 from micmec_gb300.sampling.iterative import StateItem
-from micmec_gb300.sampling.utils import get_random_vel, clean_momenta, get_ndof_internal_md
+from micmec_gb300.sampling.utils import get_random_vel, clean_momenta, get_ndof_internal_md, stabilized_cholesky_decomp
 from micmec_gb300.sampling.verlet import VerletHook
 
 __all__ = [
-    "AndersenThermostat", "BerendsenThermostat", "LangevinThermostat", "CSVRThermostat", "NHCThermostat",
-    "NHChain", "NHCAttributeStateItem",
+    "AndersenThermostat", "BerendsenThermostat", "LangevinThermostat", "CSVRThermostat", "GLEThermostat",
+    "NHCThermostat", "NHChain", "NHCAttributeStateItem",
 ]
 
 
@@ -189,6 +189,65 @@ class CSVRThermostat(VerletHook):
 
     def post(self, iterative, G1_add=None):
         pass
+
+
+class GLEThermostat(VerletHook):
+    """Generalised Langevin (coloured-noise) thermostat (Ceriotti, Bussi, Parrinello, J. Chem.
+    Theory Comput. 6, 1170 (2010)); nvt.py:277-358.
+
+    ns auxiliary momenta per degree of freedom; before and after every step the extended
+    vector (sqrt(m) v, s) is propagated by T = exp(-A dt / 2) and noise S xi with
+    S S^T = C - T C T^T (C = kT I unless given); the kinetic-energy change goes into the
+    conserved-quantity correction. A host hook (the step's forces still run on the GPU).
+
+    Extra, for validation: ``replay_noise`` (a list: the (ns, 3N) draw of ``init``, then one
+    (ns + 1, 3N) draw per call) makes the run use given standard normals.
+    """
+
+    name = "GLE"
+    kind = "stochastic"
+    method = "thermostat"
+
+    def __init__(self, temp, a_p, c_p=None, start=0, replay_noise=None):
+        self.temp = temp
+        self.ns = int(a_p.shape[0] - 1)
+        self.a_p = np.asarray(a_p, dtype=float)
+        self.c_p = boltzmann * self.temp * np.eye(self.ns + 1) if c_p is None else np.asarray(c_p, dtype=float)
+        self.replay_noise = None if replay_noise is None else list(replay_noise)
+        VerletHook.__init__(self, start, 1)
+
+    def _normal(self, shape):
+        if self.replay_noise is not None:
+            z = np.asarray(self.replay_noise.pop(0), dtype=float)
+            if z.shape != tuple(shape):
+                raise ValueError("replayed draw of shape %s, expected %s" % (z.shape, tuple(shape)))
+            return z
+        return np.random.normal(size=shape)
+
+    def init(self, iterative):
+        clean_momenta(iterative.pos, iterative.vel, iterative.masses, iterative.mmf.system.domain)
+        self.s = 0.5 * boltzmann * self.temp * self._normal((self.ns, iterative.pos.size))
+        eigval, eigvec = np.linalg.eig(-self.a_p * iterative.timestep / 2)
+        self.t = np.dot(eigvec * np.exp(eigval), np.linalg.inv(eigvec)).real
+        self.S = stabilized_cholesky_decomp(self.c_p - np.dot(np.dot(self.t, self.c_p), self.t.T)).real
+        self.n_atoms = iterative.pos.shape[0]
+
+    def pre(self, iterative, G1_add=None):
+        self.thermo(iterative)
+
+    def post(self, iterative, G1_add=None):
+        self.thermo(iterative)
+
+    def thermo(self, iterative):
+        ekin0 = iterative.ekin
+        sq = np.sqrt(iterative.masses)[:, None]
+        p = (sq * iterative.vel).reshape(-1)
+        s_old = np.vstack([p, self.s])
+        s_new = np.dot(self.t, s_old) + np.dot(self.S, self._normal((self.ns + 1, 3 * self.n_atoms)))
+        iterative.vel[:] = np.sqrt(1.0 / iterative.masses)[:, None] * s_new[0, :].reshape((self.n_atoms, 3))
+        self.s[:] = s_new[1:, :]
+        iterative.ekin = iterative._compute_ekin()
+        self.econs_correction += ekin0 - iterative.ekin
 
 
 class NHChain(object):

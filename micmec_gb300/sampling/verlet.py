@@ -550,8 +550,11 @@ class VerletHook(Hook):
     """Hook with init/pre/post calls around each Verlet step (thermostats, barostats)."""
 
     def __init__(self, start=0, step=1):
+        # The reference accepts start and step but calls every Verlet hook at every step
+        # from step 0 (its VerletHook passes start=0, step=1 to Hook, verlet.py:316-327);
+        # trajectories are kept identical to the reference's, so this does the same.
         self.econs_correction = 0.0
-        Hook.__init__(self, start=start, step=step)
+        Hook.__init__(self, start=0, step=1)
 
     def __call__(self, iterative):
         pass

@@ -37,7 +37,9 @@ from micmec.system import System  # noqa: E402
 from micmec.pes.mmff import MicMecForceField, ForcePartMechanical  # noqa: E402
 from micmec.sampling.verlet import VerletIntegrator  # noqa: E402
 from micmec.sampling.iterative import Hook  # noqa: E402
-from micmec.sampling.nvt import BerendsenThermostat, CSVRThermostat, LangevinThermostat, NHCThermostat  # noqa: E402
+from micmec.sampling.nvt import (  # noqa: E402
+    AndersenThermostat, BerendsenThermostat, CSVRThermostat, GLEThermostat, LangevinThermostat, NHCThermostat,
+)
 from micmec.sampling.npt import BerendsenBarostat, LangevinBarostat, MTKBarostat, TBCombination  # noqa: E402
 from micmec.sampling.dof import CartesianDOF, FullCellDOF, StrainCellDOF  # noqa: E402
 from micmec.sampling.opt import QNOptimizer  # noqa: E402
@@ -397,6 +399,32 @@ def make_hook_fixtures():
     run_md("nhc_lbaro_nanocell", "nanocell", 100, nhc_lbaro, 25, extra=end_state)
 
 
+def make_gle_fixture():
+    """The coloured-noise (GLE) thermostat with two auxiliary momenta (nvt.py:277-358)."""
+    T = 300.0 * units.kelvin
+    fs = units.femtosecond
+    a_p = np.array([[1.0, 0.5, 0.2], [-0.5, 2.0, 0.0], [-0.2, 0.0, 3.0]]) / (100 * fs)
+
+    def gle(ff):
+        return [GLEThermostat(T, a_p)], {"temp": T, "a_p": a_p}
+
+    def draws(arrays, vi):
+        d = vi.noise_draws
+        n3 = vi.pos.size
+        arrays["gle_s0"] = [x for x in d if x.shape == (2, n3)][0]
+        arrays["gle_noise"] = np.array([x for x in d if x.shape == (3, n3)])
+
+    run_md("gle_nanocell", "nanocell", 40, gle, 20, extra=draws)
+
+    def andersen(ff):
+        # velocities redrawn every 5 steps for half of the nodes, with annealing; the draws
+        # come from np.random seeded as run_md seeds it (seed + 2000)
+        return ([AndersenThermostat(2 * T, step=5, select=np.arange(0, 27, 2), annealing=0.99)],
+                {"temp": 2 * T, "step": 5, "annealing": 0.99, "np_random_seed": 2001})
+
+    run_md("andersen_nanocell", "nanocell", 50, andersen, 25)
+
+
 # ------------------------------------------------------------------ optimiser
 
 
@@ -445,7 +473,7 @@ def make_cell_opt_fixtures():
 
 
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["forces", "builder", "md", "hooks", "opt", "cellopt"]
+    which = sys.argv[1:] or ["forces", "builder", "md", "hooks", "gle", "opt", "cellopt"]
     if "forces" in which:
         make_force_fixtures()
     if "builder" in which:
@@ -454,6 +482,8 @@ if __name__ == "__main__":
         make_md_fixtures()
     if "hooks" in which:
         make_hook_fixtures()
+    if "gle" in which:
+        make_gle_fixture()
     if "opt" in which:
         make_opt_fixture()
     if "cellopt" in which:

@@ -3,8 +3,8 @@
 The force field is the NumPy oracle (``oracle/mmff.py``) behind the ``ForcePart``
 interface, so the hook classes of ``micmec_gb300.sampling`` run their host path on the
 CPU. The golden files hold the reference's per-step records for every thermostat and
-barostat ``TBCombination`` accepts (alone and combined) and the CSVR thermostat; the
-stochastic hooks replay the reference's recorded draws.
+barostat ``TBCombination`` accepts (alone and combined), the CSVR and the GLE thermostats;
+the stochastic hooks replay the reference's recorded draws.
 """
 import numpy as np
 import pytest
@@ -58,6 +58,15 @@ def hooks_for(name, g, ff):
     from micmec_gb300.sampling.nvt import BerendsenThermostat, CSVRThermostat, LangevinThermostat, NHCThermostat
 
     T = float(g["meta/temp"])
+    if name == "md_andersen_nanocell":
+        from micmec_gb300.sampling.nvt import AndersenThermostat
+
+        return [AndersenThermostat(T, step=int(g["meta/step"]), select=np.arange(0, 27, 2),
+                                   annealing=float(g["meta/annealing"]))]
+    if name == "md_gle_nanocell":
+        from micmec_gb300.sampling.nvt import GLEThermostat
+
+        return [GLEThermostat(T, g["meta/a_p"], replay_noise=[g["gle_s0"]] + list(g["gle_noise"]))]
     if name == "md_langevin_nanocell":
         return [LangevinThermostat(T, timecon=float(g["meta/timecon"]), replay_noise=g["noise"])]
     if name == "md_nhc_nanocell":
@@ -94,7 +103,8 @@ def hooks_for(name, g, ff):
 
 NAMES = ["md_langevin_nanocell", "md_nhc_nanocell", "md_mtk_nanocell", "md_nhc_mtk_nanocell",
          "md_langevin_mtk_nanocell", "md_berendsen_nanocell", "md_csvr_nanocell", "md_berendsen_mtk_nanocell",
-         "md_nhc_bbaro_nanocell", "md_lbaro_nanocell", "md_nhc_lbaro_nanocell"]
+         "md_nhc_bbaro_nanocell", "md_lbaro_nanocell", "md_nhc_lbaro_nanocell", "md_gle_nanocell",
+         "md_andersen_nanocell"]
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -105,8 +115,11 @@ def test_host_hooks_match_reference(name):
     s, ff = _oracle_ff(g)
     rows = Rows()
     n = len(g["records"]) - 1
-    vi = VerletIntegrator(ff, float(g["timestep"]), hooks=hooks_for(name, g, ff) + [rows.hook],
-                          vel0=g["vel0"].copy(), device=False)
+    hooks = hooks_for(name, g, ff)
+    if "meta/np_random_seed" in g.files:  # draws from np.random, seeded as the reference run was
+        np.random.seed(int(g["meta/np_random_seed"]))
+    vi = VerletIntegrator(ff, float(g["timestep"]), hooks=hooks + [rows.hook], vel0=g["vel0"].copy(),
+                          device=False)
     vi.run(n)
     ref = g["records"][: n + 1]
     got = np.array(rows.rows)
