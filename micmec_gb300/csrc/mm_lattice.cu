@@ -261,6 +261,12 @@ __global__ void __launch_bounds__(kCellThreads) k_cells(Topo t, const TypeTable*
 // block's partial of a component is one warp sum.
 constexpr int kCell8Threads = 256;
 constexpr int kCell8Cells = kCell8Threads / 8;
+// Row stride of the staging tiles ([24 rows = corner x component][cell slot]). A warp's
+// staging store writes one row per corner (8 corners x 4 cell slots): with stride 44
+// (3 x 44 = 4 mod 32) those 32 words fall in 32 different banks; with stride 32 the eight
+// corners of a cell shared a bank (8-way conflicts on every store).
+constexpr int kTileStride = 44;
+constexpr int kTileElems = (2 * 24) * kTileStride + kCell8Cells;  // tile, relt, et
 static_assert(kCell8Threads == 256 && kCellPart == 10, "component ownership assumes 8 warps and 10 components");
 
 template <typename T, bool STRUCT, bool SIMPLE>
@@ -273,7 +279,7 @@ __global__ void __launch_bounds__(kCell8Threads, sizeof(T) == 4 ? 3 : 2) k_cells
   const size_t tp_bytes = ((sizeof(TypeParams<T>) * ntypes + 15) / 16) * 16;
   // two buffers (alternating groups), so one barrier per group suffices
   T* const buf0 = reinterpret_cast<T*>(smem_raw + tp_bytes);
-  constexpr int kBuf = (2 * 24 + 1) * kCell8Cells;
+  constexpr int kBuf = kTileElems;
   __shared__ T Ls[9];
   load_params<T>(tp, tt, ntypes, box);
   if (threadIdx.x < 9) Ls[threadIdx.x] = (T)box[threadIdx.x];
@@ -315,9 +321,9 @@ __global__ void __launch_bounds__(kCell8Threads, sizeof(T) == 4 ? 3 : 2) k_cells
   };
   if constexpr (kPrefetch) load_group(blockIdx.x);
   for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x, parity ^= 1) {
-  T* tile = buf0 + parity * kBuf;      // [24][kCell8Cells] corner gradients
-  T* relt = tile + 24 * kCell8Cells;   // [24][kCell8Cells] vertex offsets r_a - r_0
-  T* et = relt + 24 * kCell8Cells;     // [kCell8Cells] cell energies
+  T* tile = buf0 + parity * kBuf;      // [24][kTileStride] corner gradients
+  T* relt = tile + 24 * kTileStride;   // [24][kTileStride] vertex offsets r_a - r_0
+  T* et = relt + 24 * kTileStride;     // [kCell8Cells] cell energies
   const int cell = grp * kCell8Cells + cl;
   const bool valid = cell < t.M;
   if constexpr (!kPrefetch) load_group(grp);
@@ -331,13 +337,13 @@ __global__ void __launch_bounds__(kCell8Threads, sizeof(T) == 4 ? 3 : 2) k_cells
   const int src0 = lane & ~7;
 #pragma unroll
   for (int x = 0; x < 3; ++x) {
-    tile[(corner * 3 + x) * kCell8Cells + cl] = valid ? g[x] : T(0);
+    tile[(corner * 3 + x) * kTileStride + cl] = valid ? g[x] : T(0);
     const T d0 = __shfl_sync(0xffffffffu, du[x], src0);
     T r = du[x] - d0;
     if (a & 1) r += Ls[0 * 3 + x];
     if (a & 2) r += Ls[1 * 3 + x];
     if (a & 4) r += Ls[2 * 3 + x];
-    relt[(corner * 3 + x) * kCell8Cells + cl] = r;
+    relt[(corner * 3 + x) * kTileStride + cl] = r;
   }
   if (a == 0) et[cl] = valid ? Ecell : T(0);
   if (valid && a == 0 && ecell) ecell[cell] = (double)Ecell;
@@ -346,14 +352,14 @@ __global__ void __launch_bounds__(kCell8Threads, sizeof(T) == 4 ? 3 : 2) k_cells
     // component c0 of cell slot `lane`, corners in reference order
     T v = T(0);
 #pragma unroll
-    for (int k = 0; k < 8; ++k) v += tile[(k * 3 + c0x) * kCell8Cells + lane] * relt[(k * 3 + c0y) * kCell8Cells + lane];
+    for (int k = 0; k < 8; ++k) v += tile[(k * 3 + c0x) * kTileStride + lane] * relt[(k * 3 + c0y) * kTileStride + lane];
     if constexpr (sizeof(T) == 8) acc0 += v;
     else acc0 = f2_add(acc0, F2{v, 0.0f});
     if (warp < 2) {
       T w = T(0);
       if (warp == 0) {
 #pragma unroll
-        for (int k = 0; k < 8; ++k) w += tile[(k * 3 + 2) * kCell8Cells + lane] * relt[(k * 3 + 2) * kCell8Cells + lane];
+        for (int k = 0; k < 8; ++k) w += tile[(k * 3 + 2) * kTileStride + lane] * relt[(k * 3 + 2) * kTileStride + lane];
       } else {
         w = et[lane];
       }
@@ -366,7 +372,7 @@ __global__ void __launch_bounds__(kCell8Threads, sizeof(T) == 4 ? 3 : 2) k_cells
     const int c = grp * kCell8Cells + lane;
     if (c < t.M)
 #pragma unroll
-      for (int r = warp; r < 24; r += 8) G[r * (size_t)t.M + c] = tile[r * kCell8Cells + lane];
+      for (int r = warp; r < 24; r += 8) G[r * (size_t)t.M + c] = tile[r * kTileStride + lane];
   }
   }  // groups
   // block partials: slot 0 energy, slot 1 + 3x + y virial; component c -> slot (c == 9 ? 0 : 1 + c)
@@ -873,7 +879,7 @@ static void topo_of(const mm_handle* h, Topo& t) {
 static size_t cell_smem(const mm_handle* h) {
   const size_t esz = h->prec == MM_PREC_FP32 ? sizeof(float) : sizeof(double);
   const size_t tp = (h->prec == MM_PREC_FP32 ? sizeof(TypeParams<float>) : sizeof(TypeParams<double>)) * h->ntypes;
-  if (h->model == MM_MODEL_NANOCELL) return ((tp + 15) / 16) * 16 + 2 * esz * (2 * 24 + 1) * kCell8Cells;
+  if (h->model == MM_MODEL_NANOCELL) return ((tp + 15) / 16) * 16 + 2 * esz * kTileElems;
   return ((tp + 15) / 16) * 16 + sizeof(double) * kCellPart * (kCellThreads / 32);
 }
 
