@@ -212,27 +212,39 @@ def test_device_and_host_langevin_paths_agree_with_replayed_noise_fp32():
         assert np.abs(a[:, col] - b[:, col]).max() <= 1e-6 * np.abs(b[:, col]).max()
 
 
-@pytest.mark.parametrize("thermo", ["nhc", "langevin"])
-def test_engine_fp32_tracks_fp64_with_barostat(thermo):
-    """Lattice engine (NHC or Langevin + MTK, 100 MPa): FP32 cells (gather fused into the
-    kicks, FP32 increments, compensated FP32 kinetic sums) against FP64 cells."""
+@pytest.mark.parametrize("hooks", ["nhc+mtk", "langevin+mtk", "berendsen+bbaro", "csvr", "nhc+lbaro"])
+def test_engine_fp32_tracks_fp64_with_hooks(hooks):
+    """Lattice engine with thermostat / barostat hooks (100 MPa): FP32 cells (gather fused into
+    the kicks, FP32 increments, compensated FP32 kinetic sums) against FP64 cells, with the same
+    generated draws for the stochastic hooks."""
     from micmec_gb300 import units
+    from micmec_gb300.sampling.npt import BerendsenBarostat, LangevinBarostat, MTKBarostat
+    from micmec_gb300.sampling.nvt import BerendsenThermostat, CSVRThermostat, LangevinThermostat, NHCThermostat
     from micmec_gb300.pes.mmff import ForcePartMechanical, MicMecForceField
-    from micmec_gb300.sampling.npt import MTKBarostat
-    from micmec_gb300.sampling.nvt import LangevinThermostat, NHCThermostat
     from micmec_gb300.sampling.verlet import VerletIntegrator
 
+    fs = units.femtosecond
+    P = 100e6 * units.pascal
     out = {}
     for prec in ("fp64", "fp32"):
         s, vel = _lattice(10, 2, 5)
         ff = MicMecForceField(s, [ForcePartMechanical(s, model="nanocell", precision=prec)])
         rec = Rec()
         # fixed initial chain and barostat velocities (by default both are drawn at random)
-        t = (NHCThermostat(300.0, timecon=100 * units.femtosecond, chain_vel0=np.array([1e-5, -2e-5, 1e-5]))
-             if thermo == "nhc" else LangevinThermostat(300.0, timecon=100 * units.femtosecond, seed=3))
-        b = MTKBarostat(ff, 300.0, 100e6 * units.pascal, timecon=1000 * units.femtosecond, vel_press0=np.zeros((3, 3)))
-        vi = VerletIntegrator(ff, 1.0 * units.femtosecond, hooks=[t, b, rec.hook], vel0=vel, device=True)
+        nhc = NHCThermostat(300.0, timecon=100 * fs, chain_vel0=np.array([1e-5, -2e-5, 1e-5]))
+        hs = {
+            "nhc+mtk": lambda: [nhc, MTKBarostat(ff, 300.0, P, timecon=1000 * fs, vel_press0=np.zeros((3, 3)))],
+            "langevin+mtk": lambda: [LangevinThermostat(300.0, timecon=100 * fs, seed=3),
+                                     MTKBarostat(ff, 300.0, P, timecon=1000 * fs, vel_press0=np.zeros((3, 3)))],
+            "berendsen+bbaro": lambda: [BerendsenThermostat(300.0, timecon=100 * fs),
+                                        BerendsenBarostat(ff, 300.0, P, timecon=1000 * fs)],
+            "csvr": lambda: [CSVRThermostat(300.0, timecon=100 * fs, seed=5)],
+            "nhc+lbaro": lambda: [nhc, LangevinBarostat(ff, 300.0, P, timecon=2000 * fs, vel_press0=np.zeros((3, 3)),
+                                                        seed=7)],
+        }[hooks]()
+        vi = VerletIntegrator(ff, 1.0 * fs, hooks=hs + [rec.hook], vel0=vel, device=True)
         vi.batch_max_cells = 0
+        assert vi._device_plan()[1]["engine"] == "lattice"
         vi.run(60)
         out[prec] = np.array(rec.rows)
     a, b = out["fp64"], out["fp32"]
