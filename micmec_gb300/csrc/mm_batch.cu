@@ -209,6 +209,8 @@ mm_status mm_batch_create(int nsys, const int32_t* shapes, const int32_t* cell_t
       return MM_ERR_ARG;
     }
     y.M = y.nx * y.ny * y.nz;
+    y.div_nyz = mm::make_fastdiv((uint32_t)(y.ny * y.nz));
+    y.div_nz = mm::make_fastdiv((uint32_t)y.nz);
     y.off = off;
     off += y.M;
     b->sys.push_back(y);

@@ -40,7 +40,16 @@ using namespace mmc;
 struct BSys {
   int nx, ny, nz, M;
   long long off;  // first node / cell in the concatenated arrays
+  FastDiv div_nyz, div_nz;  // cell / node index -> grid coordinates
 };
+
+// grid coordinates (i, j, k) of cell or node index n of system s
+__device__ __forceinline__ void grid_coords(const BSys& s, int n, int& i, int& j, int& k) {
+  i = fdiv(n, s.div_nyz);
+  const int r = n - i * (s.ny * s.nz);
+  j = fdiv(r, s.div_nz);
+  k = r - j * s.nz;
+}
 
 struct BArgs {
   const BSys* sys;
@@ -177,7 +186,8 @@ __device__ void forces(const BArgs& a, Shared<T>& sh, const BSys& sy) {
       T du[3] = {T(0), T(0), T(0)};
       int ty = 0;
       if (valid) {
-        const int nyz = sy.ny * sy.nz, i = cell / nyz, r = cell - i * nyz, j = r / sy.nz, k = r - j * sy.nz;
+        int i, j, k;
+        grid_coords(sy, cell, i, j, k);
         const int node = wrap_node(sy, i + (av & 1), j + ((av >> 1) & 1), k + (av >> 2));
         for (int x = 0; x < 3; ++x) du[x] = disp[x * N3 + sy.off + node];
         ty = a.ctype[sy.off + cell];
@@ -210,7 +220,8 @@ __device__ void forces(const BArgs& a, Shared<T>& sh, const BSys& sy) {
     }
   } else {
     for (int cell = threadIdx.x; cell < M; cell += blockDim.x) {
-      const int nyz = sy.ny * sy.nz, i = cell / nyz, r = cell - i * nyz, j = r / sy.nz, k = r - j * sy.nz;
+      int i, j, k;
+      grid_coords(sy, cell, i, j, k);
       T du[8][3];
       for (int b = 0; b < 8; ++b) {
         const int node = wrap_node(sy, i + (b & 1), j + ((b >> 1) & 1), k + (b >> 2));
@@ -242,7 +253,8 @@ __device__ void forces(const BArgs& a, Shared<T>& sh, const BSys& sy) {
     for (int i = 0; i < 9; ++i) sh.ctl[C_VT + i] = acc[1 + i];
   }
   for (int n = threadIdx.x; n < M; n += blockDim.x) {
-    const int nyz = sy.ny * sy.nz, i = n / nyz, r = n - i * nyz, j = r / sy.nz, k = r - j * sy.nz;
+    int i, j, k;
+    grid_coords(sy, n, i, j, k);
     T s[3] = {T(0), T(0), T(0)};
     for (int kc = 0; kc < 8; ++kc) {
       const int b = corner_to_bits(kc);

@@ -764,8 +764,10 @@ __global__ void __launch_bounds__(kMDThreads, 1) k_md_nodes(Topo t, MDArgs p, co
 #pragma unroll
     for (int i = 0; i < kNodePart; ++i) accum[i] += obs[i];
   } else {
+    // obs[1] is not summed for FP32 cells (formed from the kinetic tensor's diagonal)
 #pragma unroll
-    for (int i = 0; i < kNodePart; ++i) accum[i] = f2_add(accum[i], F2{(float)obs[i], 0.0f});
+    for (int i = 0; i < kNodePart; ++i)
+      if (i != 1) accum[i] = f2_add(accum[i], F2{(float)obs[i], 0.0f});
   }
   }  // nodes
   double tot[kNodePart];
