@@ -540,6 +540,7 @@ __global__ void __launch_bounds__(kMDThreads, 1) k_md_nodes(Topo t, MDArgs p, co
   // block b owns the contiguous node range [N b / nb, N (b + 1) / nb): equal shares
   // for all SMs; its threads stride through it
   const int n_end = (int)(((long long)t.N * (blockIdx.x + 1)) / nb);
+  const int n_first_end = (int)(((long long)t.N * blockIdx.x) / nb) + (int)blockDim.x;  // first pass
   for (int n = (int)(((long long)t.N * blockIdx.x) / nb) + threadIdx.x; n < n_end; n += blockDim.x) {
   R obs[kNodePart];
 #pragma unroll
@@ -764,10 +765,17 @@ __global__ void __launch_bounds__(kMDThreads, 1) k_md_nodes(Topo t, MDArgs p, co
 #pragma unroll
     for (int i = 0; i < kNodePart; ++i) accum[i] += obs[i];
   } else {
-    // obs[1] is not summed for FP32 cells (formed from the kinetic tensor's diagonal)
+    // obs[1] is not summed for FP32 cells (formed from the kinetic tensor's diagonal); a
+    // thread's first node starts the compensated sums (exactly what adding it to zero gives)
+    if (n < n_first_end) {
 #pragma unroll
-    for (int i = 0; i < kNodePart; ++i)
-      if (i != 1) accum[i] = f2_add(accum[i], F2{(float)obs[i], 0.0f});
+      for (int i = 0; i < kNodePart; ++i)
+        if (i != 1) accum[i] = F2{(float)obs[i], 0.0f};
+    } else {
+#pragma unroll
+      for (int i = 0; i < kNodePart; ++i)
+        if (i != 1) accum[i] = f2_add(accum[i], F2{(float)obs[i], 0.0f});
+    }
   }
   }  // nodes
   double tot[kNodePart];
