@@ -258,7 +258,10 @@ mm_status mm_batch_create(int nsys, const int32_t* shapes, const int32_t* cell_t
          bok(cudaMemcpy(b->d_invm, invm.data(), N * 8, cudaMemcpyHostToDevice), "upload") &&
          bok(cudaMemset(b->d_v, 0, 3 * N * 8), "memset") && bok(cudaMemset(b->d_u, 0, 3 * N * 8), "memset") &&
          bok(cudaMemset(b->d_ctl, 0, (size_t)nsys * C_LEN * 8), "memset");
-  if (!ok || batch_partition(b, std::min(nsys, 2 * b->num_sms)) != MM_OK) {
+  // default: one system per CTA, longest first; the CTA scheduler then starts each
+  // system as soon as a slot frees, which balances uneven step costs better than a
+  // fixed assignment of several systems to each resident CTA
+  if (!ok || batch_partition(b, nsys) != MM_OK) {
     batch_free(b);
     return MM_ERR_CUDA;
   }
@@ -433,8 +436,8 @@ mm_status mm_batch_relax_cell(mm_batch* b, int max_iter, double gtol, double sto
 }
 
 // Autotuner: times `probe_steps` MD steps for each CTA size (128, 256) and number of
-// persistent CTAs (1, 2, 4 per SM, capped by the system count), restoring the state
-// after every probe, and keeps the fastest configuration.
+// CTAs (1, 2, 4 per SM, or one per system; capped by the system count), restoring the
+// state after every probe, and keeps the fastest configuration.
 mm_status mm_batch_autotune(mm_batch* b, int probe_steps, double timestep, int thermo, double temp, double timecon,
                             int baro, double press, int chain, double* best_ms) {
   if (!b || probe_steps < 1 || !(timestep > 0.0) || !hooks_valid(thermo, timecon, baro, chain)) return MM_ERR_ARG;
@@ -450,11 +453,12 @@ mm_status mm_batch_autotune(mm_batch* b, int probe_steps, double timestep, int t
   float best = 1e30f;
   int best_bt = b->bt, best_ctas = b->nctas;
   const int bts[2] = {128, 256};
-  const int per_sm[3] = {1, 2, 4};
+  const int ctas[4] = {b->num_sms, 2 * b->num_sms, 4 * b->num_sms, b->nsys};
   for (int ib = 0; ib < 2; ++ib)
-    for (int ip = 0; ip < 3; ++ip) {
+    for (int ip = 0; ip < 4; ++ip) {
+      if (ip > 0 && std::min(b->nsys, ctas[ip]) == std::min(b->nsys, ctas[ip - 1])) continue;
       b->bt = bts[ib];
-      mm_status s = batch_partition(b, std::min(b->nsys, per_sm[ip] * b->num_sms));
+      mm_status s = batch_partition(b, std::min(b->nsys, ctas[ip]));
       if (s != MM_OK) return s;
       BMD p;
       p.dt = timestep;
