@@ -549,53 +549,63 @@ __device__ __forceinline__ T cell8_eval(const T (&du)[3], int a, const TypeParam
   }
   const int ns_lane = valid ? tpl.nstates : 1;
   const int ns = __reduce_max_sync(0xffffffffu, ns_lane);
-  // state-weighted row gradients of matrix a (online -kT log-sum-exp weights); the
-  // exchange with the neighbouring matrices happens once, after the state loop
-  T Gacc[9];
-#pragma unroll
-  for (int i = 0; i < 9; ++i) Gacc[i] = T(0);
-  T m = T(0), wsum = T(0);
   const T kT = tpl.kT;
-  for (int s = 0; s < ns; ++s) {
-    const bool active = s < ns_lane;
-    const StateParams<T>& p = tpl.s[active ? s : 0];
-    T W[9], Dm[9], sv[6], Es, df;
-    const T sc = T(0.125) * p.v0;
-    struct NoView {};
-    typename std::conditional<SIMPLE && sizeof(T) == 4, CubicView<float>, NoView>::type cv;
+  struct NoView {};
+  typedef typename std::conditional<SIMPLE && sizeof(T) == 4, CubicView<float>, NoView>::type View;
+  // energy part of state p: strain and stress of matrix a (Dm, sv), the cell's elastic
+  // energy summed over the group, plus the state's free energy
+  auto energy = [&](const StateParams<T>& p, View& cv, T (&Dm)[9], T (&sv)[6]) -> T {
+    T W[9], Es, df;
     if constexpr (SIMPLE && sizeof(T) == 4) {
       load_cubic(p, cv);
 #pragma unroll
       for (int d = 0; d < 3; ++d)
 #pragma unroll
         for (int x = 0; x < 3; ++x) W[d * 3 + x] = cv.B[d * 3 + x] + ed[d][x];
-      Es = state_energy<T, true, CubicView<float>>(W, cv, sc, Dm, sv);
+      Es = state_energy<T, true, CubicView<float>>(W, cv, T(0.125) * cv.v0, Dm, sv);
       df = cv.df;
     } else {
 #pragma unroll
       for (int d = 0; d < 3; ++d)
 #pragma unroll
         for (int x = 0; x < 3; ++x) W[d * 3 + x] = p.B[d * 3 + x] + ed[d][x];
-      Es = state_energy<T, SIMPLE>(W, p, sc, Dm, sv);
+      Es = state_energy<T, SIMPLE>(W, p, T(0.125) * p.v0, Dm, sv);
       df = p.df;
     }
     Es += __shfl_xor_sync(0xffffffffu, Es, 1);
     Es += __shfl_xor_sync(0xffffffffu, Es, 2);
     Es += __shfl_xor_sync(0xffffffffu, Es, 4);
-    const T E = Es + df;
+    return Es + df;
+  };
+  // row gradients of matrix a in state p from the energy part's Dm, sv
+  auto gradient = [&](const StateParams<T>& p, const View& cv, const T (&Dm)[9], const T (&sv)[6], T* GW) {
+    if constexpr (SIMPLE && sizeof(T) == 4) state_gradient<T, true, CubicView<float>>(Dm, sv, cv, T(0.125) * cv.v0, GW);
+    else state_gradient<T, SIMPLE>(Dm, sv, p, T(0.125) * p.v0, GW);
+  };
+  // state-weighted row gradients of matrix a (online -kT log-sum-exp weights); the
+  // exchange with the neighbouring matrices happens once, after the state loop. The
+  // first state (every lane has one) starts the running minimum m and the sums.
+  T Gacc[9];
+  T m, wsum = T(1);
+  {
+    View cv;
+    T Dm[9], sv[6];
+    m = energy(tpl.s[0], cv, Dm, sv);
+    gradient(tpl.s[0], cv, Dm, sv, Gacc);
+  }
+  for (int s = 1; s < ns; ++s) {
+    const bool active = s < ns_lane;
+    const StateParams<T>& p = tpl.s[active ? s : 0];
+    View cv;
+    T Dm[9], sv[6];
+    const T E = energy(p, cv, Dm, sv);
     // A state whose weight against the lowest energy so far is below e^-50 adds nothing
     // representable to the weighted gradient (nor to the weight sum): its gradient is not
     // formed. The lowest energy can only fall later, so the weight stays below e^-50.
-    if (active && (s == 0 || !(E - m >= T(50) * kT))) {
+    if (active && !(E - m >= T(50) * kT)) {
       T GW[9];
-      if constexpr (SIMPLE && sizeof(T) == 4) state_gradient<T, true, CubicView<float>>(Dm, sv, cv, sc, GW);
-      else state_gradient<T, SIMPLE>(Dm, sv, p, sc, GW);
-      if (s == 0) {
-        m = E;
-        wsum = T(1);
-#pragma unroll
-        for (int i = 0; i < 9; ++i) Gacc[i] = GW[i];
-      } else if (E < m) {
+      gradient(p, cv, Dm, sv, GW);
+      if (E < m) {
         const T r = lse_weight<T>(E - m, kT, tpl.lkT);
         wsum = wsum * r + T(1);
 #pragma unroll

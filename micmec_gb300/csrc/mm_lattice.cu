@@ -293,6 +293,11 @@ __global__ void __launch_bounds__(kCell8Threads, sizeof(T) == 4 ? 3 : 2) k_cells
   // components owned by this warp: c0 = warp (virial x = c0 / 3, y = c0 % 3), and for
   // warps 0, 1 also c1 = 8 (virial zz) / 9 (energy)
   const int c0x = warp / 3, c0y = warp % 3;
+  // lattice offset of vertex a, offset(a) . L (the same in every group)
+  T loff[3];
+#pragma unroll
+  for (int x = 0; x < 3; ++x)
+    loff[x] = ((a & 1) ? Ls[x] : T(0)) + ((a & 2) ? Ls[3 + x] : T(0)) + ((a & 4) ? Ls[6 + x] : T(0));
   typedef typename std::conditional<sizeof(T) == 8, double, F2>::type Acc;
   Acc acc0{}, acc1{};
   int parity = 0;
@@ -339,11 +344,7 @@ __global__ void __launch_bounds__(kCell8Threads, sizeof(T) == 4 ? 3 : 2) k_cells
   for (int x = 0; x < 3; ++x) {
     tile[(corner * 3 + x) * kTileStride + cl] = valid ? g[x] : T(0);
     const T d0 = __shfl_sync(0xffffffffu, du[x], src0);
-    T r = du[x] - d0;
-    if (a & 1) r += Ls[0 * 3 + x];
-    if (a & 2) r += Ls[1 * 3 + x];
-    if (a & 4) r += Ls[2 * 3 + x];
-    relt[(corner * 3 + x) * kTileStride + cl] = r;
+    relt[(corner * 3 + x) * kTileStride + cl] = (du[x] - d0) + loff[x];
   }
   if (a == 0) et[cl] = valid ? Ecell : T(0);
   if (valid && a == 0 && ecell) ecell[cell] = (double)Ecell;
