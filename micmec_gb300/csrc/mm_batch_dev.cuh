@@ -472,6 +472,130 @@ __device__ void thermostat(const BArgs& a, Shared<T>& sh, const BSys& sy, const 
   }
 }
 
+// ---- 3x3 algebra of the barostats on warp 0. On this part an FP64 instruction takes the
+// same issue time on its SM sub-partition (~64 cycles) whether one lane or 32 are active,
+// so a one-thread 3x3 product costs 27 such instructions and the CTA waits at the next
+// barrier meanwhile. Here lane e < 9 forms entry e = 3 i + j of each 3x3 result (the same
+// expression, in the same order, as the one-thread forms in mm_control.cuh), and scalars
+// are formed redundantly by every lane. All 32 lanes of warp 0 call these.
+
+__device__ __forceinline__ int wentry() {
+  const int l = threadIdx.x & 31;
+  return l < 9 ? l : 0;
+}
+
+// (A B)[e] from one entry per lane (a = A[e], b = B[e]).
+__device__ __forceinline__ double wmatmul3(double a, double b) {
+  const int e = wentry(), i = e / 3, j = e % 3;
+  const double a0 = __shfl_sync(0xffffffffu, a, 3 * i), a1 = __shfl_sync(0xffffffffu, a, 3 * i + 1),
+               a2 = __shfl_sync(0xffffffffu, a, 3 * i + 2);
+  const double b0 = __shfl_sync(0xffffffffu, b, j), b1 = __shfl_sync(0xffffffffu, b, 3 + j),
+               b2 = __shfl_sync(0xffffffffu, b, 6 + j);
+  return a0 * b0 + a1 * b1 + a2 * b2;
+}
+
+// norm1_3 (largest column sum of |A|) from one entry per lane; every lane gets it. The
+// column sums are non-negative, so their largest is taken on the bit patterns.
+__device__ __forceinline__ double wnorm1(double a) {
+  const int l = threadIdx.x & 31, cj = l < 3 ? l : 0;
+  const double x = fabs(a);
+  const double col = __shfl_sync(0xffffffffu, x, cj) + __shfl_sync(0xffffffffu, x, 3 + cj) +
+                     __shfl_sync(0xffffffffu, x, 6 + cj);
+  const long long b = __double_as_longlong(col);
+  const long long b0 = __shfl_sync(0xffffffffu, b, 0), b1 = __shfl_sync(0xffffffffu, b, 1),
+                  b2 = __shfl_sync(0xffffffffu, b, 2);
+  return __longlong_as_double(max(b0, max(b1, b2)));
+}
+
+// Entry e of exp(f S) from s = S[e] (sym_exp: scaling and squaring of the Taylor series).
+__device__ __forceinline__ double wsym_exp(double s, double f) {
+  const int e = wentry();
+  double A = f * s;
+  int k = 0;
+  double nrm = wnorm1(A);
+  while (nrm > 0.125 && k < 64) {
+    A *= 0.5;
+    nrm *= 0.5;
+    ++k;
+  }
+  double term = (e % 4 == 0) ? 1.0 : 0.0, r = term;
+  for (int n = 1; n <= 20; ++n) {
+    const double t = wmatmul3(term, A);
+    const double inv = 1.0 / n;
+    term = t * inv;
+    r += term;
+    if (wnorm1(term) <= 1e-18 * wnorm1(r)) break;
+  }
+  for (int q = 0; q < k; ++q) r = wmatmul3(r, r);
+  return r;
+}
+
+// update_baro_vel with lane e updating c[C_VP + e].
+__device__ __forceinline__ void wupdate_baro_vel(double* c, const BMD& p, bool chain, double cv0, const double* z6) {
+  const int l = threadIdx.x & 31, e = wentry(), i = e / 3, j = e % 3;
+  const double dt = p.dt;
+  double vp = c[C_VP + e];
+  const double fric = z6 ? exp(-dt / (8 * c[C_BTAU])) : 1.0;
+  if (z6) vp *= fric;
+  if (chain) vp *= exp(-dt * cv0 / 8);
+  const double pt_ij = c[C_KT + e] - c[C_VT + e];
+  const double pt_ji = c[C_KT + j * 3 + i] - c[C_VT + j * 3 + i];
+  const double ps = 0.5 * (pt_ji + pt_ij);
+  const double diag = 2.0 * c[C_EKIN] / c[C_NDOF] - p.press * c[C_VOL];
+  double R = 0.0;
+  if (z6) {
+    const double sc = sqrt(2 * c[C_MPRESS] * kBoltzmannHa * c[C_BTEMP] / (dt * c[C_BTAU]));
+    const int mx = i > j ? i : j, mn = i > j ? j : i, tri = mx * (mx + 1) / 2 + mn;  // lower-triangle slot
+    double z = z6[0];
+#pragma unroll
+    for (int t = 1; t < 6; ++t)
+      if (tri == t) z = z6[t];
+    R = z * sc;
+  }
+  const double Gi = (ps + ((e % 4 == 0) ? diag : 0.0)) / c[C_MPRESS];
+  if (z6) vp += (Gi - R / c[C_MPRESS]) * dt / 4;
+  else vp += Gi * dt / 4;
+  if (z6) vp *= fric;
+  if (chain) vp *= exp(-dt * cv0 / 8);
+  __syncwarp();
+  if (l < 9) c[C_VP + e] = vp;
+  __syncwarp();
+}
+
+// berendsen_mu, entry e on lane e.
+__device__ __forceinline__ double wberendsen_mu(const double* c, const BMD& p) {
+  const int e = wentry(), i = e / 3, j = e % 3;
+  auto m = [&](int k) {
+    const double ptens = (c[C_KT + k] - c[C_VT + k]) / c[C_VOL];
+    const double dmu = p.dt / c[C_MPRESS] * (((k % 4 == 0) ? p.press : 0.0) - ptens);
+    return ((k % 4 == 0) ? 1.0 : 0.0) - dmu;
+  };
+  return 0.5 * (m(i * 3 + j) + m(j * 3 + i));
+}
+
+// scale_domain: L <- L M, rv <- rv M (lane e: entry e), volume from the new rv.
+__device__ __forceinline__ void wscale_domain(double* c, const double* M) {
+  const int l = threadIdx.x & 31, e = wentry(), i = e / 3, j = e % 3;
+  double sl = 0.0, sr = 0.0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    sl += c[C_L + i * 3 + k] * M[k * 3 + j];
+    sr += c[C_RV + i * 3 + k] * M[k * 3 + j];
+  }
+  __syncwarp();
+  if (l < 9) {
+    c[C_L + e] = sl;
+    c[C_RV + e] = sr;
+  }
+  __syncwarp();
+  const double* r = c + C_RV;
+  const double vol = fabs(r[0] * (r[4] * r[8] - r[5] * r[7]) + r[1] * (r[5] * r[6] - r[3] * r[8]) +
+                          r[2] * (r[3] * r[7] - r[4] * r[6]));
+  __syncwarp();
+  if (l == 0) c[C_VOL] = vol;
+  __syncwarp();
+}
+
 // MTK half step (MTKBarostat.baro, npt.py:653-736): barostat velocity, position and
 // domain scaling, force evaluation, velocity scaling, barostat velocity again. With
 // BA_LANGEVIN the barostat-velocity updates carry the Langevin barostat's friction and
@@ -482,23 +606,25 @@ __device__ void baro_half(const BArgs& a, Shared<T>& sh, const BSys& sy, const B
   double* c = sh.ctl;
   const long long N3 = a.Ntot;
   const bool lang = p.baro == BA_LANGEVIN;
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 32) {
     double z6[6];
     if (lang) lbaro_draws(p, sys, a.nsys, step, call0, z6);
-    update_baro_vel(c, p, chain, chain ? *cv0p : 0.0, lang ? z6 : nullptr);
-    sym_exp(c + C_VP, p.dt / 2, sh.mat);
-    scale_domain(c, sh.mat);
+    wupdate_baro_vel(c, p, chain, chain ? *cv0p : 0.0, lang ? z6 : nullptr);
+    const double r = wsym_exp(c[C_VP + wentry()], p.dt / 2);
+    if (threadIdx.x < 9) sh.mat[threadIdx.x] = r;
+    __syncwarp();
+    wscale_domain(c, sh.mat);
   }
   __syncthreads();
   positions<T>(a, sy, sh.mat, 0.0);
   refresh_B<T>(sh, a.tt, a.ntypes, c + C_L);
   __syncthreads();
   forces<T, MODEL>(a, sh, sy);
-  if (threadIdx.x == 0) {
-    double S[9];
+  if (threadIdx.x < 32) {
+    const int e = wentry();
     const double tr = c[C_VP + 0] + c[C_VP + 4] + c[C_VP + 8];
-    for (int i = 0; i < 9; ++i) S[i] = c[C_VP + i] + ((i % 4 == 0) ? tr / c[C_NDOF] : 0.0);
-    sym_exp(S, -p.dt / 2, sh.mat);
+    const double r = wsym_exp(c[C_VP + e] + ((e % 4 == 0) ? tr / c[C_NDOF] : 0.0), -p.dt / 2);
+    if (threadIdx.x < 9) sh.mat[threadIdx.x] = r;
   }
   __syncthreads();
   // v <- v R; the kinetic tensor follows as R^T K R (no second sum over the nodes)
@@ -510,20 +636,23 @@ __device__ void baro_half(const BArgs& a, Shared<T>& sh, const BSys& sy, const B
     a.v[N3 + g] = y;
     a.v[2 * N3 + g] = z;
   }
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 32) {
+    // K <- sym(R^T (K R)), entry e on lane e
+    const int e = wentry(), i = e / 3, j = e % 3;
     const double* R = sh.mat;
-    double KR[9], K2[9];
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j)
-        KR[i * 3 + j] = c[C_KT + i * 3] * R[j] + c[C_KT + i * 3 + 1] * R[3 + j] + c[C_KT + i * 3 + 2] * R[6 + j];
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) K2[i * 3 + j] = R[i] * KR[j] + R[3 + i] * KR[3 + j] + R[6 + i] * KR[6 + j];
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) c[C_KT + i * 3 + j] = 0.5 * (K2[i * 3 + j] + K2[j * 3 + i]);
-    c[C_EKIN] = 0.5 * (c[C_KT + 0] + c[C_KT + 4] + c[C_KT + 8]);
+    const double KR = wmatmul3(c[C_KT + e], R[e]);
+    const double K2 = wmatmul3(R[j * 3 + i], KR);
+    const double kt = 0.5 * (K2 + __shfl_sync(0xffffffffu, K2, j * 3 + i));
+    __syncwarp();
+    if (threadIdx.x < 9) c[C_KT + e] = kt;
+    __syncwarp();
+    const double ek = 0.5 * (c[C_KT + 0] + c[C_KT + 4] + c[C_KT + 8]);
+    __syncwarp();
+    if (threadIdx.x == 0) c[C_EKIN] = ek;
+    __syncwarp();
     double z6[6];
     if (lang) lbaro_draws(p, sys, a.nsys, step, call0 + 1, z6);
-    update_baro_vel(c, p, chain, chain ? *cv0p : 0.0, lang ? z6 : nullptr);
+    wupdate_baro_vel(c, p, chain, chain ? *cv0p : 0.0, lang ? z6 : nullptr);
   }
   __syncthreads();
 }
@@ -533,10 +662,12 @@ __device__ void baro_half(const BArgs& a, Shared<T>& sh, const BSys& sy, const B
 template <typename T, int MODEL>
 __device__ void berendsen_baro(const BArgs& a, Shared<T>& sh, const BSys& sy, const BMD& p) {
   double* c = sh.ctl;
-  if (threadIdx.x == 0) {
-    c[C_SAVE] = c[C_EPOT];
-    berendsen_mu(c, p, sh.mat);
-    scale_domain(c, sh.mat);
+  if (threadIdx.x < 32) {
+    const double mu = wberendsen_mu(c, p);
+    if (threadIdx.x == 0) c[C_SAVE] = c[C_EPOT];
+    if (threadIdx.x < 9) sh.mat[threadIdx.x] = mu;
+    __syncwarp();
+    wscale_domain(c, sh.mat);
   }
   __syncthreads();
   positions<T>(a, sy, sh.mat, 0.0);
