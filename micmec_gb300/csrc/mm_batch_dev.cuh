@@ -163,6 +163,24 @@ __device__ __forceinline__ T from_double(double x) {
   else return x;
 }
 
+// Totals of block_sum_f2_pairs (held by thread 0) in FP64, lane l < NV of warp 0 forming
+// total l (one FP64 add for all of them; the conversions are exact integer-pipe ones).
+// Called by all 32 lanes of warp 0.
+template <int NV>
+__device__ __forceinline__ double f2_total_of_lane(const F2 (&v)[NV]) {
+  const int l = threadIdx.x & 31;
+  float hi = 0.0f, lo = 0.0f;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    const float h = __shfl_sync(0xffffffffu, v[i].hi, 0), w = __shfl_sync(0xffffffffu, v[i].lo, 0);
+    if (l == i) {
+      hi = h;
+      lo = w;
+    }
+  }
+  return f2d(hi) + f2d(lo);
+}
+
 // Energy, virial (into sh.ctl) and node gradient (a.gpos) of system sy.
 template <typename T, int MODEL>
 __device__ void forces(const BArgs& a, Shared<T>& sh, const BSys& sy) {
@@ -242,15 +260,19 @@ __device__ void forces(const BArgs& a, Shared<T>& sh, const BSys& sy) {
         }
     }
   }
-  if (sizeof(T) == 4 && MODEL >= 1) {
-    block_sum_f2<10>(facc, acc, sh.red);
+  // (the CTA sum's barrier also orders every corner-gradient write before the gather)
+  if constexpr (sizeof(T) == 4 && MODEL >= 1) {
+    block_sum_f2_pairs<10>(facc, sh.red);
+    if (threadIdx.x < 32) {
+      const double t = f2_total_of_lane<10>(facc);
+      if (threadIdx.x < 10) sh.ctl[threadIdx.x == 0 ? C_EPOT : C_VT + threadIdx.x - 1] = t;
+    }
   } else {
     cta_sum<10>(acc, sh.red);
-  }
-  // (the CTA sum's barrier also orders every corner-gradient write before the gather)
-  if (threadIdx.x == 0) {
-    sh.ctl[C_EPOT] = acc[0];
-    for (int i = 0; i < 9; ++i) sh.ctl[C_VT + i] = acc[1 + i];
+    if (threadIdx.x == 0) {
+      sh.ctl[C_EPOT] = acc[0];
+      for (int i = 0; i < 9; ++i) sh.ctl[C_VT + i] = acc[1 + i];
+    }
   }
   for (int n = threadIdx.x; n < M; n += blockDim.x) {
     int i, j, k;
@@ -347,19 +369,31 @@ __device__ void kinetic(const BArgs& a, double* ctl, double* red, const BSys& sy
       f[5] += m * w0 * w1;
     }
   }
-  double t6[6];
   if constexpr (sizeof(T) == 4) {
-    block_sum_f2<6>(f, t6, red);
+    block_sum_f2_pairs<6>(f, red);
+    if (threadIdx.x < 32) {
+      // lane l < 6 converts total l; lane l < 9 writes kinetic-tensor entry l
+      // (xx yy zz yz xz xy -> row-major 3x3: source totals 0 5 4 5 1 3 4 3 2)
+      const int l = threadIdx.x;
+      const double t = f2_total_of_lane<6>(f);
+      const int src = (int)((0x234315450ull >> (4 * (l < 9 ? l : 0))) & 15u);
+      const double kv = __shfl_sync(0xffffffffu, t, src);
+      const double ek = 0.5 * (__shfl_sync(0xffffffffu, t, 0) + __shfl_sync(0xffffffffu, t, 1) +
+                               __shfl_sync(0xffffffffu, t, 2));
+      if (l < 9) ctl[C_KT + l] = kv;
+      if (l == 0) ctl[C_EKIN] = ek;
+    }
   } else {
+    double t6[6];
     for (int i = 0; i < 6; ++i) t6[i] = f[i];
     block_sum<6>(t6, red);
-  }
-  if (threadIdx.x == 0) {
-    acc[0] = 0.5 * (t6[0] + t6[1] + t6[2]);
-    for (int i = 0; i < 6; ++i) acc[1 + i] = t6[i];
-    ctl[C_EKIN] = acc[0];
-    const double k[9] = {acc[1], acc[6], acc[5], acc[6], acc[2], acc[4], acc[5], acc[4], acc[3]};
-    for (int i = 0; i < 9; ++i) ctl[C_KT + i] = k[i];
+    if (threadIdx.x == 0) {
+      acc[0] = 0.5 * (t6[0] + t6[1] + t6[2]);
+      for (int i = 0; i < 6; ++i) acc[1 + i] = t6[i];
+      ctl[C_EKIN] = acc[0];
+      const double k[9] = {acc[1], acc[6], acc[5], acc[6], acc[2], acc[4], acc[5], acc[4], acc[3]};
+      for (int i = 0; i < 9; ++i) ctl[C_KT + i] = k[i];
+    }
   }
   __syncthreads();
 }
