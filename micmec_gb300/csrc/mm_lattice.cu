@@ -26,6 +26,7 @@
 #include <cstring>
 #include <string>
 #include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "../../include/micmec_gb300.h"
@@ -269,6 +270,32 @@ constexpr int kTileStride = 44;
 constexpr int kTileElems = (2 * 24) * kTileStride + kCell8Cells;  // tile, relt, et
 static_assert(kCell8Threads == 256 && kCellPart == 10, "component ownership assumes 8 warps and 10 components");
 
+// Programmatic dependent launch of the step kernels (k_cells8, k_md_nodes; launch_pdl):
+// such a grid may be scheduled while the kernel before it on the stream is still running.
+// Every thread first waits until that kernel has completed and its writes are visible
+// (griddepcontrol.wait), before any global access, so the order of reads and writes is
+// that of a plain launch; it then lets the next kernel's blocks be scheduled. Launched
+// without the attribute, both instructions do nothing.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t st, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
+
 template <typename T, bool STRUCT, bool SIMPLE>
 __global__ void __launch_bounds__(kCell8Threads, sizeof(T) == 4 ? 3 : 2) k_cells8(Topo t, const TypeTable* __restrict__ tt, int ntypes,
                                                           const double* __restrict__ box, const T* __restrict__ disp,
@@ -281,6 +308,7 @@ __global__ void __launch_bounds__(kCell8Threads, sizeof(T) == 4 ? 3 : 2) k_cells
   T* const buf0 = reinterpret_cast<T*>(smem_raw + tp_bytes);
   constexpr int kBuf = kTileElems;
   __shared__ T Ls[9];
+  pdl_enter();
   load_params<T>(tp, tt, ntypes, box);
   if (threadIdx.x < 9) Ls[threadIdx.x] = (T)box[threadIdx.x];
   __syncthreads();
@@ -515,6 +543,7 @@ __global__ void __launch_bounds__(kMDThreads, 1) k_md_nodes(Topo t, MDArgs p, co
   __shared__ double ctot[kCellPart];
   __shared__ bool last;
   extern __shared__ __align__(16) float md_stage[];  // FP32 cells: per-thread input slots (kMDStageBytes)
+  pdl_enter();
   // blocks 0 .. nb-1 update the nodes; block nb (the last one) sums the cell kernel's
   // partials meanwhile, so the block that finishes last has only nb node partials left
   const int nb = gridDim.x - 1;
@@ -917,11 +946,11 @@ static void launch_cells_t(mm_handle* h, cudaStream_t st, double* ecell) {
   const int nblk = cell_grid(h);
   if constexpr (MODEL == 1) {
     if (h->simple)
-      k_cells8<T, STRUCT, true><<<nblk, kCell8Threads, cell_smem(h), st>>>(
-          t, h->d_tt, h->ntypes, h->d_box, (const T*)h->d_disp, (T*)h->d_G, ecell, h->d_cpart);
+      launch_pdl(k_cells8<T, STRUCT, true>, nblk, kCell8Threads, cell_smem(h), st, t, (const TypeTable*)h->d_tt,
+                 h->ntypes, (const double*)h->d_box, (const T*)h->d_disp, (T*)h->d_G, ecell, h->d_cpart);
     else
-      k_cells8<T, STRUCT, false><<<nblk, kCell8Threads, cell_smem(h), st>>>(
-          t, h->d_tt, h->ntypes, h->d_box, (const T*)h->d_disp, (T*)h->d_G, ecell, h->d_cpart);
+      launch_pdl(k_cells8<T, STRUCT, false>, nblk, kCell8Threads, cell_smem(h), st, t, (const TypeTable*)h->d_tt,
+                 h->ntypes, (const double*)h->d_box, (const T*)h->d_disp, (T*)h->d_G, ecell, h->d_cpart);
   } else {
     k_cells<T, MODEL, STRUCT><<<nblk, kCellThreads, cell_smem(h), st>>>(
         t, h->d_tt, h->ntypes, h->d_box, (const T*)h->d_disp, (T*)h->d_G, ecell, h->d_cpart);
@@ -1031,9 +1060,10 @@ static void launch_md_nodes_t(mm_handle* h, const MDArgs& a, const double* noise
     if (smem) cudaFuncSetAttribute(k_md_nodes<T, STRUCT, THERMO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     occ = occupancy_of(k_md_nodes<T, STRUCT, THERMO>, kMDThreads, smem);
   }
-  k_md_nodes<T, STRUCT, THERMO><<<node_grid(h, THERMO) + 1, kMDThreads, smem, st>>>(
-      t, a, (const T*)h->d_G, h->d_u, h->d_v, (T*)h->d_disp, h->d_mass, h->d_invm, h->d_c2, noise, h->d_npart,
-      h->d_cpart, cell_grid(h), h->d_ticket, h->d_carry, record, gpos_out, h->d_nodef);
+  launch_pdl(k_md_nodes<T, STRUCT, THERMO>, node_grid(h, THERMO) + 1, kMDThreads, smem, st, t, a, (const T*)h->d_G,
+             h->d_u, h->d_v, (T*)h->d_disp, (const double*)h->d_mass, (const double*)h->d_invm,
+             (const double*)h->d_c2, noise, h->d_npart, (const double*)h->d_cpart, cell_grid(h), h->d_ticket,
+             h->d_carry, record, gpos_out, (const float4*)h->d_nodef);
 }
 
 // Node-update grid: at most one block per kMDThreads nodes, and one block fewer than fit
