@@ -305,7 +305,8 @@ mm_status mm_batch_relax(mm_batch* b, int max_iter, double gtol, void* stream);
  */
 mm_status mm_batch_relax_cell(mm_batch* b, int max_iter, double gtol, double stol, double press, int full,
                               void* stream);
-/* Choose CTA size and persistent CTA count by timing probe_steps MD steps (state restored). */
+/* Choose the CTA size (128/256) and the CTA count (1, 2, 4 per SM or one per system; the default
+   after mm_batch_create is one per system) by timing probe_steps MD steps (state restored). */
 mm_status mm_batch_autotune(mm_batch* b, int probe_steps, double timestep, int thermo, double temp, double timecon,
                             int baro, double press, int chain, double* best_ms);
 mm_status mm_batch_config(mm_batch* b, int* cta_threads, int* nctas);

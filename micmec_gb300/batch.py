@@ -6,8 +6,9 @@
 (none / Langevin / Nose-Hoover chain thermostat, optionally the anisotropic MTK
 barostat) in one persistent kernel (optionally replayed from a CUDA graph);
 ``relax`` minimises every system's energy over node positions with nonlinear
-conjugate gradients; ``autotune`` picks the CTA size and the number of
-persistent CTAs by timing.
+conjugate gradients. By default every system is its own CTA (launched longest
+first); ``autotune`` picks the CTA size (128 or 256 threads) and the number of
+CTAs (1, 2 or 4 per SM, or one per system) by timing.
 
 The hook constants are set up the way the reference's hook ``init`` methods set
 them (micmec/sampling/nvt.py:393-400, 507-523; npt.py:82-97, 579-614):
