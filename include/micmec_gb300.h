@@ -349,6 +349,14 @@ const char* mm_version(void);
  */
 mm_status mm_selftest_convert(const double* din, float* dout, const float* fin, double* fout, int n, void* stream);
 
+/*
+ * Self-test of the batch kernels' warp-parallel 3x3 algebra: the matrix exponential
+ * R = exp(f S) of n row-major 3x3 matrices S (9 doubles each) by the one-thread form
+ * (r_thread) and by the form with lane e of a warp forming entry e (r_warp); the two are
+ * the same expressions in the same order and agree bit for bit. All pointers device.
+ */
+mm_status mm_selftest_sym_exp(const double* S, int n, double f, double* r_thread, double* r_warp, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -50,13 +50,14 @@ def _declare(L):
     L.mm_md_engine.argtypes = [c_void_p, P, P, c_int, c_double, c_int, c_double, c_double, c_int, c_double, c_int,
                                c_uint64, P, P, P, P, c_int64, c_void_p]
     L.mm_selftest_convert.argtypes = [P, P, P, P, c_int, c_void_p]
+    L.mm_selftest_sym_exp.argtypes = [P, c_int, c_double, P, P, c_void_p]
     L.mm_build_topology.argtypes = [P, c_int, c_int, c_int, P, P, c_int, P, P, P, P, P, P, P, P, c_void_p]
     L.mm_last_error.restype = ctypes.c_char_p
     L.mm_version.restype = ctypes.c_char_p
     for name in ("mm_create", "mm_destroy", "mm_set_domain", "mm_compute", "mm_compute_host", "mm_cell_results",
                  "mm_md_run", "mm_md_begin", "mm_md_advance", "mm_md_end", "mm_md_step_host",
                  "mm_md_time_kernels", "mm_set_params", "mm_adjoint", "mm_md_engine", "mm_selftest_convert",
-                 "mm_build_topology"):
+                 "mm_selftest_sym_exp", "mm_build_topology"):
         getattr(L, name).restype = c_int
 
 

@@ -498,6 +498,16 @@ mm_status mm_batch_autotune(mm_batch* b, int probe_steps, double timestep, int t
   return s;
 }
 
+mm_status mm_selftest_sym_exp(const double* S, int n, double f, double* r_thread, double* r_warp, void* stream) {
+  if (n < 0 || (n > 0 && (!S || !r_thread || !r_warp))) {
+    mm::set_error("mm_selftest_sym_exp: bad arguments");
+    return MM_ERR_ARG;
+  }
+  if (n > 0) mmb::k_selftest_sym_exp<<<n, 32, 0, (cudaStream_t)stream>>>(S, n, f, r_thread, r_warp);
+  BCUDA(cudaGetLastError());
+  return MM_OK;
+}
+
 mm_status mm_batch_config(mm_batch* b, int* cta_threads, int* nctas) {
   if (!b) return MM_ERR_ARG;
   if (cta_threads) *cta_threads = b->bt;

@@ -509,9 +509,10 @@ __device__ void thermostat(const BArgs& a, Shared<T>& sh, const BSys& sy, const 
 // ---- 3x3 algebra of the barostats on warp 0. On this part an FP64 instruction takes the
 // same issue time on its SM sub-partition (~64 cycles) whether one lane or 32 are active,
 // so a one-thread 3x3 product costs 27 such instructions and the CTA waits at the next
-// barrier meanwhile. Here lane e < 9 forms entry e = 3 i + j of each 3x3 result (the same
-// expression, in the same order, as the one-thread forms in mm_control.cuh), and scalars
-// are formed redundantly by every lane. All 32 lanes of warp 0 call these.
+// barrier meanwhile. Here lane e < 9 forms entry e = 3 i + j of each 3x3 result (the
+// expressions of the one-thread forms in mm_control.cuh; the matrix exponential with the
+// same explicitly fused steps, so its two forms agree bit for bit), and scalars are formed
+// redundantly by every lane. All 32 lanes of warp 0 call these.
 
 __device__ __forceinline__ int wentry() {
   const int l = threadIdx.x & 31;
@@ -525,7 +526,7 @@ __device__ __forceinline__ double wmatmul3(double a, double b) {
                a2 = __shfl_sync(0xffffffffu, a, 3 * i + 2);
   const double b0 = __shfl_sync(0xffffffffu, b, j), b1 = __shfl_sync(0xffffffffu, b, 3 + j),
                b2 = __shfl_sync(0xffffffffu, b, 6 + j);
-  return a0 * b0 + a1 * b1 + a2 * b2;
+  return fma(a2, b2, fma(a1, b1, __dmul_rn(a0, b0)));  // the rounding steps of matmul3
 }
 
 // norm1_3 (largest column sum of |A|) from one entry per lane; every lane gets it. The
@@ -556,8 +557,8 @@ __device__ __forceinline__ double wsym_exp(double s, double f) {
   for (int n = 1; n <= 20; ++n) {
     const double t = wmatmul3(term, A);
     const double inv = 1.0 / n;
-    term = t * inv;
-    r += term;
+    term = __dmul_rn(t, inv);
+    r = __dadd_rn(r, term);
     if (wnorm1(term) <= 1e-18 * wnorm1(r)) break;
   }
   for (int q = 0; q < k; ++q) r = wmatmul3(r, r);
@@ -628,6 +629,17 @@ __device__ __forceinline__ void wscale_domain(double* c, const double* M) {
   __syncwarp();
   if (l == 0) c[C_VOL] = vol;
   __syncwarp();
+}
+
+// Self-test of the warp form: exp(f S) of n 3x3 matrices (row-major, 9 doubles each) by
+// sym_exp on one thread (r_thread) and by wsym_exp on the warp (r_warp); one 32-thread
+// block per matrix (mm_selftest_sym_exp).
+__global__ void k_selftest_sym_exp(const double* S, int n, double f, double* r_thread, double* r_warp) {
+  const int m = blockIdx.x;
+  if (m >= n) return;
+  if (threadIdx.x == 0) sym_exp(S + 9 * m, f, r_thread + 9 * m);
+  const double r = wsym_exp(S[9 * m + wentry()], f);
+  if (threadIdx.x < 9) r_warp[9 * m + threadIdx.x] = r;
 }
 
 // MTK half step (MTKBarostat.baro, npt.py:653-736): barostat velocity, position and

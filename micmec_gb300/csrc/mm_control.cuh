@@ -149,9 +149,12 @@ __device__ inline double norm1_3(const double* A) {
   }
   return m;
 }
+// C = A B; each entry with explicitly fused steps (a0 b0, then + a1 b1, then + a2 b2), so
+// that the one-entry-per-lane form of the batch kernels rounds identically.
 __device__ inline void matmul3(const double* A, const double* B, double* C) {
   for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) C[i * 3 + j] = A[i * 3] * B[j] + A[i * 3 + 1] * B[3 + j] + A[i * 3 + 2] * B[6 + j];
+    for (int j = 0; j < 3; ++j)
+      C[i * 3 + j] = fma(A[i * 3 + 2], B[6 + j], fma(A[i * 3 + 1], B[3 + j], __dmul_rn(A[i * 3], B[j])));
 }
 
 // R = exp(f S) for a symmetric 3x3 S: the matrix exponential the reference forms from
@@ -177,8 +180,8 @@ __device__ inline void sym_exp(const double* S, double f, double* R) {
     matmul3(term, A, tmp);
     const double inv = 1.0 / n;
     for (int i = 0; i < 9; ++i) {
-      term[i] = tmp[i] * inv;
-      R[i] += term[i];
+      term[i] = __dmul_rn(tmp[i], inv);  // not fused with the sum below
+      R[i] = __dadd_rn(R[i], term[i]);
     }
     if (norm1_3(term) <= 1e-18 * norm1_3(R)) break;
   }
