@@ -5,7 +5,8 @@
  * The reference (molmod/micmec) is a Python package; its force path is the
  * `ForcePart.compute(gpos, vtens)` call of micmec/pes/mmff.py:87-149 and the
  * Verlet loop of micmec/sampling/verlet.py:140-166. This library is what a
- * binding of that path calls (see INTEGRATION.md for the ctypes binding).
+ * binding of that path calls (the package's micmec_gb300/_native.py binds it with
+ * ctypes).
  *
  * Conventions
  *  - All quantities are in atomic units and FP64 at the boundary.
@@ -193,16 +194,20 @@ mm_status mm_md_step_host(mm_handle* h, double* pos, double* vel, double* gpos, 
  * numbered as the reference's Grid does), and calls no cudaMalloc/cudaFree.
  *  lattice_shape[3]  : host, cells per direction (each >= 2), at most
  *                      MM_NOALLOC_MAX_CELLS cells in total (larger lattices: MM_ERR_ARG).
- *  cell_type (M)     : device int32, 0-based type index per cell.
+ *  cell_type (M)     : device int32, 0-based type index per cell; a type outside
+ *                      [0, ntypes) is found on the device and returned as MM_ERR_ARG
+ *                      before any energy is evaluated.
  *  ntypes, nstates, h0, C, free_energy, temp_eff : host, as mm_create.
  *  rvecs (3,3)       : host domain vectors.
  *  pos (N,3)         : device.  gpos (N,3), vtens (3,3): device or NULL, ADDED to.
  *  energy            : device double[1], written.
  * Working memory is one static device array of MM_NOALLOC_SCRATCH_BYTES bytes per
  * GPU, held until the process exits. The first call on a device looks up the
- * array's address (make it before any stream capture). Calls share the array:
- * calls that overlap on the GPU race. The call synchronises `stream` before it
- * returns.
+ * array's address (make it before any stream capture); the address is kept for the
+ * process's life, so a process that calls cudaDeviceReset does not use this entry
+ * point afterwards. Calls share the array: calls that overlap on the GPU race. The
+ * call synchronises `stream` before it returns. Returns MM_ERR_NAN when the energy,
+ * gradient or virial holds a NaN (as mm_compute_host).
  */
 #define MM_NOALLOC_MAX_CELLS 32768
 #define MM_NOALLOC_SCRATCH_BYTES (8u << 20)

@@ -41,7 +41,7 @@ def load_chk(fn):
             result[name] = tail.strip().lower() in ("true", "1")
         elif kind == "none":
             result[name] = None
-        elif kind in ("intar", "fltar", "blnar"):
+        elif kind in ("intar", "fltar", "blnar", "strar"):
             shape = tuple(int(s) for s in tail.split(",")) if tail else (0,)
             size = int(np.prod(shape)) if shape else 1
             words = []
@@ -52,6 +52,8 @@ def load_chk(fn):
                 arr = np.array([int(w) for w in words[:size]], dtype=np.int64)
             elif kind == "fltar":
                 arr = np.array([float(w) for w in words[:size]], dtype=np.float64)
+            elif kind == "strar":  # right-aligned words without blanks (atom type names)
+                arr = np.array(words[:size], dtype=object)
             else:
                 arr = np.array([w.lower() in ("true", "1") for w in words[:size]])
             result[name] = arr.reshape(shape)

@@ -6,7 +6,7 @@
 // owns every device allocation, or code paths where an allocation would
 // synchronise the device at the wrong moment. mm_create allocates a handle's
 // buffers, so those callers cannot use it. This entry point takes everything it
-// needs from the caller's buffers and keeps its working memory (node
+// needs from the caller's buffers and keeps its working memory (status words, node
 // displacements, corner gradients, block partial sums, the parameter table) in
 // one file-scope __device__ array, g_noalloc_scratch, of MM_NOALLOC_SCRATCH_BYTES
 // bytes. Every GPU that loads the library holds that array until the process
@@ -15,10 +15,19 @@
 // Set-up: the first call on each device looks up the array's device address with
 // cudaGetSymbolAddress while that device is current (the array's name in host code
 // is only a host-side stand-in, not a device address). Make that first call before
-// any stream capture. Every call shares the one array and leaves its contents
-// behind; everything a call needs is rewritten or cleared by that call. Calls whose
-// work overlaps on the GPU (different streams or host threads, same device) race
-// on the array and must be serialised by the caller.
+// any stream capture. The address is kept for the life of the process: after a
+// cudaDeviceReset the module is loaded again and the kept address is stale, so a
+// process that resets a device does not call this entry point afterwards.
+//
+// Every call shares the one array and leaves its contents behind; everything a call
+// needs is rewritten or cleared by that call (the status words are cleared first).
+// Calls whose work overlaps on the GPU (different streams or host threads, same
+// device) race on the array and must be serialised by the caller.
+//
+// Checks on the device: cell types outside [0, ntypes) are found by the kernel that
+// narrows them to bytes; the call reads that verdict back and returns MM_ERR_ARG
+// before any kernel indexes the parameter table with them. A NaN in the energy,
+// gradient or virial is returned as MM_ERR_NAN, as mm_compute_host does.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -46,9 +55,14 @@ size_t round_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 mm_status scratch_address(unsigned char** out) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+  if (e != cudaSuccess) {
     mm::set_error(std::string("mm_compute_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
     return MM_ERR_CUDA;
+  }
+  if (dev < 0 || dev >= kMaxDevices) {
+    mm::set_error("mm_compute_noalloc: device index " + std::to_string(dev) + " is beyond the " +
+                  std::to_string(kMaxDevices) + " devices this entry point keeps addresses for");
+    return MM_ERR_ARG;
   }
   std::lock_guard<std::mutex> lock(g_setup_mutex);
   if (!g_scratch_ptr[dev]) {
@@ -93,9 +107,20 @@ void stress_map(const double* C, double* A) {
     }
 }
 
-__global__ void k_types_to_u8(int M, const int32_t* __restrict__ in, uint8_t* __restrict__ out) {
+// Status words at the start of the scratch array: [0] a cell type outside [0, ntypes)
+// was seen, [1] a NaN was produced (set by the gather and finalize kernels).
+constexpr int kStatusWords = 2;
+
+// Cell types narrowed to bytes; an out-of-range type is stored as 0 (so nothing reads
+// beyond the parameter table) and reported through bad[0].
+__global__ void k_types_to_u8(int M, int ntypes, const int32_t* __restrict__ in, uint8_t* __restrict__ out,
+                              int* __restrict__ bad) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c < M) out[c] = (uint8_t)in[c];
+  if (c >= M) return;
+  const int32_t t = in[c];
+  const bool ok = t >= 0 && t < ntypes;
+  out[c] = ok ? (uint8_t)t : (uint8_t)0;
+  if (!ok) atomicOr(bad, 1);
 }
 
 }  // namespace
@@ -155,6 +180,7 @@ extern "C" mm_status mm_compute_noalloc(const int32_t* lattice_shape, const int3
     off += round_up(bytes);
     return p;
   };
+  int* d_status = (int*)carve(kStatusWords * sizeof(int));
   h.d_u = (double*)carve(3 * M * sizeof(double));
   h.d_disp = carve(3 * M * esz);
   h.d_G = carve(24 * M * esz);
@@ -194,21 +220,44 @@ extern "C" mm_status mm_compute_noalloc(const int32_t* lattice_shape, const int3
     mm::set_error(std::string("mm_compute_noalloc: parameter upload: ") + cudaGetErrorString(e));
     return MM_ERR_CUDA;
   }
-  k_types_to_u8<<<(int)((M + 255) / 256), 256, 0, st>>>((int)M, cell_type, h.d_cell_type);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_status, 0, kStatusWords * sizeof(int), st);
+  if (e != cudaSuccess) {
+    mm::set_error(std::string("mm_compute_noalloc: parameter upload: ") + cudaGetErrorString(e));
+    return MM_ERR_CUDA;
+  }
+  // Types first: their verdict is read back before any kernel indexes the parameter table.
+  k_types_to_u8<<<(int)((M + 255) / 256), 256, 0, st>>>((int)M, ntypes, cell_type, h.d_cell_type, d_status);
+  int status[kStatusWords] = {0, 0};
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(status, d_status, sizeof(status), cudaMemcpyDeviceToHost, st);
+  // This also waits for the parameter copies, which read host stack memory.
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    mm::set_error(std::string("mm_compute_noalloc: ") + cudaGetErrorString(e));
+    return MM_ERR_CUDA;
+  }
+  if (status[0]) {
+    mm::set_error("mm_compute_noalloc: a cell type is outside [0, ntypes)");
+    return MM_ERR_ARG;
+  }
   mm::launch_pos_to_state(&h, pos, st);
   mm::launch_cells(&h, st, nullptr);
-  if (gpos) mm::launch_gather(&h, gpos, nullptr, st);
-  mm::launch_finalize(&h, energy, vtens, nullptr, st);
+  if (gpos) mm::launch_gather(&h, gpos, d_status + 1, st);
+  mm::launch_finalize(&h, energy, vtens, d_status + 1, st);
   e = cudaGetLastError();
   if (e != cudaSuccess) {
     mm::set_error(std::string("mm_compute_noalloc: launch: ") + cudaGetErrorString(e));
     return MM_ERR_CUDA;
   }
-  // The parameter copies read host stack memory: wait for them before it goes away.
-  e = cudaStreamSynchronize(st);
+  e = cudaMemcpyAsync(status, d_status, sizeof(status), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
     mm::set_error(std::string("mm_compute_noalloc: ") + cudaGetErrorString(e));
     return MM_ERR_CUDA;
+  }
+  if (status[1]) {
+    mm::set_error("mm_compute_noalloc: NaN in energy, gradient or virial");
+    return MM_ERR_NAN;
   }
   return MM_OK;
 }

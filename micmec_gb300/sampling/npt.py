@@ -20,7 +20,7 @@ from micmec_gb300.sampling.utils import (
     domain_symmetrize, get_random_vel_press, get_ndof_internal_md, clean_momenta, get_ndof_baro,
 )
 from micmec_gb300.sampling.verlet import VerletHook
-from micmec_gb300.sampling.nvt import NHCThermostat, LangevinThermostat, BerendsenThermostat
+from micmec_gb300.sampling.nvt import NHCThermostat, LangevinThermostat, BerendsenThermostat, find_hook
 
 __all__ = ["TBCombination", "BerendsenBarostat", "LangevinBarostat", "MTKBarostat", "MTKAttributeStateItem"]
 
@@ -396,26 +396,19 @@ class MTKBarostat(VerletHook):
 
 
 class MTKAttributeStateItem(StateItem):
+    """Recorded MTK barostat variable under the key baro_<attr>: an attribute of the barostat
+    ("vel_press", "mass_press", ...) or, for attr "chain_<name>", the variable <name> of the
+    barostat's own Nose-Hoover chain (0 when it has none)."""
+
     def __init__(self, attr):
-        StateItem.__init__(self, "baro_" + attr)
         self.attr = attr
+        StateItem.__init__(self, "baro_" + attr)
 
     def get_value(self, iterative):
-        baro = None
-        for hook in iterative.hooks:
-            if isinstance(hook, MTKBarostat):
-                baro = hook
-                break
-            if isinstance(hook, TBCombination) and isinstance(hook.barostat, MTKBarostat):
-                baro = hook.barostat
-                break
+        baro = find_hook(iterative, MTKBarostat, "barostat")
         if baro is None:
-            raise TypeError("Iterative does not contain an MTKBarostat hook.")
-        if self.key.startswith("baro_chain_"):
-            if baro.baro_thermo is None:
-                return 0
-            return getattr(baro.baro_thermo.chain, self.key.split("_")[2])
+            raise TypeError("No MTKBarostat among the iterative's hooks: baro_%s cannot be recorded." % self.attr)
+        if self.attr.startswith("chain_"):
+            chain_attr = self.attr[len("chain_"):]
+            return 0 if baro.baro_thermo is None else getattr(baro.baro_thermo.chain, chain_attr)
         return getattr(baro, self.attr)
-
-    def copy(self):
-        return self.__class__(self.attr)

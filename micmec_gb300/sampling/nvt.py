@@ -340,20 +340,26 @@ class NHCThermostat(VerletHook):
         self.econs_correction = self.chain.get_econs_correction()
 
 
+def find_hook(iterative, cls, role):
+    """The hook of type ``cls`` among the iterative's hooks, also when it sits inside a
+    TBCombination under the attribute ``role`` ("thermostat" / "barostat"); None if absent."""
+    for hook in iterative.hooks:
+        for candidate in (hook, getattr(hook, role, None)):
+            if isinstance(candidate, cls):
+                return candidate
+    return None
+
+
 class NHCAttributeStateItem(StateItem):
+    """Recorded Nose-Hoover chain variable (``attr`` "pos", "vel", "masses", ...) under the key
+    thermo_<attr>, for trajectories of NHC runs."""
+
     def __init__(self, attr):
-        StateItem.__init__(self, "thermo_" + attr)
         self.attr = attr
+        StateItem.__init__(self, "thermo_" + attr)
 
     def get_value(self, iterative):
-        from micmec_gb300.sampling.npt import TBCombination
-
-        for hook in iterative.hooks:
-            if isinstance(hook, NHCThermostat):
-                return getattr(hook.chain, self.attr)
-            if isinstance(hook, TBCombination) and isinstance(hook.thermostat, NHCThermostat):
-                return getattr(hook.thermostat.chain, self.attr)
-        raise TypeError("Iterative does not contain a NHCThermostat hook.")
-
-    def copy(self):
-        return self.__class__(self.attr)
+        thermo = find_hook(iterative, NHCThermostat, "thermostat")
+        if thermo is None:
+            raise TypeError("No NHCThermostat among the iterative's hooks: thermo_%s cannot be recorded." % self.attr)
+        return getattr(thermo.chain, self.attr)

@@ -43,11 +43,12 @@ def angular_moment(pos, vel, masses):
     return np.einsum("i,ij->j", masses, np.cross(pos, vel))
 
 
-def angular_velocity(amom, itens, epsilon=1e-6):
-    """Solve I w = L, ignoring near-singular directions (linear/planar bodies)."""
+def angular_velocity(amom, itens, epsilon=1e-10):
+    """Solve I w = L on the eigenvectors of I whose eigenvalue exceeds epsilon (a pseudo-inverse
+    for linear bodies; utils.py:229-270)."""
     evals, evecs = np.linalg.eigh(itens)
-    inv = np.array([1.0 / e if abs(e) > epsilon * max(1.0, abs(evals).max()) else 0.0 for e in evals])
-    return evecs @ (inv * (evecs.T @ amom))
+    keep = evals > epsilon
+    return evecs[:, keep] @ ((evecs[:, keep].T @ amom) / evals[keep])
 
 
 def rigid_body_angular_velocities(pos, avel):

@@ -4,27 +4,38 @@ Restates micmec/sampling/verlet.py:140-166 (half kick, drift, force evaluation,
 half kick) with the Langevin thermostat of micmec/sampling/nvt.py:196-218
 applied before and after each step, on top of the NumPy force oracle in
 ``oracle/mmff.py``. The force evaluation can be split by cells over a pool of
-worker processes (start the pool with the 'spawn' method).
+worker processes (start the pool with the 'spawn' method); every task carries the
+data of its cells, so the workers hold no state.
 """
 
 import numpy as np
 
 from oracle import mmff as om
 
-_W = {}
+
+def chunk_deformation(job):
+    """Energies and corner gradients of one chunk of cells (a worker-process task).
+
+    The job carries everything the chunk needs, so workers keep no state: the corner
+    positions of its cells (m, 8, 3), rvecs, cell types, image shifts, parameters and
+    model. Returns (per-cell energies, corner gradients, vertices).
+    """
+    corner_pos, rvecs, types, shifts, params, model = job
+    m = len(types)
+    sn = np.arange(8 * m, dtype=np.int64).reshape(m, 8)
+    return om.deformation(corner_pos.reshape(-1, 3), rvecs, None, sn, types, params, model, pbc=True,
+                          shifts=shifts)
 
 
-def _init_worker(static):
-    _W.clear()
-    _W.update(static)
-
-
-def _work(args):
-    pos, rvecs, lo, hi = args
-    cells = np.arange(lo, hi)
-    e, g, _ = om.deformation(pos, rvecs, _W["grid"], _W["sn"], _W["types"], _W["params"], _W["model"],
-                             cells=cells, shifts=_W["shifts"])
-    return lo, e, g
+def pooled_deformation(pool, nproc, pos, rvecs, sn, types, shifts, params, model, ncells=None):
+    """om.deformation over the first ``ncells`` cells (all by default), split over a process pool."""
+    M = len(sn) if ncells is None else int(ncells)
+    bounds = np.linspace(0, M, 4 * nproc + 1).astype(int)
+    jobs = [(pos[sn[lo:hi]], rvecs, types[lo:hi], shifts[lo:hi], params, model)
+            for lo, hi in zip(bounds[:-1], bounds[1:])]
+    parts = pool.map(chunk_deformation, jobs)
+    return (np.concatenate([p[0] for p in parts]), np.concatenate([p[1] for p in parts]),
+            np.concatenate([p[2] for p in parts]))
 
 
 class LangevinState(object):
@@ -38,7 +49,7 @@ class LangevinState(object):
         self.vel = np.array(vel, dtype=np.float64)
         self.masses = np.asarray(d["masses"], dtype=np.float64)
         self.rvecs = np.asarray(d["rvecs"], dtype=np.float64).reshape(-1, 3)
-        fs = 1e-15 / 2.418884326500e-17
+        fs = 1e-15 / 2.418884326505e-17
         self.dt = dt_fs * fs
         self.temp = temp
         self.tau = timecon_fs * fs
@@ -51,10 +62,6 @@ class LangevinState(object):
         self.shifts = om.cell_shifts(self.grid, self.sn, self.rvecs.shape[0] == 3)
         self.pool = pool
         self.nproc = nproc
-        if pool is not None:
-            static = dict(grid=self.grid, sn=self.sn, types=self.types, params=self.params, model=model,
-                          shifts=self.shifts)
-            pool.map(_init_worker, [static] * nproc)
         self.epot, self.gpos = self.forces()
 
     def forces(self, ncells=None):
@@ -63,18 +70,13 @@ class LangevinState(object):
         if self.pool is None:
             e, g, _ = om.deformation(self.pos, self.rvecs, self.grid, self.sn, self.types, self.params, self.model,
                                      shifts=self.shifts, cells=None if ncells is None else np.arange(M))
-            if ncells is not None:
-                gfull = np.zeros((len(self.sn), 8, 3))
-                gfull[:M] = g
-                g = gfull
         else:
-            bounds = np.linspace(0, M, 4 * self.nproc + 1).astype(int)
-            parts = self.pool.map(_work, [(self.pos, self.rvecs, lo, hi) for lo, hi in zip(bounds[:-1], bounds[1:])])
-            e = np.zeros(M)
-            g = np.zeros((len(self.sn), 8, 3))
-            for lo, ee, gg in parts:
-                e[lo:lo + len(ee)] = ee
-                g[lo:lo + len(ee)] = gg
+            e, g, _ = pooled_deformation(self.pool, self.nproc, self.pos, self.rvecs, self.sn, self.types,
+                                         self.shifts, self.params, self.model, ncells)
+        if ncells is not None:
+            gfull = np.zeros((len(self.sn), 8, 3))
+            gfull[:M] = g
+            g = gfull
         return float(np.sum(e)), om.gather_gpos(g, self.sc)
 
     def thermo(self):

@@ -472,8 +472,82 @@ def make_cell_opt_fixtures():
         save("opt_cell_%s_nanocell" % tag, **arrays)
 
 
+# ------------------------------------------------------------------ units and sampling utilities
+
+
+def make_units_fixture():
+    """Numbers of the reference's data that pin the atomic mass unit: the 'fcu' type mass
+    (data/type_1x1x1_fcu_atomic.pickle) and the element counts of the atomic structure
+    (data/1x1x1_fcu_atomic.chk) whose atomic weights it sums."""
+    import pickle
+
+    from molmod.io.chk import load_chk
+
+    with open(os.path.join(DATA, "type_1x1x1_fcu_atomic.pickle"), "rb") as f:
+        fcu = pickle.load(f)
+    numbers = np.asarray(load_chk(os.path.join(DATA, "1x1x1_fcu_atomic.chk"))["numbers"])
+    z, counts = np.unique(numbers, return_counts=True)
+    save("units_pin", fcu_mass=np.array(float(np.asarray(fcu["mass"]))), numbers=z, counts=counts)
+
+
+class _FakeFF(object):
+    """The three members of a force field that domain_symmetrize uses."""
+
+    def __init__(self, pos, rvecs):
+        from micmec.pes.ext import Domain
+
+        self.system = type("S", (), {})()
+        self.system.pos = np.array(pos)
+        self.system.domain = Domain(np.ascontiguousarray(rvecs))
+
+    def update_rvecs(self, rvecs):
+        self.system.domain.update_rvecs(np.ascontiguousarray(rvecs))
+
+    def update_pos(self, pos):
+        self.system.pos[:] = pos
+
+
+def make_sampling_utils_fixture():
+    """The reference's initial-velocity, momentum-removal, dof and symmetrisation routines
+    (micmec/sampling/utils.py) on seeded inputs; np.random seeds are recorded."""
+    from micmec.pes.ext import Domain
+    from micmec.sampling import utils as su
+
+    arrays = {}
+    rng = np.random.default_rng(5)
+    masses = rng.uniform(0.5, 1.5, 50) * lattices.FCU_MASS
+    arrays["masses"] = masses
+    cases = [(300.0, True, None), (300.0, False, None), (600.0, True, np.array([1, 5, 7, 30])), (0.0, True, None)]
+    for i, (temp, scale, select) in enumerate(cases):
+        np.random.seed(100 + i)
+        arrays["vel%d" % i] = su.get_random_vel(temp, scale, masses, select=select)
+    arrays["vel_seeds"] = 100 + np.arange(len(cases))
+    baro_mass = (3 * 50 + 9) * units.boltzmann * 300.0 / (2 * np.pi / (1000 * units.femtosecond)) ** 2
+    np.random.seed(200)
+    arrays["vel_press"] = su.get_random_vel_press(baro_mass, 300.0)
+    arrays["baro_mass"] = np.array(baro_mass)
+    pos = rng.normal(size=(50, 3)) * 50.0
+    vel = rng.normal(size=(50, 3)) * 1e-4
+    arrays["clean_pos0"], arrays["clean_vel0"] = pos, vel
+    for tag, rvecs in (("pbc", np.eye(3) * 100.0), ("iso", np.zeros((0, 3)))):
+        p, v = pos.copy(), vel.copy()
+        su.clean_momenta(p, v, masses, Domain(np.ascontiguousarray(rvecs)))
+        arrays["clean_%s_pos" % tag], arrays["clean_%s_vel" % tag] = p, v
+    arrays["ndof_internal"] = np.array([su.get_ndof_internal_md(57, n) for n in (0, 1, 2, 3)])
+    arrays["ndof_baro"] = np.array([su.get_ndof_baro(3, a, c) for a, c in ((True, False), (True, True), (False, False))])
+    rv = np.array([[40.0, 1.5, -0.7], [0.9, 41.0, 2.1], [-1.2, 0.3, 39.0]])
+    ff = _FakeFF(pos, rv)
+    vecs, tens = su.domain_symmetrize(ff, vector_lst=[vel[:3].copy()], tensor_lst=[np.outer(vel[0], vel[1])])
+    arrays["sym_rvecs0"] = rv
+    arrays["sym_rvecs"] = np.array(ff.system.domain.rvecs)
+    arrays["sym_pos"] = np.array(ff.system.pos)
+    arrays["sym_vec"] = vecs[0]
+    arrays["sym_tens"] = tens[0]
+    save("sampling_utils", **arrays)
+
+
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["forces", "builder", "md", "hooks", "gle", "opt", "cellopt"]
+    which = sys.argv[1:] or ["forces", "builder", "md", "hooks", "gle", "opt", "cellopt", "units", "sutils"]
     if "forces" in which:
         make_force_fixtures()
     if "builder" in which:
@@ -488,3 +562,7 @@ if __name__ == "__main__":
         make_opt_fixture()
     if "cellopt" in which:
         make_cell_opt_fixtures()
+    if "units" in which:
+        make_units_fixture()
+    if "sutils" in which:
+        make_sampling_utils_fixture()

@@ -96,3 +96,35 @@ def test_device_cg_positions_reach_reference_minimum():
     e = ff.compute()
     assert e <= g["energies"][-1] + 1e-9 * abs(g["energies"][-1])
     assert np.abs(s.pos - g["pos_end"]).max() < 1e-3
+
+
+def test_strain_cell_relaxation_with_pressure_part_matches_batched_relaxer():
+    """ForcePartPressure beside ForcePartMechanical under StrainCellDOF + CG (host optimiser,
+    GPU forces): the relaxed enthalpy E + P V, domain and residual stress vtens / V + P I
+    equal those of the batched device relaxer run at the same external pressure."""
+    from micmec_gb300 import units
+    from micmec_gb300.batch import BatchSystems
+    from micmec_gb300.pes.mmff import ForcePartMechanical, ForcePartPressure, MicMecForceField
+    from micmec_gb300.sampling.dof import StrainCellDOF
+    from micmec_gb300.sampling.opt import CGOptimizer
+
+    P = 500e6 * units.pascal
+    g = load_golden("opt_cell_strain_nanocell")
+    d = system_dict(g, "sys/")
+    s = make_system(d)
+    mech = ForcePartMechanical(s, model="nanocell")
+    ff = MicMecForceField(s, [mech, ForcePartPressure(s, P)])
+    dof = StrainCellDOF(ff, gpos_rms=1e-9, dpos_rms=1e-7, grvecs_rms=1e-9, drvecs_rms=1e-7)
+    CGOptimizer(dof).run(4000)
+    vtens = np.zeros((3, 3))
+    h_host = ff.compute(None, vtens)
+    V = s.domain.volume
+    assert np.abs(vtens / V).max() < 1e-9  # mechanical virial / V balances -P I
+    b = BatchSystems([make_system(d)], model="nanocell", precision="fp64")
+    b.set_state([d["pos"]], None, [d["rvecs"]])
+    gmax, iters = b.relax(max_iter=4000, gtol=1e-8, cell="strain", press=P, stress_tol=1e-11)
+    assert gmax[0] < 1e-8, iters
+    h_batch = b.energies()[0] + P * b.control()[0, 18]
+    assert abs(h_host - h_batch) <= 1e-9 * abs(h_batch)
+    rv, ref = np.asarray(s.domain.rvecs), b.get_state()[2][0]
+    assert np.abs(rv @ rv.T - ref @ ref.T).max() <= 1e-5 * np.abs(ref @ ref.T).max()
