@@ -362,6 +362,13 @@ mm_status mm_selftest_convert(const double* din, float* dout, const float* fin, 
  */
 mm_status mm_selftest_sym_exp(const double* S, int n, double f, double* r_thread, double* r_warp, void* stream);
 
+/*
+ * Self-test of the exponential the hook algebra uses for its small arguments (a Taylor
+ * polynomial to x^9 for |x| < 2^-5, the library exp otherwise): out[i] = exp(x[i]) for
+ * i < n. All pointers device. No reference counterpart (test support).
+ */
+mm_status mm_selftest_exp_small(const double* x, double* out, int n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

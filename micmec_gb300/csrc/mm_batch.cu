@@ -508,6 +508,16 @@ mm_status mm_selftest_sym_exp(const double* S, int n, double f, double* r_thread
   return MM_OK;
 }
 
+mm_status mm_selftest_exp_small(const double* x, double* out, int n, void* stream) {
+  if (n < 0 || (n > 0 && (!x || !out))) {
+    mm::set_error("mm_selftest_exp_small: bad arguments");
+    return MM_ERR_ARG;
+  }
+  if (n > 0) mmb::k_selftest_exp_small<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(x, out, n);
+  BCUDA(cudaGetLastError());
+  return MM_OK;
+}
+
 mm_status mm_batch_config(mm_batch* b, int* cta_threads, int* nctas) {
   if (!b) return MM_ERR_ARG;
   if (cta_threads) *cta_threads = b->bt;

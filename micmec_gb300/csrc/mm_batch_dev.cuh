@@ -102,6 +102,12 @@ template <> void launch_md_t<double, 1>(const BatchLaunch&, const BMD&, cudaStre
 namespace {
 
 
+// systems with at least this many cells per thread evaluate them one thread per cell
+// (cell1_eval); smaller ones use eight lanes per cell (cell8_eval)
+#ifndef MM_BATCH_CELL1_MIN
+#define MM_BATCH_CELL1_MIN 1
+#endif
+constexpr int kCell1MinCellsPerThread = MM_BATCH_CELL1_MIN;
 constexpr int kMaxBT = 256;  // largest CTA size; the kernels are instantiated for 128 and 256
 constexpr int kMaxNW = kMaxBT / 32;
 
@@ -181,9 +187,14 @@ __device__ __forceinline__ double f2_total_of_lane(const F2 (&v)[NV]) {
   return f2d(hi) + f2d(lo);
 }
 
-// Energy, virial (into sh.ctl) and node gradient (a.gpos) of system sy.
+// Energy, virial (into sh.ctl) and node gradient (a.gpos) of system sy. Not inlined: a step
+// evaluates the forces at up to four places (MTK half steps, the Verlet step, the Berendsen
+// barostat), and one copy of this code keeps the kernel smaller in the instruction cache.
+#ifndef MM_FORCES_INLINE
+#define MM_FORCES_INLINE __noinline__
+#endif
 template <typename T, int MODEL>
-__device__ void forces(const BArgs& a, Shared<T>& sh, const BSys& sy) {
+__device__ MM_FORCES_INLINE void forces(const BArgs& a, Shared<T>& sh, const BSys& sy) {
   const T* disp = (const T*)a.disp;
   T* G = (T*)a.G + 24 * sy.off;
   const long long N3 = a.Ntot;
@@ -194,7 +205,47 @@ __device__ void forces(const BArgs& a, Shared<T>& sh, const BSys& sy) {
   // narrow), converted once per system in the CTA sum
   F2 facc[10];
   for (int i = 0; i < 10; ++i) facc[i] = F2{0.0f, 0.0f};
-  if (MODEL >= 1) {  // eight corner matrices; MODEL 2: diagonal h0 and cubic stress maps
+  if (MODEL >= 1 && M >= kCell1MinCellsPerThread * (int)blockDim.x) {
+    // eight corner matrices, one thread per cell (systems with at least a cell per thread);
+    // a thread's few cells are summed in the cell precision, then join the CTA sums below
+    T vs[10];
+#pragma unroll
+    for (int q = 0; q < 10; ++q) vs[q] = T(0);
+    for (int cell = threadIdx.x; cell < M; cell += blockDim.x) {
+      int i, j, k;
+      grid_coords(sy, cell, i, j, k);
+      T du[8][3];
+#pragma unroll
+      for (int b = 0; b < 8; ++b) {
+        const int node = wrap_node(sy, i + (b & 1), j + ((b >> 1) & 1), k + (b >> 2));
+#pragma unroll
+        for (int x = 0; x < 3; ++x) du[b][x] = disp[x * N3 + sy.off + node];
+      }
+      T g[8][3];
+      const T E = cell1_eval<T, MODEL == 2>(du, sh.tp[a.ctype[sy.off + cell]], g);
+#pragma unroll
+      for (int kc = 0; kc < 8; ++kc)
+#pragma unroll
+        for (int x = 0; x < 3; ++x) G[(kc * 3 + x) * (size_t)M + cell] = g[corner_to_bits(kc)][x];
+      vs[0] += E;
+#pragma unroll
+      for (int b = 1; b < 8; ++b)
+#pragma unroll
+        for (int y = 0; y < 3; ++y) {
+          T r = du[b][y] - du[0][y];
+          if (b & 1) r += sh.L[0 * 3 + y];
+          if (b & 2) r += sh.L[1 * 3 + y];
+          if (b & 4) r += sh.L[2 * 3 + y];
+#pragma unroll
+          for (int x = 0; x < 3; ++x) vs[1 + x * 3 + y] += g[b][x] * r;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 10; ++q) {
+      if constexpr (sizeof(T) == 4) facc[q] = F2{vs[q], 0.0f};
+      else acc[q] = (double)vs[q];
+    }
+  } else if (MODEL >= 1) {  // eight lanes per cell (small systems); MODEL 2: diagonal h0, cubic stress maps
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, av = threadIdx.x & 7;
     const int ngroups = (M + 3) / 4;
     const int nw = blockDim.x >> 5;
@@ -554,12 +605,14 @@ __device__ __forceinline__ double wsym_exp(double s, double f) {
     ++k;
   }
   double term = (e % 4 == 0) ? 1.0 : 0.0, r = term;
+  double bound = 1.0;
   for (int n = 1; n <= 20; ++n) {
     const double t = wmatmul3(term, A);
-    const double inv = 1.0 / n;
+    const double inv = kInvN[n];
     term = __dmul_rn(t, inv);
     r = __dadd_rn(r, term);
-    if (wnorm1(term) <= 1e-18 * wnorm1(r)) break;
+    bound = __dmul_rn(__dmul_rn(bound, nrm), inv);
+    if (bound <= 5e-19) break;
   }
   for (int q = 0; q < k; ++q) r = wmatmul3(r, r);
   return r;
@@ -570,9 +623,11 @@ __device__ __forceinline__ void wupdate_baro_vel(double* c, const BMD& p, bool c
   const int l = threadIdx.x & 31, e = wentry(), i = e / 3, j = e % 3;
   const double dt = p.dt;
   double vp = c[C_VP + e];
-  const double fric = z6 ? exp(-dt / (8 * c[C_BTAU])) : 1.0;
+  const double fric = z6 ? exp_small(-dt / (8 * c[C_BTAU])) : 1.0;
+  const double cfac = chain ? exp_small(-dt * cv0 / 8) : 1.0;
+  const double inv_mass = 1.0 / c[C_MPRESS];
   if (z6) vp *= fric;
-  if (chain) vp *= exp(-dt * cv0 / 8);
+  if (chain) vp *= cfac;
   const double pt_ij = c[C_KT + e] - c[C_VT + e];
   const double pt_ji = c[C_KT + j * 3 + i] - c[C_VT + j * 3 + i];
   const double ps = 0.5 * (pt_ji + pt_ij);
@@ -587,11 +642,11 @@ __device__ __forceinline__ void wupdate_baro_vel(double* c, const BMD& p, bool c
       if (tri == t) z = z6[t];
     R = z * sc;
   }
-  const double Gi = (ps + ((e % 4 == 0) ? diag : 0.0)) / c[C_MPRESS];
-  if (z6) vp += (Gi - R / c[C_MPRESS]) * dt / 4;
+  const double Gi = (ps + ((e % 4 == 0) ? diag : 0.0)) * inv_mass;
+  if (z6) vp += (Gi - R * inv_mass) * dt / 4;
   else vp += Gi * dt / 4;
   if (z6) vp *= fric;
-  if (chain) vp *= exp(-dt * cv0 / 8);
+  if (chain) vp *= cfac;
   __syncwarp();
   if (l < 9) c[C_VP + e] = vp;
   __syncwarp();
@@ -629,6 +684,12 @@ __device__ __forceinline__ void wscale_domain(double* c, const double* M) {
   __syncwarp();
   if (l == 0) c[C_VOL] = vol;
   __syncwarp();
+}
+
+// Self-test of exp_small: out[i] = exp_small(x[i]).
+__global__ void k_selftest_exp_small(const double* x, double* out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = exp_small(x[i]);
 }
 
 // Self-test of the warp form: exp(f S) of n 3x3 matrices (row-major, 9 doubles each) by

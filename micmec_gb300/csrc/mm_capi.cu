@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -171,6 +172,9 @@ mm_status mm_create(int nnodes, int ncells, const int32_t* node_coords, const in
   }
 
   h->simple = mm::tables_are_simple(h->tt, ntypes);
+  // cell kernel of the eight-corner-matrix model: one thread per cell unless the environment
+  // asks for the eight-lane form (MICMEC_CELL_KERNEL=8); both give the same results
+  if (const char* ck = std::getenv("MICMEC_CELL_KERNEL")) h->cell_kernel = (std::atoi(ck) == 8) ? 8 : 1;
 
   // structured lattice detection: periodic, every lattice site a node and a cell,
   // tables identical to the implicit ones

@@ -139,6 +139,37 @@ __device__ inline double gamma_mt(double a, unsigned long long seed, unsigned sy
 // tags of the hook draws
 enum { TAG_CSVR_R = 1, TAG_CSVR_S = 2, TAG_LBARO = 8 };
 
+// ------------------------------------------------------------ FP64 scalar helpers
+// On this part an FP64 instruction occupies its SM sub-partition for ~64 cycles, and the
+// hook algebra below is a dependent chain of them on one thread or warp while the rest of
+// the CTA waits: it avoids FP64 divisions (a Newton sequence each) where the reciprocal of
+// a constant does, and evaluates the exponentials of the hooks' small arguments by a short
+// Taylor series.
+
+// 1 / n for n = 0..20 (entry 0 unused), each the correctly rounded double.
+static __device__ __constant__ const double kInvN[21] = {
+    0.0, 1.0 / 1, 1.0 / 2, 1.0 / 3, 1.0 / 4, 1.0 / 5, 1.0 / 6, 1.0 / 7, 1.0 / 8, 1.0 / 9, 1.0 / 10,
+    1.0 / 11, 1.0 / 12, 1.0 / 13, 1.0 / 14, 1.0 / 15, 1.0 / 16, 1.0 / 17, 1.0 / 18, 1.0 / 19, 1.0 / 20};
+
+// exp(x). For |x| < 2^-5 (the thermostat and barostat factors: x = -dt v / 8 and the like)
+// the Taylor polynomial to x^9 in Horner form (truncation below x^10 / 10! < 2.5e-22, far
+// under half an ulp of the result); otherwise the library exp. The range test reads the
+// exponent field on the integer pipe.
+__device__ inline double exp_small(double x) {
+  const unsigned hi = (unsigned)(__double_as_longlong(x) >> 32);
+  if (((hi >> 20) & 0x7FFu) >= 1023u - 5u) return exp(x);
+  double r = 2.7557319223985893e-06;  // 1/9!
+  r = fma(r, x, 2.48015873015873e-05);  // 1/8!
+  r = fma(r, x, 0.0001984126984126984);  // 1/7!
+  r = fma(r, x, 0.001388888888888889);  // 1/6!
+  r = fma(r, x, 0.008333333333333333);  // 1/5!
+  r = fma(r, x, 0.041666666666666664);  // 1/4!
+  r = fma(r, x, 0.16666666666666666);  // 1/3!
+  r = fma(r, x, 0.5);
+  r = fma(r, x, 1.0);
+  return fma(r, x, 1.0);
+}
+
 // ------------------------------------------------------------ small 3x3 helpers (thread 0, FP64)
 
 __device__ inline double norm1_3(const double* A) {
@@ -161,9 +192,11 @@ __device__ inline void matmul3(const double* A, const double* B, double* C) {
 // an eigen-decomposition (np.linalg.eigh, npt.py:700-716), here by scaling and squaring
 // of the Taylor series (Moler and Van Loan, "Nineteen dubious ways to compute the
 // exponential of a matrix, twenty-five years later", SIAM Review 45, 2003): A = f S / 2^k
-// with ||A||_1 <= 1/8, T = sum_n A^n / n! until a term falls below 1e-18 ||T||_1, then
-// R = T^(2^k). The barostat's arguments are small (k = 0, a handful of terms), and the
-// result agrees with the eigen-decomposition form to FP64 rounding.
+// with ||A||_1 <= 1/8, T = sum_n A^n / n!, then R = T^(2^k). Terms are added until the
+// bound ||A||^n / n! of the last one falls below 5e-19 (||T||_1 >= 2 - e^(1/8) > 0.86, so
+// every omitted term is below 1e-18 ||T||_1). The barostat's arguments are small (k = 0, a
+// handful of terms), and the result agrees with the eigen-decomposition form to FP64
+// rounding.
 __device__ inline void sym_exp(const double* S, double f, double* R) {
   double A[9];
   for (int i = 0; i < 9; ++i) A[i] = f * S[i];
@@ -176,14 +209,16 @@ __device__ inline void sym_exp(const double* S, double f, double* R) {
   }
   double term[9], tmp[9];
   for (int i = 0; i < 9; ++i) R[i] = term[i] = (i % 4 == 0) ? 1.0 : 0.0;
+  double bound = 1.0;
   for (int n = 1; n <= 20; ++n) {
     matmul3(term, A, tmp);
-    const double inv = 1.0 / n;
+    const double inv = kInvN[n];
     for (int i = 0; i < 9; ++i) {
       term[i] = __dmul_rn(tmp[i], inv);  // not fused with the sum below
       R[i] = __dadd_rn(R[i], term[i]);
     }
-    if (norm1_3(term) <= 1e-18 * norm1_3(R)) break;
+    bound = __dmul_rn(__dmul_rn(bound, nrm), inv);
+    if (bound <= 5e-19) break;
   }
   for (int q = 0; q < k; ++q) {
     matmul3(R, R, tmp);
@@ -197,11 +232,13 @@ __device__ inline void sym_exp(const double* S, double f, double* R) {
 // random force R = z sqrt(2 W kT / (dt timecon)) (symmetric) in the update.
 __device__ inline void update_baro_vel(double* c, const BMD& p, bool chain, double cv0, const double* z6 = nullptr) {
   const double dt = p.dt;
-  const double fric = z6 ? exp(-dt / (8 * c[C_BTAU])) : 1.0;
+  const double fric = z6 ? exp_small(-dt / (8 * c[C_BTAU])) : 1.0;
+  const double cfac = chain ? exp_small(-dt * cv0 / 8) : 1.0;
+  const double inv_mass = 1.0 / c[C_MPRESS];
   if (z6)
     for (int i = 0; i < 9; ++i) c[C_VP + i] *= fric;
   if (chain)
-    for (int i = 0; i < 9; ++i) c[C_VP + i] *= exp(-dt * cv0 / 8);
+    for (int i = 0; i < 9; ++i) c[C_VP + i] *= cfac;
   double pt[9];
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) pt[i * 3 + j] = c[C_KT + i * 3 + j] - c[C_VT + i * 3 + j];
@@ -216,14 +253,14 @@ __device__ inline void update_baro_vel(double* c, const BMD& p, bool chain, doub
     for (int i = 0; i < 9; ++i) R[i] = z6[tri[i]] * sc;
   }
   for (int i = 0; i < 9; ++i) {
-    const double Gi = (ps[i] + ((i % 4 == 0) ? diag : 0.0)) / c[C_MPRESS];
-    if (z6) c[C_VP + i] += (Gi - R[i] / c[C_MPRESS]) * dt / 4;
+    const double Gi = (ps[i] + ((i % 4 == 0) ? diag : 0.0)) * inv_mass;
+    if (z6) c[C_VP + i] += (Gi - R[i] * inv_mass) * dt / 4;
     else c[C_VP + i] += Gi * dt / 4;
   }
   if (z6)
     for (int i = 0; i < 9; ++i) c[C_VP + i] *= fric;
   if (chain)
-    for (int i = 0; i < 9; ++i) c[C_VP + i] *= exp(-dt * cv0 / 8);
+    for (int i = 0; i < 9; ++i) c[C_VP + i] *= cfac;
 }
 
 // The six unit normals of Langevin-barostat call `call` (0..3) of step `step`, system `sys`.
@@ -315,8 +352,11 @@ __device__ inline double ekin_baro(const double* c) {
 // differ from the integrator's when a Langevin barostat later widens them (npt.py:86-90)
 __device__ inline double chain_ndof(const double* c) { return c[C_CNDOF] > 0.0 ? c[C_CNDOF] : c[C_NDOF]; }
 
-// one bead update of the Nose-Hoover chain (nvt.py:411-435), thread 0
-__device__ inline void nhc_bead(double* c, const BMD& p, int k, double ekin, bool g1, double G1_add, double kT) {
+// one bead update of the Nose-Hoover chain (nvt.py:411-435), thread 0; inv_mass[k] = 1 /
+// (mass of bead k). The friction factor of the next bead is the same before and after the
+// force term, so it is formed once.
+__device__ inline void nhc_bead(double* c, const BMD& p, int k, double ekin, bool g1, double G1_add, double kT,
+                                const double (&inv_mass)[3]) {
   const int L = p.chain;
   double g;
   if (k == 0) {
@@ -325,24 +365,27 @@ __device__ inline void nhc_bead(double* c, const BMD& p, int k, double ekin, boo
   } else {
     g = c[C_CMASS + k - 1] * c[C_CVEL + k - 1] * c[C_CVEL + k - 1] - kT;
   }
-  g /= c[C_CMASS + k];
+  g *= inv_mass[k];
   if (k == L - 1) {
     c[C_CVEL + k] += g * p.dt / 4;
   } else {
-    c[C_CVEL + k] *= exp(-c[C_CVEL + k + 1] * p.dt / 8);
+    const double fr = exp_small(-c[C_CVEL + k + 1] * p.dt / 8);
+    c[C_CVEL + k] *= fr;
     c[C_CVEL + k] += g * p.dt / 4;
-    c[C_CVEL + k] *= exp(-c[C_CVEL + k + 1] * p.dt / 8);
+    c[C_CVEL + k] *= fr;
   }
 }
 
 // Full NHChain call (nvt.py:410-451): returns the velocity scale factor; updates ekin in c.
 __device__ inline double nhc_call(double* c, const BMD& p, bool g1, double G1_add, double kT) {
   double ekin = c[C_EKIN];
-  for (int k = p.chain - 1; k >= 0; --k) nhc_bead(c, p, k, ekin, g1, G1_add, kT);
+  double inv_mass[3] = {0.0, 0.0, 0.0};
+  for (int k = 0; k < p.chain; ++k) inv_mass[k] = 1.0 / c[C_CMASS + k];
+  for (int k = p.chain - 1; k >= 0; --k) nhc_bead(c, p, k, ekin, g1, G1_add, kT, inv_mass);
   for (int k = 0; k < p.chain; ++k) c[C_CPOS + k] += c[C_CVEL + k] * p.dt / 2;
-  const double factor = exp(-c[C_CVEL + 0] * p.dt / 2);
+  const double factor = exp_small(-c[C_CVEL + 0] * p.dt / 2);
   ekin *= factor * factor;
-  for (int k = 0; k < p.chain; ++k) nhc_bead(c, p, k, ekin, g1, G1_add, kT);
+  for (int k = 0; k < p.chain; ++k) nhc_bead(c, p, k, ekin, g1, G1_add, kT, inv_mass);
   c[C_EKIN] = ekin;
   return factor;
 }

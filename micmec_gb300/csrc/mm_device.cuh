@@ -642,6 +642,136 @@ __device__ __forceinline__ T cell8_eval(const T (&du)[3], int a, const TypeParam
   return Ecell;
 }
 
+// ---------------------------------------------------------------- one thread per cell
+// The eight-corner-matrix model evaluated by one thread for a whole cell: du[b][x] is the
+// displacement of the corner with offset bits b. A state's energy sums the eight corner
+// matrices; the gradient of corner matrix a adds its row d to vertex a | bit d and
+// subtracts it from vertex a & ~bit d (the two ends of that row's edge). No lane exchanges
+// are needed, and the cell's gradient and vertices stay in the thread's registers.
+
+template <typename T, bool SIMPLE>
+struct StateView;  // the part of a state's parameters the thread keeps in registers
+template <>
+struct StateView<float, true> {
+  CubicView<float> v;
+  __device__ __forceinline__ void load(const StateParams<float>& p) { load_cubic(p, v); }
+  __device__ __forceinline__ const CubicView<float>& params(const StateParams<float>&) const { return v; }
+  __device__ __forceinline__ float B(const StateParams<float>&, int i) const { return v.B[i]; }
+  __device__ __forceinline__ float v0(const StateParams<float>&) const { return v.v0; }
+  __device__ __forceinline__ float df(const StateParams<float>&) const { return v.df; }
+};
+template <typename T, bool SIMPLE>
+struct StateView {  // parameters read from shared memory where they are used
+  __device__ __forceinline__ void load(const StateParams<T>&) {}
+  __device__ __forceinline__ const StateParams<T>& params(const StateParams<T>& p) const { return p; }
+  __device__ __forceinline__ T B(const StateParams<T>& p, int i) const { return p.B[i]; }
+  __device__ __forceinline__ T v0(const StateParams<T>& p) const { return p.v0; }
+  __device__ __forceinline__ T df(const StateParams<T>& p) const { return p.df; }
+};
+
+// Corner matrix a of a cell minus the rest matrix: row d = B_d + du[a | bit d] - du[a & ~bit d].
+template <typename T, bool SIMPLE>
+__device__ __forceinline__ void corner_w(const T (&du)[8][3], int a, const StateView<T, SIMPLE>& sv,
+                                         const StateParams<T>& p, T (&W)[9]) {
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const int hi = a | (1 << d), lo = a & ~(1 << d);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) W[d * 3 + c] = sv.B(p, d * 3 + c) + (du[hi][c] - du[lo][c]);
+  }
+}
+
+// Energy of one state summed over the eight corner matrices (scale det(h0) / 8), plus its
+// free energy.
+template <typename T, bool SIMPLE>
+__device__ __forceinline__ T cell_state_energy(const T (&du)[8][3], const StateParams<T>& p) {
+  StateView<T, SIMPLE> sv;
+  sv.load(p);
+  const T scale = T(0.125) * sv.v0(p);
+  T E = T(0);
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    T W[9], D[9], st[6];
+    corner_w<T, SIMPLE>(du, a, sv, p, W);
+    E += state_energy<T, SIMPLE>(W, sv.params(p), scale, D, st);
+  }
+  return E + sv.df(p);
+}
+
+// The same, and the state's gradient times `weight` added to the vertex gradients g.
+template <typename T, bool SIMPLE>
+__device__ __forceinline__ T cell_state_energy_grad(const T (&du)[8][3], const StateParams<T>& p, T weight,
+                                                    T (&g)[8][3]) {
+  StateView<T, SIMPLE> sv;
+  sv.load(p);
+  const T scale = T(0.125) * sv.v0(p);
+  const T gscale = scale * weight;
+  T E = T(0);
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    T W[9], D[9], st[6], GW[9];
+    corner_w<T, SIMPLE>(du, a, sv, p, W);
+    E += state_energy<T, SIMPLE>(W, sv.params(p), scale, D, st);
+    state_gradient<T, SIMPLE>(D, st, sv.params(p), gscale, GW);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int hi = a | (1 << d), lo = a & ~(1 << d);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        g[hi][c] += GW[d * 3 + c];
+        g[lo][c] -= GW[d * 3 + c];
+      }
+    }
+  }
+  return E + sv.df(p);
+}
+
+// Cell energy (multi-state -kT log-sum-exp, micmec/pes/mmff.py:377-398) and vertex
+// gradients g (offset-bits order) of one cell, evaluated by one thread. State 0's energy
+// and gradient come from one pass over the corners, the other states' energies from one
+// pass each. Then the weights: a state whose weight is below e^-50 forms no gradient (the
+// lowest energy is known by then, and usually every state but one is that far up); state
+// 0's gradient is rescaled by its weight, and the other states are evaluated again with
+// their weight folded into the gradient scale.
+template <typename T, bool SIMPLE>
+__device__ __forceinline__ T cell1_eval(const T (&du)[8][3], const TypeParams<T>& p, T (&g)[8][3]) {
+#pragma unroll
+  for (int b = 0; b < 8; ++b)
+#pragma unroll
+    for (int x = 0; x < 3; ++x) g[b][x] = T(0);
+  T Ecell = cell_state_energy_grad<T, SIMPLE>(du, p.s[0], T(1), g);
+  const int ns = p.nstates;
+  if (ns > 1) {
+    T E[MM_MAX_STATES];
+    E[0] = Ecell;
+    T m = Ecell;
+    for (int s = 1; s < ns; ++s) {
+      E[s] = cell_state_energy<T, SIMPLE>(du, p.s[s]);
+      m = E[s] < m ? E[s] : m;
+    }
+    const T kT = p.kT;
+    T wsum = T(0), w0 = T(0);
+    for (int s = 0; s < ns; ++s) {
+      const T w = (E[s] - m >= T(50) * kT) ? T(0) : lse_weight<T>(m - E[s], kT, p.lkT);
+      wsum += w;
+      if (s == 0) w0 = w;
+    }
+    T inv;
+    if constexpr (sizeof(T) == 4) inv = __frcp_rn(wsum);
+    else inv = T(1) / wsum;
+    const T f0 = w0 * inv;
+#pragma unroll
+    for (int b = 0; b < 8; ++b)
+#pragma unroll
+      for (int x = 0; x < 3; ++x) g[b][x] *= f0;
+    for (int s = 1; s < ns; ++s)
+      if (E[s] - m < T(50) * kT)
+        cell_state_energy_grad<T, SIMPLE>(du, p.s[s], lse_weight<T>(m - E[s], kT, p.lkT) * inv, g);
+    Ecell = m - kT * lse_log<T>(wsum);
+  }
+  return Ecell;
+}
+
 // ---------------------------------------------------------------- reductions
 
 template <int NV>

@@ -21,6 +21,7 @@ struct mm_handle {
   int ntypes = 0;
   int num_sms = 0;
   int simple = 0;  // all rest matrices diagonal and all stress maps cubic (exactly)
+  int cell_kernel = 1;  // nanocell model: 1 = one thread per cell (k_cells1), 8 = eight lanes per cell (k_cells8)
   int cell_occ[2] = {0, 0};  // resident cell-kernel blocks per SM (general, simple); 0 = not queried
   int node_occ[2] = {0, 0};  // resident node-kernel blocks per SM (no thermostat, Langevin)
   mm::TypeTable tt[MM_MAX_TYPES];

@@ -21,6 +21,7 @@
 // index) use implicit topology (STRUCT = true): no index tables are read.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -425,6 +426,98 @@ __global__ void __launch_bounds__(kCell8Threads, sizeof(T) == 4 ? 3 : 2) k_cells
       store_pair(cpart + (1 + warp) * gridDim.x + blockIdx.x, acc0);
       if (warp < 2) store_pair(cpart + (warp == 0 ? 9 : 0) * gridDim.x + blockIdx.x, acc1);
     }
+  }
+}
+
+// One thread per cell for the eight-corner-matrix model (cell1_eval): the thread gathers
+// its cell's eight corner displacements and evaluates all eight corner matrices itself, so
+// there are no lane exchanges, no per-corner index arithmetic and no staging of virial terms
+// (the cell's gradient and vertex offsets stay in registers). Corner gradients are written
+// as in k_cells8 (corner-major, coalesced across the threads of a warp). A thread's few
+// cells are summed in the cell precision; the per-block sums are compensated FP32 pairs
+// (FP32 cells) or doubles, value-major: slot 0 energy, 1 + 3x + y virial.
+constexpr int kCell1Threads = 128;
+#ifndef MM_CELL1_MINB
+#define MM_CELL1_MINB 3
+#endif
+constexpr int kCell1MinBlocks = MM_CELL1_MINB;  // FP32: resident blocks per SM the registers are sized for
+
+template <typename T, bool STRUCT, bool SIMPLE>
+__global__ void __launch_bounds__(kCell1Threads, sizeof(T) == 4 ? kCell1MinBlocks : 2)
+    k_cells1(Topo t, const TypeTable* __restrict__ tt, int ntypes, const double* __restrict__ box,
+             const T* __restrict__ disp, T* __restrict__ G, double* __restrict__ ecell, double* __restrict__ cpart) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TypeParams<T>* tp = reinterpret_cast<TypeParams<T>*>(smem_raw);
+  double* red = reinterpret_cast<double*>(smem_raw + ((sizeof(TypeParams<T>) * ntypes + 15) / 16) * 16);
+  __shared__ T Ls[9];
+  pdl_enter();
+  load_params<T>(tp, tt, ntypes, box);
+  if (threadIdx.x < 9) Ls[threadIdx.x] = (T)box[threadIdx.x];
+  __syncthreads();
+  T acc[kCellPart];
+#pragma unroll
+  for (int i = 0; i < kCellPart; ++i) acc[i] = T(0);
+  for (int cell = blockIdx.x * blockDim.x + threadIdx.x; cell < t.M; cell += gridDim.x * blockDim.x) {
+    T du[8][3];
+    if (STRUCT) {
+      int i, j, k;
+      split_index(t, cell, i, j, k);
+#pragma unroll
+      for (int b = 0; b < 8; ++b) {
+        const int node = struct_corner_node(t, i, j, k, b);
+#pragma unroll
+        for (int x = 0; x < 3; ++x) du[b][x] = disp[x * t.N + node];
+      }
+    } else {
+#pragma unroll
+      for (int kc = 0; kc < 8; ++kc) {
+        const int node = t.cell_nodes[kc * t.M + cell];
+#pragma unroll
+        for (int x = 0; x < 3; ++x) du[corner_to_bits(kc)][x] = disp[x * t.N + node];
+      }
+    }
+    T g[8][3];
+    const T Ecell = cell1_eval<T, SIMPLE>(du, tp[t.cell_type[cell]], g);
+#pragma unroll
+    for (int kc = 0; kc < 8; ++kc)
+#pragma unroll
+      for (int x = 0; x < 3; ++x) G[(kc * 3 + x) * (size_t)t.M + cell] = g[corner_to_bits(kc)][x];
+    if (ecell) ecell[cell] = (double)Ecell;
+    acc[0] += Ecell;
+    // virial: sum_b g_b (x) (r_b - r_0), r_b - r_0 = offset(b) . L + du_b - du_0
+#pragma unroll
+    for (int b = 1; b < 8; ++b) {
+      T rel[3];
+#pragma unroll
+      for (int y = 0; y < 3; ++y) {
+        T r = du[b][y] - du[0][y];
+        if (b & 1) r += Ls[0 * 3 + y];
+        if (b & 2) r += Ls[1 * 3 + y];
+        if (b & 4) r += Ls[2 * 3 + y];
+        rel[y] = r;
+      }
+#pragma unroll
+      for (int x = 0; x < 3; ++x)
+#pragma unroll
+        for (int y = 0; y < 3; ++y) acc[1 + x * 3 + y] += g[b][x] * rel[y];
+    }
+  }
+  if constexpr (sizeof(T) == 8) {
+    double v[kCellPart];
+#pragma unroll
+    for (int i = 0; i < kCellPart; ++i) v[i] = acc[i];
+    block_sum<kCellPart>(v, red);
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int i = 0; i < kCellPart; ++i) cpart[i * gridDim.x + blockIdx.x] = v[i];
+  } else {
+    F2 f[kCellPart];
+#pragma unroll
+    for (int i = 0; i < kCellPart; ++i) f[i] = F2{acc[i], 0.0f};
+    block_sum_f2_pairs<kCellPart>(f, red);
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int i = 0; i < kCellPart; ++i) store_pair(cpart + i * gridDim.x + blockIdx.x, f[i]);
   }
 }
 
@@ -919,7 +1012,8 @@ static void topo_of(const mm_handle* h, Topo& t) {
 static size_t cell_smem(const mm_handle* h) {
   const size_t esz = h->prec == MM_PREC_FP32 ? sizeof(float) : sizeof(double);
   const size_t tp = (h->prec == MM_PREC_FP32 ? sizeof(TypeParams<float>) : sizeof(TypeParams<double>)) * h->ntypes;
-  if (h->model == MM_MODEL_NANOCELL) return ((tp + 15) / 16) * 16 + 2 * esz * kTileElems;
+  if (h->model == MM_MODEL_NANOCELL && h->cell_kernel == 8) return ((tp + 15) / 16) * 16 + 2 * esz * kTileElems;
+  if (h->model == MM_MODEL_NANOCELL) return ((tp + 15) / 16) * 16 + sizeof(double) * kCellPart * (kCell1Threads / 32);
   return ((tp + 15) / 16) * 16 + sizeof(double) * kCellPart * (kCellThreads / 32);
 }
 
@@ -935,6 +1029,9 @@ static int occupancy_of(K kern, int threads, size_t smem) {
 
 template <typename T, bool STRUCT>
 static int cell8_occupancy(const mm_handle* h) {
+  if (h->cell_kernel == 1)
+    return h->simple ? occupancy_of(k_cells1<T, STRUCT, true>, kCell1Threads, cell_smem(h))
+                     : occupancy_of(k_cells1<T, STRUCT, false>, kCell1Threads, cell_smem(h));
   return h->simple ? occupancy_of(k_cells8<T, STRUCT, true>, kCell8Threads, cell_smem(h))
                    : occupancy_of(k_cells8<T, STRUCT, false>, kCell8Threads, cell_smem(h));
 }
@@ -945,7 +1042,14 @@ static void launch_cells_t(mm_handle* h, cudaStream_t st, double* ecell) {
   topo_of(h, t);
   const int nblk = cell_grid(h);
   if constexpr (MODEL == 1) {
-    if (h->simple)
+    if (h->cell_kernel == 1) {
+      if (h->simple)
+        launch_pdl(k_cells1<T, STRUCT, true>, nblk, kCell1Threads, cell_smem(h), st, t, (const TypeTable*)h->d_tt,
+                   h->ntypes, (const double*)h->d_box, (const T*)h->d_disp, (T*)h->d_G, ecell, h->d_cpart);
+      else
+        launch_pdl(k_cells1<T, STRUCT, false>, nblk, kCell1Threads, cell_smem(h), st, t, (const TypeTable*)h->d_tt,
+                   h->ntypes, (const double*)h->d_box, (const T*)h->d_disp, (T*)h->d_G, ecell, h->d_cpart);
+    } else if (h->simple)
       launch_pdl(k_cells8<T, STRUCT, true>, nblk, kCell8Threads, cell_smem(h), st, t, (const TypeTable*)h->d_tt,
                  h->ntypes, (const double*)h->d_box, (const T*)h->d_disp, (T*)h->d_G, ecell, h->d_cpart);
     else
@@ -973,12 +1077,17 @@ void launch_cells(mm_handle* h, cudaStream_t st, double* ecell) {
   else launch_cells_p<double>(h, st, ecell);
 }
 
+// Resident blocks per SM at most: eight-lane kernel (256 threads) 4, one-thread kernel
+// (128 threads) 16.
+constexpr int kCell8MaxPerSM = 4, kCell1MaxPerSM = 16;
+
 int cell_blocks(const mm_handle* h) {
   if (h->model == MM_MODEL_NANOCELL) {
-    // grid-stride over groups of cells: at most 4 resident 256-thread blocks per SM
-    const int groups = (h->M + kCell8Cells - 1) / kCell8Cells;
-    const int cap = (h->num_sms > 0 ? h->num_sms : 152) * 4;
-    return groups < cap ? groups : cap;
+    // grid-stride over groups of cells with at most the resident blocks of either kernel
+    const int sms = h->num_sms > 0 ? h->num_sms : 152;
+    const int g8 = std::min((h->M + kCell8Cells - 1) / kCell8Cells, sms * kCell8MaxPerSM);
+    const int g1 = std::min((h->M + kCell1Threads - 1) / kCell1Threads, sms * kCell1MaxPerSM);
+    return std::max(g8, g1);
   }
   return (h->M + kCellThreads - 1) / kCellThreads;
 }
@@ -993,8 +1102,11 @@ int cell_grid(mm_handle* h) {
     if (h->prec == MM_PREC_FP32) occ = h->structured ? cell8_occupancy<float, true>(h) : cell8_occupancy<float, false>(h);
     else occ = h->structured ? cell8_occupancy<double, true>(h) : cell8_occupancy<double, false>(h);
   }
+  const int sms = h->num_sms > 0 ? h->num_sms : 152;
+  if (h->cell_kernel == 1)
+    return std::min((h->M + kCell1Threads - 1) / kCell1Threads, sms * std::min(occ, kCell1MaxPerSM));
   const int groups = (h->M + kCell8Cells - 1) / kCell8Cells;
-  const int cap = (h->num_sms > 0 ? h->num_sms : 152) * (occ < 4 ? occ : 4);
+  const int cap = sms * (occ < kCell8MaxPerSM ? occ : kCell8MaxPerSM);
   return groups < cap ? groups : cap;
 }
 

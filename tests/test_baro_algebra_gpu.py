@@ -54,3 +54,27 @@ def test_selftest_rejects_bad_arguments():
     assert nat.lib().mm_selftest_sym_exp(None, 4, 1.0, None, None, None) != 0
     assert b"sym_exp" in nat.lib().mm_last_error()
     assert nat.lib().mm_selftest_sym_exp(None, 0, 1.0, None, None, None) == 0
+
+
+def test_exp_small_against_library_exp():
+    """The hook algebra's exponential: a Taylor polynomial below |x| = 2^-5, the library exp
+    above; within 2 ulp of CUDA's exp (and of numpy's) everywhere on the tested range."""
+    import ctypes
+
+    import torch
+
+    from micmec_gb300 import _native as nat
+
+    L = nat.lib()
+    L.mm_selftest_exp_small.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    L.mm_selftest_exp_small.restype = ctypes.c_int
+    rng = np.random.default_rng(3)
+    x = np.concatenate([rng.uniform(-2.0**-5, 2.0**-5, 20000), rng.normal(size=2000) * 1e-6,
+                        rng.uniform(-3.0, 3.0, 2000), [0.0, -0.0, 2.0**-5, -2.0**-5, 2.0**-6, 1e-300, -1e-310]])
+    xd = torch.tensor(x, dtype=torch.float64, device="cuda")
+    out = torch.empty_like(xd)
+    nat.check(L.mm_selftest_exp_small(xd.data_ptr(), out.data_ptr(), len(x), None), "mm_selftest_exp_small")
+    got = out.cpu().numpy()
+    ref_cuda = torch.exp(xd).cpu().numpy()
+    assert (np.abs(got - ref_cuda) <= 2 * np.spacing(np.abs(ref_cuda))).all()
+    assert (np.abs(got - np.exp(x)) <= 2 * np.spacing(np.exp(x))).all()

@@ -71,3 +71,21 @@ def test_nan_raises_value_error():
     s.pos[3, 1] = np.nan
     with pytest.raises(ValueError):
         ff.compute(np.zeros((s.nnodes, 3)), np.zeros((3, 3)))
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("fp32", 1e-5)])
+@pytest.mark.parametrize("case", CASES)
+def test_eight_lane_cell_kernel_matches_reference(case, precision, tol, monkeypatch):
+    """The nanocell model's eight-lanes-per-cell kernel (selected with MICMEC_CELL_KERNEL=8; the
+    default is one thread per cell) against the reference's forces."""
+    monkeypatch.setenv("MICMEC_CELL_KERNEL", "8")
+    s, fp, ff = _ff(case, "nanocell", precision)
+    gpos = np.zeros((s.nnodes, 3))
+    vtens = np.zeros((3, 3))
+    e = ff.compute(gpos, vtens)
+    key = f"{case}/nanocell/"
+    e_ref, g_ref, v_ref = float(G[key + "energy"]), G[key + "gpos"], G[key + "vtens"]
+    assert abs(e - e_ref) <= tol * abs(e_ref)
+    assert np.abs(gpos - g_ref).max() <= tol * np.abs(g_ref).max()
+    assert np.abs(vtens - v_ref).max() <= tol * np.abs(v_ref).max()
+
