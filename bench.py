@@ -309,11 +309,15 @@ def batch_workload(nsys=512, seed=77, nstates=2):
     return systems, np.array(strains)
 
 
-def measure_batch(systems, strains, precision, md_steps, relax_iters):
+def measure_batch(systems, strains, precision, md_steps, relax_iters, drift=False):
+    """Config 3 on the batch kernel: batched CG relaxation of every strained system, then
+    md_steps NHC + MTK steps (300 K, 0 MPa) of all systems in one launch replayed from a CUDA
+    graph after autotuning. drift: a further untimed md_steps-step run with per-step records
+    gives each system's conserved quantity (epot + ekin + the hooks' corrections)."""
     import torch
 
     from micmec_gb300 import units
-    from micmec_gb300.batch import BatchSystems
+    from micmec_gb300.batch import REC, BatchSystems
 
     fs = units.femtosecond
     b = BatchSystems(systems, model="nanocell", precision=precision)
@@ -325,17 +329,19 @@ def measure_batch(systems, strains, precision, md_steps, relax_iters):
     t_relax = time.perf_counter() - t0
     stress = b.stress()[:, 0, 0] / units.gigapascal
     b.setup_md(temp=300.0, thermostat="nhc", barostat="mtk", timecon=100 * fs, baro_timecon=1000 * fs, seed=5)
-    cfg = b.autotune(probe_steps=3, thermostat="nhc", temp=300.0, barostat="mtk", press=0.0)
-    b.md(1, thermostat="nhc", temp=300.0, barostat="mtk", press=0.0, use_graph=True)  # capture
+    kw = dict(thermostat="nhc", temp=300.0, barostat="mtk", press=0.0)
+    cfg = b.autotune(probe_steps=3, **kw)
+    b.md(1, use_graph=True, **kw)  # capture
+    b.md(md_steps, use_graph=True, step0=1, **kw)  # capture of the timed launch's key (nsteps, step0)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
-    b.md(md_steps, thermostat="nhc", temp=300.0, barostat="mtk", press=0.0, use_graph=True, step0=1)
+    b.md(md_steps, use_graph=True, step0=1, **kw)
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     cells = float(np.sum(b.sizes))
-    return {
+    out = {
         "systems": len(systems), "cells": int(cells), "precision": precision, "md_steps": md_steps,
         "md_ms": ms, "systems_steps_per_s": len(systems) * md_steps / (ms * 1e-3),
         "cell_steps_per_s": cells * md_steps / (ms * 1e-3),
@@ -344,11 +350,27 @@ def measure_batch(systems, strains, precision, md_steps, relax_iters):
         "stress_xx_gpa_by_strain": {f"{s:.4f}": float(np.mean(stress[np.isclose(strains, s)])) for s in
                                      np.unique(strains)[:: 5]},
     }
+    if drift:
+        rec = b.md(md_steps, use_graph=False, step0=1 + md_steps, record=True, **kw)
+        econs = rec[:, :, REC["epot"]] + rec[:, :, REC["ekin"]] + rec[:, :, REC["ecorr"]]
+        etot = np.abs(rec[:, :, REC["epot"]] + rec[:, :, REC["ekin"]]).mean(axis=1)
+        per1000 = np.abs(econs[:, -1] - econs[:, 0]) / etot * (1000.0 / (md_steps - 1))
+        fluct = (econs.max(axis=1) - econs.min(axis=1)) / etot
+        out["conserved_quantity"] = {
+            "steps": md_steps, "timestep_fs": 1.0,
+            "change_per_1000_steps_rel_median": float(np.median(per1000)),
+            "change_per_1000_steps_rel_max": float(per1000.max()),
+            "fluctuation_rel_median": float(np.median(fluct)), "fluctuation_rel_max": float(fluct.max()),
+            "note": "epot + ekin + NHC and MTK corrections, relative to |epot + ekin|, per system",
+        }
+    return out
 
 
-def measure_plain_per_system(systems, nsteps):
-    """The plain FP64 GPU path for the same hooks: one System at a time through VerletIntegrator
-    (MTK barostat + NHC thermostat on the host, every force evaluation on the GPU)."""
+def measure_plain_per_system(systems, nsteps, device):
+    """The plain FP64 GPU path for the same hooks, one System at a time through VerletIntegrator
+    with NHC + MTK. device=True: the hooks run on the device (the integrator hands each system
+    to the persistent kernel as a one-system batch); device=False: host hooks, every force
+    evaluation on the GPU (three round trips per step)."""
     import torch
 
     from micmec_gb300 import units
@@ -363,23 +385,27 @@ def measure_plain_per_system(systems, nsteps):
     for s in systems:
         ff = MicMecForceField(s, [ForcePartMechanical(s, model="nanocell", precision="fp64")])
         hooks = [NHCThermostat(300.0, timecon=100 * fs), MTKBarostat(ff, 300.0, 0.0, timecon=1000 * fs)]
-        vi = VerletIntegrator(ff, 1.0 * fs, hooks=hooks, temp0=300.0)
+        vi = VerletIntegrator(ff, 1.0 * fs, hooks=hooks, temp0=300.0, device=device)
+        if device:
+            vi.run(2)  # first run: the one-system batch is created
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         vi.run(nsteps)
         torch.cuda.synchronize()
         t += time.perf_counter() - t0
         steps += nsteps
-    return {"systems": len(systems), "steps_each": nsteps, "systems_steps_per_s": steps / t,
-            "cell_steps_per_s": sum(s.ncells for s in systems) * nsteps / t}
+    return {"systems": len(systems), "steps_each": nsteps, "hooks_on_device": bool(device),
+            "systems_steps_per_s": steps / t, "cell_steps_per_s": sum(s.ncells for s in systems) * nsteps / t,
+            "system_sizes": [int(s.ncells) for s in systems]}
 
 
-def measure_large_mtk(n=256, nsteps=100, cmp_steps=4):
-    """Large single system (periodic n^3 lattice, 20% clustered defects, two states per
-    type) under NHC + MTK NPT at 300 K and 100 MPa, dt = 2 fs, through VerletIntegrator
-    (device=True routes it to the lattice engine). FP64 and FP32 cells run the same
-    cmp_steps steps from the same state (conserved quantity compared at the end); the FP32
-    run then continues for nsteps timed steps."""
+def measure_large_mtk(n=256, nsteps=1000, cmp_steps=100):
+    """Config 5: a large single system (periodic n^3 lattice, 20% clustered defects, two
+    states per type) under NHC + MTK NPT at 300 K and 100 MPa, dt = 2 fs, through
+    VerletIntegrator (device=True routes it to the lattice engine). FP64 and FP32 cells run
+    the same cmp_steps steps from the same state (conserved quantity and energy compared at
+    the end); the FP32 run then continues for nsteps timed steps, with the conserved quantity
+    recorded before and after them."""
     import torch
 
     from micmec_gb300 import lattices, units
@@ -400,14 +426,14 @@ def measure_large_mtk(n=256, nsteps=100, cmp_steps=4):
            "host_setup_s": t_setup}
 
     class Econs(Hook):
-        # fires after step 2 and after step 2 + cmp_steps only (a per-step host hook would
-        # bring the state back to the host every step)
+        # fires only where it is scheduled (a per-step host hook would bring the state back
+        # to the host every step)
         def __init__(self):
             Hook.__init__(self, 2, cmp_steps)
             self.rows = []
 
         def __call__(self, it):
-            self.rows.append((it.counter, it.econs, it.epot))
+            self.rows.append((it.counter, it.econs, it.epot, it.ekin))
 
     vel = None
     end = {}
@@ -430,24 +456,136 @@ def measure_large_mtk(n=256, nsteps=100, cmp_steps=4):
         vi.run(cmp_steps)
         torch.cuda.synchronize()
         t_cmp = time.perf_counter() - t0
-        (c0, e0, p0), (c1, e1, p1) = rec.rows[-2], rec.rows[-1]
-        end[prec] = (e1, p1)
-        res = {"econs_change_over_cmp_steps": e1 - e0, "epot": p1}
-        if prec == "fp64":
-            res.update({"steps": cmp_steps, "s": t_cmp, "cell_steps_per_s": n ** 3 * cmp_steps / t_cmp})
-        else:
-            rec.step = 10 ** 9  # no further host hook calls in the timed run
+        (c0, e0, p0, k0), (c1, e1, p1, k1) = rec.rows[-2], rec.rows[-1]
+        end[prec] = (e1, p1, k1)
+        res = {"econs_change_over_cmp_steps": e1 - e0, "epot": p1, "ekin": k1,
+               "cmp_s": t_cmp, "cmp_cell_steps_per_s": n ** 3 * cmp_steps / t_cmp}
+        if prec == "fp32":
+            rec.start, rec.step = 2 + cmp_steps + nsteps, 1  # one call, after the timed run
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             vi.run(nsteps)
             torch.cuda.synchronize()
             dt = time.perf_counter() - t0
-            res.update({"steps": nsteps, "s": dt, "cell_steps_per_s": n ** 3 * nsteps / dt})
+            c2, e2, p2, k2 = rec.rows[-1]
+            res.update({"steps": nsteps, "s": dt, "cell_steps_per_s": n ** 3 * nsteps / dt,
+                        "econs_change_over_steps_rel": (e2 - e1) / abs(p2 + k2),
+                        "epot_change_over_steps_rel": (p2 - p1) / abs(p2 + k2)})
         out[prec] = res
         del vi, ff, s
         torch.cuda.empty_cache()
     out["cmp_steps"] = cmp_steps
-    out["econs_fp32_minus_fp64_rel"] = float((end["fp32"][0] - end["fp64"][0]) / abs(end["fp64"][1]))
+    etot = abs(end["fp64"][1] + end["fp64"][2])
+    out["fp32_minus_fp64_after_cmp_steps_rel"] = {
+        "econs": float((end["fp32"][0] - end["fp64"][0]) / etot),
+        "epot": float((end["fp32"][1] - end["fp64"][1]) / etot),
+        "ekin": float((end["fp32"][2] - end["fp64"][2]) / etot)}
+    return out
+
+
+def lattice_md_rate(s, vel, model, precision, nsteps, flush):
+    """Langevin NVT steps (300 K, 100 fs, dt 1 fs) of a lattice through the MD session API:
+    per-step CUDA events with L2 flushed before every step, and the per-kernel event times
+    (cells, nodes) from mm_md_time_kernels. Returns (cell-steps/s, ms/step, cell ms, node ms)."""
+    import torch
+
+    from micmec_gb300 import _native as nat, units
+    from micmec_gb300.pes.mmff import ForcePartMechanical
+
+    L = nat.lib()
+    dev = flush.device
+    fp = ForcePartMechanical(s, model=model, precision=precision)
+    stream = torch.cuda.current_stream().cuda_stream
+    pos_d = torch.from_numpy(np.ascontiguousarray(s.pos)).to(dev)
+    vel_d = torch.from_numpy(np.ascontiguousarray(vel)).to(dev)
+    dt, tau = 1.0 * units.femtosecond, 100.0 * units.femtosecond
+    nat.check(L.mm_md_begin(fp.handle, pos_d.data_ptr(), vel_d.data_ptr(), dt, 1, 300.0, tau, SEED, None, 0, stream),
+              "mm_md_begin")
+    for _ in range(3):
+        nat.check(L.mm_md_advance(fp.handle, 1, None, 0, stream), "mm_md_advance")
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nsteps)]
+    for i in range(nsteps):
+        flush.fill_(i & 0xFF)
+        ev[i][0].record()
+        nat.check(L.mm_md_advance(fp.handle, 1, None, 0, stream), "mm_md_advance")
+        ev[i][1].record()
+    torch.cuda.synchronize()
+    ms = float(sum(a.elapsed_time(b) for a, b in ev))
+    mc, mn = nat.c_double(), nat.c_double()
+    nat.check(L.mm_md_time_kernels(fp.handle, nsteps, flush.data_ptr(), FLUSH_BYTES, nat.ctypes.byref(mc),
+                                   nat.ctypes.byref(mn), stream), "mm_md_time_kernels")
+    nat.check(L.mm_md_advance(fp.handle, 1, None, 1, stream), "mm_md_advance")
+    torch.cuda.synchronize()
+    del fp
+    return s.ncells * nsteps / (ms * 1e-3), ms / nsteps, mc.value / nsteps, mn.value / nsteps
+
+
+def measure_models(flush, sizes=(64, 256)):
+    """The averaged-matrix model the reference's mmff.py imports (nanocell_original.py) beside
+    the eight-corner-matrix model, FP32 cells, Langevin NVT, on the two-type two-state lattice
+    (10% defects) at each size: step rate, per-kernel times and the HBM fraction of the step's
+    97 algorithmic bytes per cell-step and of the cell kernel's 109 bytes per cell."""
+    import torch
+
+    from micmec_gb300 import lattices, units
+    from micmec_gb300.system import System
+
+    hbm, kind = peaks()
+    out = {"peak_gbs": hbm, "peak_kind": kind}
+    for n in sizes:
+        rng = np.random.default_rng(SEED + n)
+        d = lattices.make_lattice(lattices.defect_grid(n, DEFECT, rng), nstates=2, device=n > 128)
+        d["pos"] = lattices.displace(d["pos"], 0.05 * units.angstrom, rng)
+        s = System.from_dict(d)
+        vel = rng.normal(0.0, 1.0, s.pos.shape) * np.sqrt(units.boltzmann * 300.0 / s.masses)[:, None]
+        vel -= (s.masses @ vel) / s.masses.sum()
+        for model in ("original", "nanocell"):
+            steps = 20 if n <= 64 else 10
+            v, ms, cms, nms = lattice_md_rate(s, vel, model, "fp32", steps, flush)
+            M = s.ncells
+            out["%s_%d" % (model, n)] = {
+                "cell_steps_per_s": v, "ms_per_step": ms, "cells_ms": cms, "nodes_ms": nms,
+                "step_hbm_gbs": STEP_BYTES * M / (ms * 1e-3) / 1e9,
+                "step_hbm_frac": STEP_BYTES * M / (ms * 1e-3) / 1e9 / hbm,
+                "cell_kernel_hbm_gbs": CELL_KERNEL_BYTES * M / (cms * 1e-3) / 1e9,
+                "cell_kernel_hbm_frac": CELL_KERNEL_BYTES * M / (cms * 1e-3) / 1e9 / hbm}
+        del s, d
+        torch.cuda.empty_cache()
+    return out
+
+
+def measure_drift_nve(s, vel, nsteps=1000):
+    """Energy conservation of the 64^3 workload lattice under plain velocity Verlet (NVE,
+    dt = 1 fs) for FP64 and FP32 cells: change and spread of epot + ekin over nsteps steps
+    relative to |epot + ekin| (the records of the device MD loop, one per step)."""
+    import torch
+
+    from micmec_gb300 import _native as nat, units
+    from micmec_gb300.pes.mmff import ForcePartMechanical
+
+    L = nat.lib()
+    out = {"lattice": [N_SIDE] * 3, "steps": nsteps, "timestep_fs": 1.0, "ensemble": "NVE"}
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream().cuda_stream
+    for prec in ("fp64", "fp32"):
+        fp = ForcePartMechanical(s, model="nanocell", precision=prec)
+        e0 = fp.compute()
+        ek0 = 0.5 * float(np.sum(s.masses[:, None] * vel ** 2))
+        pos_d = torch.from_numpy(np.ascontiguousarray(s.pos)).to(dev)
+        vel_d = torch.from_numpy(np.ascontiguousarray(vel)).to(dev)
+        rec = torch.zeros((nsteps, nat.MM_REC_LEN), dtype=torch.float64, device=dev)
+        nat.check(L.mm_md_run(fp.handle, pos_d.data_ptr(), vel_d.data_ptr(), nsteps, 1.0 * units.femtosecond, 0, 0.0,
+                              1.0, SEED, None, rec.data_ptr(), 0, stream), "mm_md_run")
+        r = rec.cpu().numpy()
+        econs = np.concatenate([[e0 + ek0], r[:, 0] + r[:, 1]])
+        ref = abs(econs[0])
+        slope = np.polyfit(np.arange(nsteps + 1), econs, 1)[0]
+        out[prec] = {"econs_change_rel": float((econs[-1] - econs[0]) / ref),
+                     "econs_trend_per_1000_steps_rel": float(slope * 1000 / ref),
+                     "econs_spread_rel": float((econs.max() - econs.min()) / ref),
+                     "ekin_mean_over_initial": float(r[:, 1].mean() / ek0)}
+        del fp
     return out
 
 
@@ -594,20 +732,27 @@ def measure_config4(n=16, npts=11, nsteps=200, every=20):
         for t, v in zip(tensors, saved):
             t.copy_(v)
     t_setup = time.perf_counter() - t_start
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    loss0, grads, _, _ = evaluate((sig_t, f_t), grad=True)
-    torch.cuda.synchronize()
-    t_grad = time.perf_counter() - t0
-    t0 = time.perf_counter()
+    # one untimed evaluation of each kind, then the median of `reps` timed ones
+    reps = 3
+    evaluate((sig_t, f_t), grad=True)
     evaluate((sig_t, f_t))
-    t_loss = time.perf_counter() - t0
-    errs = []
-    picks = [(0, (0, 0, 0)), (0, (1, 0, 1)), (1, (0, 0, 1, 1))]
-    for which, idx in picks:
+    t_grads, t_losses = [], []
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        loss0, grads, _, _ = evaluate((sig_t, f_t), grad=True)
+        torch.cuda.synchronize()
+        t_grads.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        evaluate((sig_t, f_t))
+        torch.cuda.synchronize()
+        t_losses.append(time.perf_counter() - t0)
+    t_grad, t_loss = float(np.median(t_grads)), float(np.median(t_losses))
+
+    def central(which, idx, hrel):
         t = tensors[which]
         base = float(t.detach()[idx])
-        h = 1e-4 * abs(base)
+        h = hrel * abs(base)
         vals = []
         for sgn in (1, -1):
             with torch.no_grad():
@@ -615,12 +760,34 @@ def measure_config4(n=16, npts=11, nsteps=200, every=20):
             vals.append(evaluate((sig_t, f_t))[0])
         with torch.no_grad():
             t[idx] = base
-        fd = (vals[0] - vals[1]) / (2 * h)
+        return (vals[0] - vals[1]) / (2 * h)
+
+    errs = []
+    picks = [(0, (0, 0, 0)), (0, (1, 0, 1)), (1, (0, 0, 1, 1))]
+    for which, idx in picks:
+        fd = central(which, idx, 1e-4)
         errs.append(abs(float(grads[which][idx]) - fd) / max(abs(fd), 1e-300))
+    # the h0 component: central differences over a range of steps and their Richardson
+    # extrapolation (D(h) - D(2h)) / 3 + D(h), which removes the O(h^2) truncation term
+    which, idx = picks[2]
+    g_adj = float(grads[which][idx])
+    sweep = {}
+    prev = None
+    for hrel in (4e-4, 2e-4, 1e-4, 5e-5, 2.5e-5, 1e-5):
+        fd = central(which, idx, hrel)
+        entry = {"fd_rel_err": abs(g_adj - fd) / abs(fd)}
+        if prev is not None and abs(prev[0] / hrel - 2.0) < 1e-9:
+            rich = fd + (fd - prev[1]) / 3.0
+            entry["richardson_rel_err"] = abs(g_adj - rich) / abs(rich)
+        sweep["%g" % hrel] = entry
+        prev = (hrel, fd)
     return {"lattice": [n] * 3, "strain_points": npts, "trajectory_steps": nsteps, "checkpoint_every": every,
-            "loss": loss0, "loss_s": t_loss, "loss_and_gradient_s": t_grad, "setup_s": t_setup,
+            "loss": loss0, "loss_s": t_loss, "loss_and_gradient_s": t_grad,
+            "grad_over_fwd": t_grad / t_loss, "timing": "median of %d after one untimed evaluation of each" % reps,
+            "loss_s_all": t_losses, "loss_and_gradient_s_all": t_grads, "setup_s": t_setup,
             "relax_iterations_max": max(relax_iters), "fd_rel_err": errs, "fd_h": "1e-4 relative",
-            "fd_params": ["C11 type 0 state 0", "C12 type 1 state 0", "h0_yy type 0 state 0"]}
+            "fd_params": ["C11 type 0 state 0", "C12 type 1 state 0", "h0_yy type 0 state 0"],
+            "h0_yy_step_sweep": sweep}
 
 
 def measure_grad_over_fwd(n=16, reps=5):
@@ -873,18 +1040,28 @@ def run_gpu(args):
             line["general_params_fp32"] = {"value": vg, "unit": UNIT, "ms_per_step": msg,
                                            "note": "anisotropic C, sheared h0: full 3x3/6x6 products"}
             systems, strains = batch_workload()
-            bf = measure_batch(systems, strains, "fp32", 200, 400)
-            bd = measure_batch(systems, strains, "fp64", 20, 100)
-            plain = measure_plain_per_system(systems[:6], 10)
+            bf = measure_batch(systems, strains, "fp32", 2000, 400, drift=True)
+            bd = measure_batch(systems, strains, "fp64", 100, 100)
+            # the plain FP64 GPU path, one system at a time: a sample across the size range
+            sample = sorted(systems, key=lambda s: s.ncells)[:: max(1, len(systems) // 8)][:8]
+            plain_dev = measure_plain_per_system(sample, 50, device=True)
+            plain_host = measure_plain_per_system(sample[:4], 5, device=False)
             sx32 = np.array(list(bf["stress_xx_gpa_by_strain"].values()))
             sx64 = np.array(list(bd["stress_xx_gpa_by_strain"].values()))
             bf["stress_rel_err_vs_fp64"] = float(np.abs(sx32 - sx64).max() / np.abs(sx64).max())
-            line["batched"] = {"fp32": bf, "fp64": bd, "plain_fp64_per_system": plain,
-                               "batched_fp32_over_plain_fp64_systems_per_s":
-                                   bf["systems_steps_per_s"] / plain["systems_steps_per_s"]}
+            line["batched"] = {
+                "fp32": bf, "fp64": bd, "plain_fp64_per_system_device_hooks": plain_dev,
+                "plain_fp64_per_system_host_hooks": plain_host,
+                "batched_fp32_over_batched_fp64_systems_per_s": bf["systems_steps_per_s"] / bd["systems_steps_per_s"],
+                "batched_fp32_over_plain_fp64_device_systems_per_s":
+                    bf["systems_steps_per_s"] / plain_dev["systems_steps_per_s"],
+                "batched_fp32_over_plain_fp64_host_hooks_systems_per_s":
+                    bf["systems_steps_per_s"] / plain_host["systems_steps_per_s"]}
         except Exception as exc:  # extra measurements never block the main line
             line["extra_error"] = _error_text(exc)
-        for key, fn in (("builder", measure_builder), ("adjoint", measure_grad_over_fwd),
+        for key, fn in (("drift_nve_64", lambda: measure_drift_nve(s, vel)),
+                        ("models_fp32", lambda: measure_models(flush)),
+                        ("builder", measure_builder), ("adjoint", measure_grad_over_fwd),
                         ("differentiation_16cubed", measure_config4), ("large_mtk", measure_large_mtk)):
             try:
                 line[key] = fn()

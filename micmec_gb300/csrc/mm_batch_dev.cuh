@@ -205,9 +205,10 @@ __device__ MM_FORCES_INLINE void forces(const BArgs& a, Shared<T>& sh, const BSy
   // narrow), converted once per system in the CTA sum
   F2 facc[10];
   for (int i = 0; i < 10; ++i) facc[i] = F2{0.0f, 0.0f};
-  if (MODEL >= 1 && M >= kCell1MinCellsPerThread * (int)blockDim.x) {
-    // eight corner matrices, one thread per cell (systems with at least a cell per thread);
-    // a thread's few cells are summed in the cell precision, then join the CTA sums below
+  if (MODEL == 0 || M >= kCell1MinCellsPerThread * (int)blockDim.x) {
+    // one thread per cell: the averaged-matrix model always, the eight-corner-matrix model
+    // for systems with at least a cell per thread; a thread's few cells are summed in the
+    // cell precision, then join the CTA sums below
     T vs[10];
 #pragma unroll
     for (int q = 0; q < 10; ++q) vs[q] = T(0);
@@ -222,7 +223,7 @@ __device__ MM_FORCES_INLINE void forces(const BArgs& a, Shared<T>& sh, const BSy
         for (int x = 0; x < 3; ++x) du[b][x] = disp[x * N3 + sy.off + node];
       }
       T g[8][3];
-      const T E = cell1_eval<T, MODEL == 2>(du, sh.tp[a.ctype[sy.off + cell]], g);
+      const T E = cell1_eval<T, MODEL == 2, (MODEL == 0 ? 0 : 1)>(du, sh.tp[a.ctype[sy.off + cell]], g);
 #pragma unroll
       for (int kc = 0; kc < 8; ++kc)
 #pragma unroll
@@ -245,7 +246,7 @@ __device__ MM_FORCES_INLINE void forces(const BArgs& a, Shared<T>& sh, const BSy
       if constexpr (sizeof(T) == 4) facc[q] = F2{vs[q], 0.0f};
       else acc[q] = (double)vs[q];
     }
-  } else if (MODEL >= 1) {  // eight lanes per cell (small systems); MODEL 2: diagonal h0, cubic stress maps
+  } else {  // eight lanes per cell (small systems); MODEL 2: diagonal h0, cubic stress maps
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, av = threadIdx.x & 7;
     const int ngroups = (M + 3) / 4;
     const int nw = blockDim.x >> 5;
@@ -287,32 +288,9 @@ __device__ MM_FORCES_INLINE void forces(const BArgs& a, Shared<T>& sh, const BSy
         }
       }
     }
-  } else {
-    for (int cell = threadIdx.x; cell < M; cell += blockDim.x) {
-      int i, j, k;
-      grid_coords(sy, cell, i, j, k);
-      T du[8][3];
-      for (int b = 0; b < 8; ++b) {
-        const int node = wrap_node(sy, i + (b & 1), j + ((b >> 1) & 1), k + (b >> 2));
-        for (int x = 0; x < 3; ++x) du[b][x] = disp[x * N3 + sy.off + node];
-      }
-      T g[8][3];
-      const double E = cell_eval<T, 0>(du, sh.tp[a.ctype[sy.off + cell]], g);
-      for (int kc = 0; kc < 8; ++kc)
-        for (int x = 0; x < 3; ++x) G[(kc * 3 + x) * (size_t)M + cell] = g[corner_to_bits(kc)][x];
-      acc[0] += E;
-      for (int b = 1; b < 8; ++b)
-        for (int y = 0; y < 3; ++y) {
-          T rr = du[b][y] - du[0][y];
-          if (b & 1) rr += sh.L[0 * 3 + y];
-          if (b & 2) rr += sh.L[1 * 3 + y];
-          if (b & 4) rr += sh.L[2 * 3 + y];
-          for (int x = 0; x < 3; ++x) acc[1 + x * 3 + y] += (double)(g[b][x] * rr);
-        }
-    }
   }
   // (the CTA sum's barrier also orders every corner-gradient write before the gather)
-  if constexpr (sizeof(T) == 4 && MODEL >= 1) {
+  if constexpr (sizeof(T) == 4) {
     block_sum_f2_pairs<10>(facc, sh.red);
     if (threadIdx.x < 32) {
       const double t = f2_total_of_lane<10>(facc);

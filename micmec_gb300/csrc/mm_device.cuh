@@ -726,6 +726,70 @@ __device__ __forceinline__ T cell_state_energy_grad(const T (&du)[8][3], const S
   return E + sv.df(p);
 }
 
+// The averaged-matrix model (nanocell_original.py:46-132) by one thread: the cell matrix
+// minus the rest matrix has rows W_d = B_d + (sum of the four edge vectors along d) / 4;
+// the energy is that of one strain with scale det(h0), and row d of its gradient is spread
+// over the four edges along d with weight 1/4.
+template <typename T, bool SIMPLE>
+__device__ __forceinline__ void average_w(const T (&du)[8][3], const StateView<T, SIMPLE>& sv, const StateParams<T>& p,
+                                          T (&W)[9]) {
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      T e = T(0);
+#pragma unroll
+      for (int lo = 0; lo < 8; ++lo)
+        if (!((lo >> d) & 1)) e += du[lo | (1 << d)][c] - du[lo][c];
+      W[d * 3 + c] = sv.B(p, d * 3 + c) + T(0.25) * e;
+    }
+}
+
+template <typename T, bool SIMPLE>
+__device__ __forceinline__ T avg_state_energy(const T (&du)[8][3], const StateParams<T>& p) {
+  StateView<T, SIMPLE> sv;
+  sv.load(p);
+  T W[9], D[9], st[6];
+  average_w<T, SIMPLE>(du, sv, p, W);
+  return state_energy<T, SIMPLE>(W, sv.params(p), sv.v0(p), D, st) + sv.df(p);
+}
+
+template <typename T, bool SIMPLE>
+__device__ __forceinline__ T avg_state_energy_grad(const T (&du)[8][3], const StateParams<T>& p, T weight,
+                                                   T (&g)[8][3]) {
+  StateView<T, SIMPLE> sv;
+  sv.load(p);
+  T W[9], D[9], st[6], GW[9];
+  average_w<T, SIMPLE>(du, sv, p, W);
+  const T E = state_energy<T, SIMPLE>(W, sv.params(p), sv.v0(p), D, st);
+  state_gradient<T, SIMPLE>(D, st, sv.params(p), T(0.25) * sv.v0(p) * weight, GW);
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+#pragma unroll
+    for (int lo = 0; lo < 8; ++lo)
+      if (!((lo >> d) & 1))
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          g[lo | (1 << d)][c] += GW[d * 3 + c];
+          g[lo][c] -= GW[d * 3 + c];
+        }
+  return E + sv.df(p);
+}
+
+// Energy (with free energy) of one state of a cell, MODEL 0 averaged matrix, 1 eight
+// corner matrices; and the same with the state's gradient times `weight` added to g.
+template <typename T, int MODEL, bool SIMPLE>
+__device__ __forceinline__ T model_state_energy(const T (&du)[8][3], const StateParams<T>& p) {
+  if constexpr (MODEL == 0) return avg_state_energy<T, SIMPLE>(du, p);
+  else return cell_state_energy<T, SIMPLE>(du, p);
+}
+template <typename T, int MODEL, bool SIMPLE>
+__device__ __forceinline__ T model_state_energy_grad(const T (&du)[8][3], const StateParams<T>& p, T weight,
+                                                     T (&g)[8][3]) {
+  if constexpr (MODEL == 0) return avg_state_energy_grad<T, SIMPLE>(du, p, weight, g);
+  else return cell_state_energy_grad<T, SIMPLE>(du, p, weight, g);
+}
+
 // Cell energy (multi-state -kT log-sum-exp, micmec/pes/mmff.py:377-398) and vertex
 // gradients g (offset-bits order) of one cell, evaluated by one thread. State 0's energy
 // and gradient come from one pass over the corners, the other states' energies from one
@@ -733,20 +797,20 @@ __device__ __forceinline__ T cell_state_energy_grad(const T (&du)[8][3], const S
 // lowest energy is known by then, and usually every state but one is that far up); state
 // 0's gradient is rescaled by its weight, and the other states are evaluated again with
 // their weight folded into the gradient scale.
-template <typename T, bool SIMPLE>
+template <typename T, bool SIMPLE, int MODEL = 1>
 __device__ __forceinline__ T cell1_eval(const T (&du)[8][3], const TypeParams<T>& p, T (&g)[8][3]) {
 #pragma unroll
   for (int b = 0; b < 8; ++b)
 #pragma unroll
     for (int x = 0; x < 3; ++x) g[b][x] = T(0);
-  T Ecell = cell_state_energy_grad<T, SIMPLE>(du, p.s[0], T(1), g);
+  T Ecell = model_state_energy_grad<T, MODEL, SIMPLE>(du, p.s[0], T(1), g);
   const int ns = p.nstates;
   if (ns > 1) {
     T E[MM_MAX_STATES];
     E[0] = Ecell;
     T m = Ecell;
     for (int s = 1; s < ns; ++s) {
-      E[s] = cell_state_energy<T, SIMPLE>(du, p.s[s]);
+      E[s] = model_state_energy<T, MODEL, SIMPLE>(du, p.s[s]);
       m = E[s] < m ? E[s] : m;
     }
     const T kT = p.kT;
@@ -766,7 +830,7 @@ __device__ __forceinline__ T cell1_eval(const T (&du)[8][3], const TypeParams<T>
       for (int x = 0; x < 3; ++x) g[b][x] *= f0;
     for (int s = 1; s < ns; ++s)
       if (E[s] - m < T(50) * kT)
-        cell_state_energy_grad<T, SIMPLE>(du, p.s[s], lse_weight<T>(m - E[s], kT, p.lkT) * inv, g);
+        model_state_energy_grad<T, MODEL, SIMPLE>(du, p.s[s], lse_weight<T>(m - E[s], kT, p.lkT) * inv, g);
     Ecell = m - kT * lse_log<T>(wsum);
   }
   return Ecell;

@@ -429,10 +429,10 @@ __global__ void __launch_bounds__(kCell8Threads, sizeof(T) == 4 ? 3 : 2) k_cells
   }
 }
 
-// One thread per cell for the eight-corner-matrix model (cell1_eval): the thread gathers
-// its cell's eight corner displacements and evaluates all eight corner matrices itself, so
-// there are no lane exchanges, no per-corner index arithmetic and no staging of virial terms
-// (the cell's gradient and vertex offsets stay in registers). Corner gradients are written
+// One thread per cell (cell1_eval), both energy models: the thread gathers its cell's eight
+// corner displacements and evaluates the cell itself (eight corner matrices or the averaged
+// one), so there are no lane exchanges, no per-corner index arithmetic and no staging of
+// virial terms (the cell's gradient and vertex offsets stay in registers). Corner gradients are written
 // as in k_cells8 (corner-major, coalesced across the threads of a warp). A thread's few
 // cells are summed in the cell precision; the per-block sums are compensated FP32 pairs
 // (FP32 cells) or doubles, value-major: slot 0 energy, 1 + 3x + y virial.
@@ -442,7 +442,7 @@ constexpr int kCell1Threads = 128;
 #endif
 constexpr int kCell1MinBlocks = MM_CELL1_MINB;  // FP32: resident blocks per SM the registers are sized for
 
-template <typename T, bool STRUCT, bool SIMPLE>
+template <typename T, int MODEL, bool STRUCT, bool SIMPLE>
 __global__ void __launch_bounds__(kCell1Threads, sizeof(T) == 4 ? kCell1MinBlocks : 2)
     k_cells1(Topo t, const TypeTable* __restrict__ tt, int ntypes, const double* __restrict__ box,
              const T* __restrict__ disp, T* __restrict__ G, double* __restrict__ ecell, double* __restrict__ cpart) {
@@ -477,7 +477,7 @@ __global__ void __launch_bounds__(kCell1Threads, sizeof(T) == 4 ? kCell1MinBlock
       }
     }
     T g[8][3];
-    const T Ecell = cell1_eval<T, SIMPLE>(du, tp[t.cell_type[cell]], g);
+    const T Ecell = cell1_eval<T, SIMPLE, MODEL>(du, tp[t.cell_type[cell]], g);
 #pragma unroll
     for (int kc = 0; kc < 8; ++kc)
 #pragma unroll
@@ -1012,8 +1012,8 @@ static void topo_of(const mm_handle* h, Topo& t) {
 static size_t cell_smem(const mm_handle* h) {
   const size_t esz = h->prec == MM_PREC_FP32 ? sizeof(float) : sizeof(double);
   const size_t tp = (h->prec == MM_PREC_FP32 ? sizeof(TypeParams<float>) : sizeof(TypeParams<double>)) * h->ntypes;
-  if (h->model == MM_MODEL_NANOCELL && h->cell_kernel == 8) return ((tp + 15) / 16) * 16 + 2 * esz * kTileElems;
-  if (h->model == MM_MODEL_NANOCELL) return ((tp + 15) / 16) * 16 + sizeof(double) * kCellPart * (kCell1Threads / 32);
+  if (h->cell_kernel == 1) return ((tp + 15) / 16) * 16 + sizeof(double) * kCellPart * (kCell1Threads / 32);
+  if (h->model == MM_MODEL_NANOCELL) return ((tp + 15) / 16) * 16 + 2 * esz * kTileElems;
   return ((tp + 15) / 16) * 16 + sizeof(double) * kCellPart * (kCellThreads / 32);
 }
 
@@ -1029,9 +1029,13 @@ static int occupancy_of(K kern, int threads, size_t smem) {
 
 template <typename T, bool STRUCT>
 static int cell8_occupancy(const mm_handle* h) {
-  if (h->cell_kernel == 1)
-    return h->simple ? occupancy_of(k_cells1<T, STRUCT, true>, kCell1Threads, cell_smem(h))
-                     : occupancy_of(k_cells1<T, STRUCT, false>, kCell1Threads, cell_smem(h));
+  if (h->cell_kernel == 1) {
+    if (h->model == MM_MODEL_ORIGINAL)
+      return h->simple ? occupancy_of(k_cells1<T, 0, STRUCT, true>, kCell1Threads, cell_smem(h))
+                       : occupancy_of(k_cells1<T, 0, STRUCT, false>, kCell1Threads, cell_smem(h));
+    return h->simple ? occupancy_of(k_cells1<T, 1, STRUCT, true>, kCell1Threads, cell_smem(h))
+                     : occupancy_of(k_cells1<T, 1, STRUCT, false>, kCell1Threads, cell_smem(h));
+  }
   return h->simple ? occupancy_of(k_cells8<T, STRUCT, true>, kCell8Threads, cell_smem(h))
                    : occupancy_of(k_cells8<T, STRUCT, false>, kCell8Threads, cell_smem(h));
 }
@@ -1041,15 +1045,17 @@ static void launch_cells_t(mm_handle* h, cudaStream_t st, double* ecell) {
   Topo t;
   topo_of(h, t);
   const int nblk = cell_grid(h);
-  if constexpr (MODEL == 1) {
-    if (h->cell_kernel == 1) {
-      if (h->simple)
-        launch_pdl(k_cells1<T, STRUCT, true>, nblk, kCell1Threads, cell_smem(h), st, t, (const TypeTable*)h->d_tt,
-                   h->ntypes, (const double*)h->d_box, (const T*)h->d_disp, (T*)h->d_G, ecell, h->d_cpart);
-      else
-        launch_pdl(k_cells1<T, STRUCT, false>, nblk, kCell1Threads, cell_smem(h), st, t, (const TypeTable*)h->d_tt,
-                   h->ntypes, (const double*)h->d_box, (const T*)h->d_disp, (T*)h->d_G, ecell, h->d_cpart);
-    } else if (h->simple)
+  if (h->cell_kernel == 1) {
+    if (h->simple)
+      launch_pdl(k_cells1<T, MODEL, STRUCT, true>, nblk, kCell1Threads, cell_smem(h), st, t,
+                 (const TypeTable*)h->d_tt, h->ntypes, (const double*)h->d_box, (const T*)h->d_disp, (T*)h->d_G,
+                 ecell, h->d_cpart);
+    else
+      launch_pdl(k_cells1<T, MODEL, STRUCT, false>, nblk, kCell1Threads, cell_smem(h), st, t,
+                 (const TypeTable*)h->d_tt, h->ntypes, (const double*)h->d_box, (const T*)h->d_disp, (T*)h->d_G,
+                 ecell, h->d_cpart);
+  } else if constexpr (MODEL == 1) {
+    if (h->simple)
       launch_pdl(k_cells8<T, STRUCT, true>, nblk, kCell8Threads, cell_smem(h), st, t, (const TypeTable*)h->d_tt,
                  h->ntypes, (const double*)h->d_box, (const T*)h->d_disp, (T*)h->d_G, ecell, h->d_cpart);
     else
@@ -1082,21 +1088,19 @@ void launch_cells(mm_handle* h, cudaStream_t st, double* ecell) {
 constexpr int kCell8MaxPerSM = 4, kCell1MaxPerSM = 16;
 
 int cell_blocks(const mm_handle* h) {
-  if (h->model == MM_MODEL_NANOCELL) {
-    // grid-stride over groups of cells with at most the resident blocks of either kernel
-    const int sms = h->num_sms > 0 ? h->num_sms : 152;
-    const int g8 = std::min((h->M + kCell8Cells - 1) / kCell8Cells, sms * kCell8MaxPerSM);
-    const int g1 = std::min((h->M + kCell1Threads - 1) / kCell1Threads, sms * kCell1MaxPerSM);
-    return std::max(g8, g1);
-  }
-  return (h->M + kCellThreads - 1) / kCellThreads;
+  // one-thread kernel: grid-stride with at most kCell1MaxPerSM resident blocks per SM
+  const int sms = h->num_sms > 0 ? h->num_sms : 152;
+  const int g1 = std::min((h->M + kCell1Threads - 1) / kCell1Threads, sms * kCell1MaxPerSM);
+  if (h->model == MM_MODEL_NANOCELL)  // or the eight-lane kernel: grid-stride over groups of cells
+    return std::max(g1, std::min((h->M + kCell8Cells - 1) / kCell8Cells, sms * kCell8MaxPerSM));
+  return std::max(g1, (h->M + kCellThreads - 1) / kCellThreads);  // or one block per kCellThreads cells
 }
 int node_blocks(const mm_handle* h) { return (h->N + kNodeThreads - 1) / kNodeThreads; }
 
 // The nanocell kernel grid-strides over groups of cells with exactly as many blocks
 // as fit on the GPU at once (so no partial second wave), at most 4 per SM.
 int cell_grid(mm_handle* h) {
-  if (h->model != MM_MODEL_NANOCELL) return cell_blocks(h);
+  if (h->model != MM_MODEL_NANOCELL && h->cell_kernel != 1) return (h->M + kCellThreads - 1) / kCellThreads;
   int& occ = h->cell_occ[h->simple ? 1 : 0];
   if (occ == 0) {
     if (h->prec == MM_PREC_FP32) occ = h->structured ? cell8_occupancy<float, true>(h) : cell8_occupancy<float, false>(h);

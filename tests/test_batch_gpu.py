@@ -268,3 +268,22 @@ def test_batch_set_params_matches_single_system_with_the_same_parameters():
     b.relax(max_iter=0, gtol=1e-3)  # one force evaluation, no step
     assert abs(b.energies()[0] - e_part) <= 1e-11 * abs(e_part)
     assert np.abs(b.stress()[0] - vt / s.domain.volume).max() <= 1e-10 * np.abs(vt / s.domain.volume).max()
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("fp32", 1e-5)])
+def test_batch_original_model_matches_single_system_path(precision, tol):
+    """The averaged-matrix model (the one the reference's mmff.py imports) in the batch kernel:
+    energy and stress of uneven systems equal those of ForcePartMechanical(model="original")."""
+    from micmec_gb300.batch import BatchSystems
+    from micmec_gb300.pes.mmff import ForcePartMechanical, MicMecForceField
+
+    systems, _ = _mixed_batch([3, 5, 9, 4], "fp64", seed=12)
+    b = BatchSystems(systems, model="original", precision=precision)
+    b.relax(max_iter=0, gtol=1e-3)  # one force evaluation, no step
+    E, W = b.energies(), b.stress()
+    for i, s in enumerate(systems):
+        vt = np.zeros((3, 3))
+        e = MicMecForceField(s, [ForcePartMechanical(s, model="original", precision="fp64")]).compute(None, vt)
+        assert abs(E[i] - e) <= tol * abs(e)
+        ref = vt / s.domain.volume
+        assert np.abs(W[i] - ref).max() <= tol * np.abs(ref).max()
