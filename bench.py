@@ -1095,6 +1095,10 @@ def main():
     ap.add_argument("--builder-only", type=int, default=0, metavar="N",
                     help="only the device system builder on an N^3 lattice with 20%% clustered defects, built "
                          "--warmup + --steps times (for kernel profiles)")
+    ap.add_argument("--lattice-only", type=int, default=0, metavar="N",
+                    help="only the Langevin step rate of an N^3 two-type two-state lattice with --model and "
+                         "FP32 cells, --steps timed steps after --warmup (for kernel profiles)")
+    ap.add_argument("--model", default="nanocell", choices=["nanocell", "original"])
     ap.add_argument("--batch-only", action="store_true",
                     help="only the batched workload (512 systems, NHC + MTK, FP32 cells): one warm-up launch of "
                          "--warmup steps and one launch of --steps steps, no autotuning or graph (for kernel profiles)")
@@ -1105,6 +1109,8 @@ def main():
         return run_reference(args)
     if args.batch_only:
         return run_batch_only(args)
+    if args.lattice_only:
+        return run_lattice_only(args)
     if args.large_only:
         print(json.dumps(measure_large_mtk(n=args.large_only, nsteps=args.steps)), flush=True)
         return 0
@@ -1114,6 +1120,25 @@ def main():
         print(json.dumps(measure_config4()), flush=True)
         return 0
     return run_gpu(args)
+
+
+def run_lattice_only(args):
+    import torch
+
+    from micmec_gb300 import lattices, units
+    from micmec_gb300.system import System
+
+    n = args.lattice_only
+    rng = np.random.default_rng(SEED + n)
+    d = lattices.make_lattice(lattices.defect_grid(n, DEFECT, rng), nstates=2, device=n > 128)
+    d["pos"] = lattices.displace(d["pos"], 0.05 * units.angstrom, rng)
+    s = System.from_dict(d)
+    vel = rng.normal(0.0, 1.0, s.pos.shape) * np.sqrt(units.boltzmann * 300.0 / s.masses)[:, None]
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    v, ms, cms, nms = lattice_md_rate(s, vel, args.model, "fp32", args.steps, flush)
+    print(json.dumps({"lattice": [n] * 3, "model": args.model, "cell_steps_per_s": v, "ms_per_step": ms,
+                      "cells_ms": cms, "nodes_ms": nms}), flush=True)
+    return 0
 
 
 def run_builder_only(args):

@@ -102,10 +102,16 @@ class MicMecParameters(object):
         return tuple(np.ascontiguousarray(a) for a in (C, H, D))
 
     def upload(self, c21, h0, df):
-        """Push parameter values into the native handle."""
+        """Push parameter values into the native handle (skipped when the handle already holds
+        exactly these tables, as along a trajectory whose steps all use the same values)."""
         C, H, D = self.native_tables(c21, h0, df)
+        last = getattr(self, "_uploaded", None)
+        if last is not None and last[0] == self.part.handle.value and all(
+                np.array_equal(a, b) for a, b in zip(last[1:], (C, H, D))):
+            return
         nat.check(nat.lib().mm_set_params(self.part.handle, H.ctypes.data, C.ctypes.data, D.ctypes.data,
                                           self.temp.ctypes.data), "mm_set_params")
+        self._uploaded = (self.part.handle.value, C, H, D)
 
 
 def _adjoint(part, pos, lam, dlattice=None, with_virial=False):
@@ -129,17 +135,20 @@ def _adjoint(part, pos, lam, dlattice=None, with_virial=False):
 
 
 def _slots_to_params(slot, params, device):
-    """dL/d(raw slot) (T, 4, 46): [dE/dA (36), dE/dh0 (9), dE/dF (1)] -> (c21, h0, free energy)."""
+    """dL/d(raw slot) (T, 4, 46): [dE/dA (36), dE/dh0 (9), dE/dF (1)] -> (c21, h0, free energy),
+    formed on the slot tensor's device (no host round trip)."""
+    sdev = slot.device
     dA = slot[..., :36].reshape(slot.shape[:2] + (6, 6))
-    w = torch.tensor([1.0, 1.0, 1.0, 2.0, 2.0, 2.0], dtype=torch.float64)
+    w = torch.tensor([1.0, 1.0, 1.0, 2.0, 2.0, 2.0], dtype=torch.float64, device=sdev)
     dCv = dA * w  # A = C_v diag(w)  ->  dL/dC_v[p, q] = dL/dA[p, q] w_q
-    i0, i1 = torch.as_tensor(_IU[0]), torch.as_tensor(_IU[1])
+    i0, i1 = torch.as_tensor(_IU[0], device=sdev), torch.as_tensor(_IU[1], device=sdev)
     dC21 = dCv[..., i0, i1] + torch.where(i0 != i1, dCv[..., i1, i0], torch.zeros_like(dCv[..., i0, i1]))
     dh0 = slot[..., 36:45].reshape(slot.shape[:2] + (3, 3))
     ddf = slot[..., 45]
     mask = torch.zeros(slot.shape[:2], dtype=torch.float64)
     for t, n in enumerate(params.nstates):
         mask[t, :n] = 1.0
+    mask = mask.to(sdev)
     return (dC21 * mask[..., None]).to(device), (dh0 * mask[..., None, None]).to(device), (ddf * mask).to(device)
 
 
@@ -161,9 +170,8 @@ class _EnergyGrad(torch.autograd.Function):
         gE = gE if gE is not None else torch.zeros((), dtype=torch.float64, device=pos.device)
         energy, gpos, hvp, pg = _adjoint(params.part, pos, lam)
         grad_pos = gE * gpos + hvp
-        # dL/dtheta per slot: gE * value + tangent (small: on the host)
-        pg = pg.cpu()
-        slot = float(gE) * pg[..., 0] + pg[..., 1]  # (T, 4, 46)
+        # dL/dtheta per slot: gE * value + tangent, kept on the device
+        slot = gE * pg[..., 0] + pg[..., 1]  # (T, 4, 46)
         dC21, dh0, ddf = _slots_to_params(slot, params, c21.device)
         return grad_pos, dC21, dh0, ddf, None
 
@@ -179,18 +187,20 @@ def _hessian_solve(part, pos, rhs, tol=1e-11, maxiter=5000):
     x = torch.zeros_like(b)
     r = b.clone()
     p = r.clone()
-    rr = float((r * r).sum())
+    rr = (r * r).sum()
     b2 = float((b * b).sum())
     if b2 == 0.0:
         return x
-    for _ in range(maxiter):
+    # the scalars stay device tensors; convergence is read back every `check` iterations only
+    check = 8
+    for it in range(maxiter):
         Ap = H(p)
         Ap = Ap - Ap.mean(dim=0)
-        alpha = rr / float((p * Ap).sum())
+        alpha = rr / (p * Ap).sum()
         x = x + alpha * p
         r = r - alpha * Ap
-        rr_new = float((r * r).sum())
-        if rr_new <= tol * tol * b2:
+        rr_new = (r * r).sum()
+        if it % check == check - 1 and float(rr_new) <= tol * tol * b2:
             break
         p = r + (rr_new / rr) * p
         rr = rr_new
@@ -235,7 +245,7 @@ def relaxed_stress_gradient(pos, params, w, tol=1e-11):
     q = (hvp + g @ epst.T) / V  # ds/dx: Hessian-tangent part + derivative of the tangent u eps
     mu = _hessian_solve(part, pos, q, tol=tol)
     pg_mu = _adjoint(part, pos, mu)[3]
-    slot = (pg[..., 1] / V - pg_mu[..., 1]).cpu()
+    slot = pg[..., 1] / V - pg_mu[..., 1]
     dC21, dh0, ddf = _slots_to_params(slot, params, params.c21.device)
     return sigma, dC21, dh0, ddf
 
