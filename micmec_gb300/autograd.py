@@ -134,6 +134,22 @@ def _adjoint(part, pos, lam, dlattice=None, with_virial=False):
     return energy, gpos, hvp, pg
 
 
+def _hvp(part, pos, lam):
+    """H lam (H = d2E/dx2 at pos) by one adjoint evaluation that forms nothing else: no
+    gradient, virial or parameter derivatives are written. The result lives in a buffer
+    kept with the part and is overwritten by the next call."""
+    buf = getattr(part, "_hvp_buf", None)
+    if buf is None or buf[1].shape != pos.shape or buf[1].device != pos.device:
+        buf = (torch.zeros(2, dtype=torch.float64, device=pos.device), torch.empty_like(pos))
+        part._hvp_buf = buf
+    energy, hvp = buf
+    st = nat.lib().mm_adjoint(part.handle, pos.contiguous().data_ptr(), lam.contiguous().data_ptr(), None,
+                              energy.data_ptr(), None, hvp.data_ptr(), None, None,
+                              torch.cuda.current_stream().cuda_stream)
+    nat.check(st, "mm_adjoint")
+    return hvp
+
+
 def _slots_to_params(slot, params, device):
     """dL/d(raw slot) (T, 4, 46): [dE/dA (36), dE/dh0 (9), dE/dF (1)] -> (c21, h0, free energy),
     formed on the slot tensor's device (no host round trip)."""
@@ -181,7 +197,7 @@ def _hessian_solve(part, pos, rhs, tol=1e-11, maxiter=5000):
     gradients on the translation-free subspace (rhs and iterates have zero mean)."""
 
     def H(p):
-        return _adjoint(part, pos, p)[2]
+        return _hvp(part, pos, p)
 
     b = rhs - rhs.mean(dim=0)
     x = torch.zeros_like(b)

@@ -235,6 +235,8 @@ __global__ void __launch_bounds__(kAdjThreads) k_cells_adj(AdjTopo t, const Type
       }
     }
     // parameter gradients of the cell energy: weights times state gradients; dE/d(free energy) = weight
+    // (not stored when the caller asked for no parameter gradients, e.g. Hessian products)
+    if (P)
     for (int s = 0; s < MM_MAX_STATES; ++s)
       for (int k = 0; k < kPG; ++k) {
         Dual val = mk(0.0);
@@ -420,12 +422,13 @@ mm_status mm_adjoint(mm_handle* h, const double* pos, const double* lam, const d
   AdjTopo t{h->N, h->M, h->structured, h->nn[0], h->nn[1], h->nn[2], h->d_cell_nodes, h->d_node_cells, h->d_node_lat,
             h->d_cell_type};
   const double* db = dlattice ? dbox : nullptr;
+  double* const Pw = pgrad ? P : nullptr;
   if (h->model == MM_MODEL_ORIGINAL) {
-    if (h->structured) k_cells_adj<0, true><<<nblk, kAdjThreads, 0, st>>>(t, h->d_tt, h->d_box, db, h->d_u, lam, G, Gt, P, cpart);
-    else k_cells_adj<0, false><<<nblk, kAdjThreads, 0, st>>>(t, h->d_tt, h->d_box, db, h->d_u, lam, G, Gt, P, cpart);
+    if (h->structured) k_cells_adj<0, true><<<nblk, kAdjThreads, 0, st>>>(t, h->d_tt, h->d_box, db, h->d_u, lam, G, Gt, Pw, cpart);
+    else k_cells_adj<0, false><<<nblk, kAdjThreads, 0, st>>>(t, h->d_tt, h->d_box, db, h->d_u, lam, G, Gt, Pw, cpart);
   } else {
-    if (h->structured) k_cells_adj<1, true><<<nblk, kAdjThreads, 0, st>>>(t, h->d_tt, h->d_box, db, h->d_u, lam, G, Gt, P, cpart);
-    else k_cells_adj<1, false><<<nblk, kAdjThreads, 0, st>>>(t, h->d_tt, h->d_box, db, h->d_u, lam, G, Gt, P, cpart);
+    if (h->structured) k_cells_adj<1, true><<<nblk, kAdjThreads, 0, st>>>(t, h->d_tt, h->d_box, db, h->d_u, lam, G, Gt, Pw, cpart);
+    else k_cells_adj<1, false><<<nblk, kAdjThreads, 0, st>>>(t, h->d_tt, h->d_box, db, h->d_u, lam, G, Gt, Pw, cpart);
   }
   if (gpos || hvp) {
     const int nb = (h->N + 255) / 256;
