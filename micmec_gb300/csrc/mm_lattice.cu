@@ -457,6 +457,7 @@ __global__ void __launch_bounds__(kCell1Threads, sizeof(T) == 4 ? kCell1MinBlock
   T acc[kCellPart];
 #pragma unroll
   for (int i = 0; i < kCellPart; ++i) acc[i] = T(0);
+  F2 eacc{0.0f, 0.0f};  // FP32 cells: a thread's cell energies summed with compensation
   for (int cell = blockIdx.x * blockDim.x + threadIdx.x; cell < t.M; cell += gridDim.x * blockDim.x) {
     T du[8][3];
     if (STRUCT) {
@@ -483,7 +484,8 @@ __global__ void __launch_bounds__(kCell1Threads, sizeof(T) == 4 ? kCell1MinBlock
 #pragma unroll
       for (int x = 0; x < 3; ++x) G[(kc * 3 + x) * (size_t)t.M + cell] = g[corner_to_bits(kc)][x];
     if (ecell) ecell[cell] = (double)Ecell;
-    acc[0] += Ecell;
+    if constexpr (sizeof(T) == 4) eacc = f2_add(eacc, F2{(float)Ecell, 0.0f});
+    else acc[0] += Ecell;
     // virial: sum_b g_b (x) (r_b - r_0), r_b - r_0 = offset(b) . L + du_b - du_0
 #pragma unroll
     for (int b = 1; b < 8; ++b) {
@@ -512,8 +514,9 @@ __global__ void __launch_bounds__(kCell1Threads, sizeof(T) == 4 ? kCell1MinBlock
       for (int i = 0; i < kCellPart; ++i) cpart[i * gridDim.x + blockIdx.x] = v[i];
   } else {
     F2 f[kCellPart];
+    f[0] = eacc;
 #pragma unroll
-    for (int i = 0; i < kCellPart; ++i) f[i] = F2{acc[i], 0.0f};
+    for (int i = 1; i < kCellPart; ++i) f[i] = F2{(float)acc[i], 0.0f};
     block_sum_f2_pairs<kCellPart>(f, red);
     if (threadIdx.x == 0)
 #pragma unroll
