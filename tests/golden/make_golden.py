@@ -472,6 +472,55 @@ def make_cell_opt_fixtures():
         save("opt_cell_%s_nanocell" % tag, **arrays)
 
 
+def make_mtk_variant_fixtures():
+    """The MTK barostat's other options (npt.py:513-757): isotropic domain fluctuations, a volume
+    constraint, and its own Nose-Hoover chain on the barostat velocity (baro_thermo)."""
+    T = 300.0 * units.kelvin
+    fs = units.femtosecond
+    press = 100e6 * units.pascal
+    rng = np.random.default_rng(8)
+    chain_vel0 = rng.normal(0, 1e-5, 3)
+    baro_chain_vel0 = rng.normal(0, 1e-5, 3)
+    vp = rng.normal(0, 1e-6, (3, 3))
+    vp = 0.5 * (vp + vp.T)
+
+    def extra(arrays, vi):
+        hook = [h for h in vi.hooks if isinstance(h, MTKBarostat) or h.name == "TBCombination"][0]
+        baro = hook if isinstance(hook, MTKBarostat) else hook.barostat
+        arrays["vel_press_end"] = np.asarray(baro.vel_press)
+        arrays["rvecs_end"] = vi.mmf.system.domain.rvecs
+        if hook.name == "TBCombination" and hasattr(hook.thermostat, "chain"):
+            arrays["chain_pos_end"] = hook.thermostat.chain.pos
+            arrays["chain_vel_end"] = hook.thermostat.chain.vel
+        if baro.baro_thermo is not None:
+            arrays["baro_chain_pos_end"] = baro.baro_thermo.chain.pos
+            arrays["baro_chain_vel_end"] = baro.baro_thermo.chain.vel
+
+    def iso(ff):
+        b = MTKBarostat(ff, T, press, timecon=1000 * fs, anisotropic=False, vel_press0=2e-6)
+        return [b], {"temp": T, "press": press, "timecon": 1000 * fs, "vel_press0": 2e-6}
+
+    run_md("mtk_iso_nanocell", "nanocell", 100, iso, 25, extra=extra)
+
+    def volc(ff):
+        b = MTKBarostat(ff, T, press, timecon=1000 * fs, vol_constraint=True, vel_press0=vp.copy())
+        t = NHCThermostat(T, timecon=100 * fs, chainlength=3, chain_vel0=chain_vel0.copy())
+        return [t, b], {"temp": T, "press": press, "timecon_baro": 1000 * fs, "timecon_thermo": 100 * fs,
+                        "vel_press0": vp, "chain_vel0": chain_vel0}
+
+    run_md("nhc_mtk_volc_nanocell", "nanocell", 100, volc, 25, extra=extra)
+
+    def bthermo(ff):
+        bt = NHCThermostat(T, timecon=500 * fs, chainlength=3, chain_vel0=baro_chain_vel0.copy())
+        b = MTKBarostat(ff, T, press, timecon=1000 * fs, baro_thermo=bt, vel_press0=vp.copy())
+        t = NHCThermostat(T, timecon=100 * fs, chainlength=3, chain_vel0=chain_vel0.copy())
+        return [t, b], {"temp": T, "press": press, "timecon_baro": 1000 * fs, "timecon_thermo": 100 * fs,
+                        "timecon_baro_thermo": 500 * fs, "vel_press0": vp, "chain_vel0": chain_vel0,
+                        "baro_chain_vel0": baro_chain_vel0}
+
+    run_md("nhc_mtk_bthermo_nanocell", "nanocell", 100, bthermo, 25, extra=extra)
+
+
 # ------------------------------------------------------------------ units and sampling utilities
 
 
@@ -547,7 +596,8 @@ def make_sampling_utils_fixture():
 
 
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["forces", "builder", "md", "hooks", "gle", "opt", "cellopt", "units", "sutils"]
+    which = sys.argv[1:] or ["forces", "builder", "md", "hooks", "gle", "opt", "cellopt", "units", "sutils",
+                             "mtkvar"]
     if "forces" in which:
         make_force_fixtures()
     if "builder" in which:
@@ -566,3 +616,5 @@ if __name__ == "__main__":
         make_units_fixture()
     if "sutils" in which:
         make_sampling_utils_fixture()
+    if "mtkvar" in which:
+        make_mtk_variant_fixtures()

@@ -83,6 +83,9 @@ def hooks_for(name, g, ff):
     if name == "md_lbaro_nanocell":
         return [LangevinBarostat(ff, T, press, timecon=float(g["meta/timecon"]), vel_press0=g["vel_press0"],
                                  replay_noise=g["baro_noise"])]
+    if name == "md_mtk_iso_nanocell":
+        return [MTKBarostat(ff, T, press, timecon=float(g["meta/timecon"]), anisotropic=False,
+                            vel_press0=float(g["meta/vel_press0"]))]
     tb, tt = float(g["meta/timecon_baro"]), float(g["meta/timecon_thermo"])
     if name == "md_langevin_mtk_nanocell":
         return [LangevinThermostat(T, timecon=tt, replay_noise=g["noise"]),
@@ -93,6 +96,13 @@ def hooks_for(name, g, ff):
     nhc = NHCThermostat(T, timecon=tt, chainlength=3, chain_vel0=g["meta/chain_vel0"].copy())
     if name == "md_nhc_mtk_nanocell":
         return [nhc, MTKBarostat(ff, T, press, timecon=tb, vel_press0=g["meta/vel_press0"].copy())]
+    if name == "md_nhc_mtk_volc_nanocell":
+        return [nhc, MTKBarostat(ff, T, press, timecon=tb, vol_constraint=True,
+                                 vel_press0=g["meta/vel_press0"].copy())]
+    if name == "md_nhc_mtk_bthermo_nanocell":
+        bt = NHCThermostat(T, timecon=float(g["meta/timecon_baro_thermo"]), chainlength=3,
+                           chain_vel0=g["meta/baro_chain_vel0"].copy())
+        return [nhc, MTKBarostat(ff, T, press, timecon=tb, baro_thermo=bt, vel_press0=g["meta/vel_press0"].copy())]
     if name == "md_nhc_bbaro_nanocell":
         return [nhc, BerendsenBarostat(ff, T, press, timecon=tb)]
     if name == "md_nhc_lbaro_nanocell":
@@ -104,7 +114,7 @@ def hooks_for(name, g, ff):
 NAMES = ["md_langevin_nanocell", "md_nhc_nanocell", "md_mtk_nanocell", "md_nhc_mtk_nanocell",
          "md_langevin_mtk_nanocell", "md_berendsen_nanocell", "md_csvr_nanocell", "md_berendsen_mtk_nanocell",
          "md_nhc_bbaro_nanocell", "md_lbaro_nanocell", "md_nhc_lbaro_nanocell", "md_gle_nanocell",
-         "md_andersen_nanocell"]
+         "md_andersen_nanocell", "md_mtk_iso_nanocell", "md_nhc_mtk_volc_nanocell", "md_nhc_mtk_bthermo_nanocell"]
 
 
 @pytest.mark.parametrize("name", NAMES)
