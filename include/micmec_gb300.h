@@ -147,7 +147,8 @@ mm_status mm_md_advance(mm_handle* h, int nsteps, double* records, int finish, v
 mm_status mm_md_end(mm_handle* h, double* pos, double* vel, void* stream);
 
 /*
- * MD with the hooks of mm_batch_md (thermo 0..4; baro 0..3; the NHC with chain length 3)
+ * MD with the hooks of mm_batch_md (thermo 0..4; the barostat codes of mm_batch_md, MTK
+ * options included; the particle NHC with chain length 3)
  * for a system of any size spread over the whole GPU: the step of
  * VerletIntegrator.propagate (micmec/sampling/verlet.py:140-166) with TBCombination and
  * the thermostats and barostats (micmec/sampling/npt.py:52-757; nvt.py:110-274,
@@ -265,15 +266,22 @@ mm_status mm_batch_get_state(mm_batch* b, double* pos, double* vel, double* rvec
  * tensor (39..47), chain positions (48..50), velocities (51..53), masses (54..56),
  * ndof (57), barostat mass (58), barostat dof (59), thermostat / barostat
  * conserved-energy corrections (60, 61), relaxation: largest gradient (62), iterations (63),
- * chain ndof (65; 0 = ndof), Langevin barostat time constant (66) and temperature (67).
+ * chain ndof (65; 0 = ndof), Langevin barostat time constant (66) and temperature (67),
+ * the MTK barostat's own chain: positions (70..72), velocities (73..75), masses (76..78),
+ * temperature (79).
  */
-#define MM_BATCH_CTL 72
+#define MM_BATCH_CTL 80
 #define MM_BATCH_REC 31
 mm_status mm_batch_control(mm_batch* b, double* ctl, int write);
 /*
  * nsteps MD steps of every system. thermo: 0 none, 1 Langevin, 2 Nose-Hoover chain of
  * length `chain`, 3 Berendsen, 4 CSVR (no barostat); baro: 0 none, 1 anisotropic MTK,
- * 2 anisotropic Berendsen, 3 anisotropic Langevin barostat, at pressure `press`. The
+ * 2 anisotropic Berendsen, 3 anisotropic Langevin barostat, at pressure `press`; for the
+ * MTK barostat, baro | MM_MTK_ISO (isotropic: the barostat velocity is the scalar at
+ * control slot 39, the rest of the tensor zero) or | MM_MTK_VOLC (volume constraint), and
+ * | MM_MTK_CHAIN | (length << 8) (a Nose-Hoover chain of its own on the barostat
+ * velocity, length 1..3, state at control slots 70..79; MTKBarostat(baro_thermo=...),
+ * micmec/sampling/npt.py:513-757). The
  * controller block must hold ndof, chain masses/state and ndof, barostat mass,
  * velocity, dof, and for the Langevin barostat its time constant and temperature (as
  * the reference's hook init sets them). noise (device, (nsteps, 2, sum N, 3)) replays
@@ -287,6 +295,9 @@ mm_status mm_batch_control(mm_batch* b, double* ctl, int write);
  * 140-166; nvt.py:110-274, 361-532; npt.py:52-757).
  */
 #define MM_HOOK_NOISE 26
+#define MM_MTK_ISO 0x10
+#define MM_MTK_VOLC 0x20
+#define MM_MTK_CHAIN 0x40
 mm_status mm_batch_md(mm_batch* b, int nsteps, double timestep, int thermo, double temp, double timecon, int baro,
                       double press, int chain, uint64_t seed, int64_t step0, const double* noise,
                       const double* hook_noise, double* records, int use_graph, void* stream);

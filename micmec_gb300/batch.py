@@ -23,17 +23,37 @@ import numpy as np
 from micmec_gb300 import _native as nat
 from micmec_gb300.units import bar, boltzmann, femtosecond
 
-__all__ = ["BatchSystems", "CTL", "REC", "HOOK_NOISE_LEN"]
+__all__ = ["BatchSystems", "CTL", "REC", "HOOK_NOISE_LEN", "baro_code"]
 
 CTL = dict(L=slice(0, 9), rvecs=slice(9, 18), volume=18, epot=19, ekin=20, vtens=slice(21, 30), ktens=slice(30, 39),
            vel_press=slice(39, 48), chain_pos=slice(48, 51), chain_vel=slice(51, 54), chain_mass=slice(54, 57),
            ndof=57, mass_press=58, baro_ndof=59, econs_thermo=60, econs_baro=61, gmax=62, iters=63, alpha=64,
-           chain_ndof=65, timecon_press=66, temp_press=67, stress_res=69)
-CTL_LEN = 72
+           chain_ndof=65, timecon_press=66, temp_press=67, stress_res=69, bchain_pos=slice(70, 73),
+           bchain_vel=slice(73, 76), bchain_mass=slice(76, 79), bchain_temp=79)
+CTL_LEN = 80
+# options of the MTK barostat in the barostat code (kind | options | chain length << 8)
+MTK_ISO, MTK_VOLC, MTK_CHAIN = 0x10, 0x20, 0x40
 REC = dict(epot=0, ekin=1, ecorr=2, volume=3, vtens=slice(4, 13), ktens=slice(13, 22), rvecs=slice(22, 31))
 REC_LEN = 31
 _THERMO = {None: 0, "langevin": 1, "nhc": 2, "berendsen": 3, "csvr": 4}
 _BARO = {None: 0, "mtk": 1, "berendsen": 2, "langevin": 3}
+
+
+def baro_code(barostat, anisotropic=True, vol_constraint=False, chainlength=0):
+    """Barostat argument of the kernels: the kind, and for the MTK barostat its options
+    (isotropic, volume constraint, a Nose-Hoover chain of ``chainlength`` beads of its own)."""
+    if barostat is None or isinstance(barostat, (int, np.integer)):
+        return int(barostat or 0)
+    code = _BARO[barostat]
+    if (not anisotropic or vol_constraint or chainlength) and barostat != "mtk":
+        raise ValueError("isotropic / volume-constrained / chained variants are MTK barostat options")
+    if not anisotropic:
+        code |= MTK_ISO
+    if vol_constraint:
+        code |= MTK_VOLC
+    if chainlength:
+        code |= MTK_CHAIN | (int(chainlength) << 8)
+    return code
 HOOK_NOISE_LEN = 26  # per system and step: CSVR R, S; Langevin barostat 4 x 6 unit normals
 
 
@@ -166,9 +186,16 @@ class BatchSystems(object):
     # ------------------------------------------------------------ hooks set-up
     def setup_md(self, vel=None, temp=300.0, thermostat=None, timecon=100 * femtosecond, chainlength=3,
                  chain_vel0=None, barostat=None, baro_timecon=1000 * femtosecond, vel_press0=None, ndof=None,
-                 seed=0, clean=True, beta=4.57e-5 / bar):
+                 seed=0, clean=True, beta=4.57e-5 / bar, anisotropic=True, vol_constraint=False, baro_chainlength=0,
+                 baro_chain_timecon=100 * femtosecond, baro_chain_temp=None, baro_chain_vel0=None):
         """Initial velocities and hook constants for every system (as the hooks' init does).
-        beta: the Berendsen barostat's compressibility."""
+        beta: the Berendsen barostat's compressibility. For the MTK barostat: ``anisotropic``
+        False (a scalar barostat velocity), ``vol_constraint`` (a traceless one), and
+        ``baro_chainlength`` > 0 for a Nose-Hoover chain of its own (time constant, temperature
+        and initial velocities ``baro_chain_*``), as MTKBarostat(anisotropic, vol_constraint,
+        baro_thermo) sets them up (npt.py:513-611)."""
+        code = baro_code(barostat, anisotropic, vol_constraint, baro_chainlength)
+        bndof = (6 if anisotropic else 1) - (1 if vol_constraint else 0)
         rng = np.random.default_rng(seed)
         pos, _, rvecs = self.get_state()
         vels = []
@@ -192,12 +219,32 @@ class BatchSystems(object):
                 else:
                     nd = n3 if (thermostat in (None, "langevin") and barostat is None) else n3 - 3
             chain_nd = nd
-            vp = np.zeros((3, 3)) if vel_press0 is None else np.asarray(vel_press0[i] if np.ndim(vel_press0) == 3
-                                                                         else vel_press0)
+            if barostat == "mtk" and not anisotropic:  # scalar barostat velocity in the first slot
+                vp = np.zeros((3, 3))
+                if vel_press0 is not None:
+                    vp[0, 0] = vel_press0[i] if np.ndim(vel_press0) == 1 else vel_press0
+            else:
+                vp = np.zeros((3, 3)) if vel_press0 is None else np.array(vel_press0[i] if np.ndim(vel_press0) == 3
+                                                                          else vel_press0, dtype=np.float64)
             if barostat == "mtk":
                 angfreq = 2 * np.pi / baro_timecon
                 c[i, CTL["mass_press"]] = (nd + 9) * boltzmann * temp / angfreq**2
+                if vol_constraint:
+                    vp -= np.trace(vp) / 3 * np.eye(3)
                 c[i, CTL["vel_press"]] = vp.ravel()
+                if baro_chainlength:
+                    bt = temp if baro_chain_temp is None else baro_chain_temp
+                    bm = np.zeros(3)
+                    bm[:baro_chainlength] = boltzmann * bt / (2 * np.pi / baro_chain_timecon) ** 2
+                    bm[0] *= bndof
+                    bv = np.zeros(3)
+                    if baro_chain_vel0 is not None:
+                        bv[:baro_chainlength] = np.asarray(baro_chain_vel0[i] if np.ndim(baro_chain_vel0) == 2
+                                                           else baro_chain_vel0)
+                    c[i, CTL["bchain_mass"]] = bm
+                    c[i, CTL["bchain_vel"]] = bv
+                    c[i, CTL["bchain_pos"]] = 0.0
+                    c[i, CTL["bchain_temp"]] = bt
             elif barostat == "berendsen":
                 c[i, CTL["mass_press"]] = 3.0 * baro_timecon / beta * np.sqrt(nd)
             elif barostat == "langevin":
@@ -206,7 +253,7 @@ class BatchSystems(object):
                 c[i, CTL["timecon_press"]] = baro_timecon
                 c[i, CTL["temp_press"]] = temp
             if barostat is not None:
-                c[i, CTL["baro_ndof"]] = 6
+                c[i, CTL["baro_ndof"]] = bndof
                 if ndof is None and (thermostat == "langevin" or barostat == "langevin"):
                     nd = n3  # TBCombination: the centre of mass fluctuates (npt.py:86-90)
             if thermostat == "nhc":
@@ -229,14 +276,16 @@ class BatchSystems(object):
         for sl in keep:
             c[:, sl] = c2[:, sl]
         self.set_control(c)
-        self.hooks = dict(thermostat=thermostat, barostat=barostat, temp=temp, timecon=timecon, chain=chainlength)
+        self.hooks = dict(thermostat=thermostat, barostat=code if code & ~0xF else barostat, temp=temp,
+                          timecon=timecon, chain=chainlength)
 
     # ------------------------------------------------------------ kernels
     def md(self, nsteps, timestep=1.0 * femtosecond, thermostat=None, temp=300.0, timecon=100 * femtosecond,
            barostat=None, press=0.0, chainlength=3, seed=1, step0=0, noise=None, hook_noise=None, record=False,
            use_graph=True):
         """nsteps MD steps of every system. thermostat: None, "langevin", "nhc", "berendsen", "csvr";
-        barostat: None, "mtk", "berendsen", "langevin" (anisotropic). The control block holds the
+        barostat: None, "mtk", "berendsen", "langevin" (anisotropic), or a ``baro_code`` (MTK
+        options; ``setup_md`` stores the one it set up in ``hooks["barostat"]``). The control block holds the
         hook state (``control`` / ``set_control``). noise: (nsteps, 2, sum N, 3) Langevin normals;
         hook_noise: (nsteps, nsys, HOOK_NOISE_LEN) CSVR / Langevin-barostat draws."""
         torch = self.torch
@@ -254,7 +303,7 @@ class BatchSystems(object):
                 raise ValueError("hook_noise must have shape (nsteps, nsys, %d)" % HOOK_NOISE_LEN)
             hz = torch.from_numpy(hook_noise).to(dev)
         st = self.L.mm_batch_md(self._h, int(nsteps), float(timestep), _THERMO[thermostat], float(temp),
-                                float(timecon), _BARO[barostat], float(press), int(chainlength),
+                                float(timecon), baro_code(barostat), float(press), int(chainlength),
                                 int(seed), int(step0), nat.ptr(nz), nat.ptr(hz), nat.ptr(rec), int(bool(use_graph)),
                                 torch.cuda.current_stream().cuda_stream)
         nat.check(st, "mm_batch_md")
@@ -288,7 +337,7 @@ class BatchSystems(object):
                  timecon=100 * femtosecond, barostat=None, press=0.0, chainlength=3):
         best = ctypes.c_double()
         nat.check(self.L.mm_batch_autotune(self._h, int(probe_steps), float(timestep), _THERMO[thermostat], float(temp),
-                                           float(timecon), _BARO[barostat], float(press),
+                                           float(timecon), baro_code(barostat), float(press),
                                            int(chainlength), ctypes.byref(best)), "mm_batch_autotune")
         bt, nc = ctypes.c_int(), ctypes.c_int()
         nat.check(self.L.mm_batch_config(self._h, ctypes.byref(bt), ctypes.byref(nc)), "mm_batch_config")

@@ -176,8 +176,9 @@ void fill_type_tables(mm_batch* b, const int32_t* nstates, const double* h0, con
 
 bool same_key(const BMD& x, const BMD& y) {
   return x.dt == y.dt && x.temp == y.temp && x.timecon == y.timecon && x.press == y.press && x.nsteps == y.nsteps &&
-         x.thermo == y.thermo && x.baro == y.baro && x.chain == y.chain && x.seed == y.seed && x.step0 == y.step0 &&
-         x.noise == y.noise && x.hnoise == y.hnoise && x.rec == y.rec;
+         x.thermo == y.thermo && x.baro == y.baro && x.bflags == y.bflags && x.bchain == y.bchain &&
+         x.chain == y.chain && x.seed == y.seed && x.step0 == y.step0 && x.noise == y.noise && x.hnoise == y.hnoise &&
+         x.rec == y.rec;
 }
 
 }  // namespace
@@ -358,7 +359,7 @@ mm_status mm_batch_md(mm_batch* b, int nsteps, double timestep, int thermo, doub
   p.press = press;
   p.nsteps = nsteps;
   p.thermo = thermo;
-  p.baro = baro;
+  parse_baro(baro, p);  // kind and MTK options
   p.chain = chain;
   p.seed = seed;
   p.step0 = step0;
@@ -467,7 +468,7 @@ mm_status mm_batch_autotune(mm_batch* b, int probe_steps, double timestep, int t
       p.press = press;
       p.nsteps = probe_steps;
       p.thermo = thermo;
-      p.baro = baro;
+      parse_baro(baro, p);  // kind and MTK options
       p.chain = chain;
       p.seed = 12345u;
       p.step0 = 0;

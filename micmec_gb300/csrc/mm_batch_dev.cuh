@@ -620,7 +620,13 @@ __device__ __forceinline__ void wupdate_baro_vel(double* c, const BMD& p, bool c
       if (tri == t) z = z6[t];
     R = z * sc;
   }
-  const double Gi = (ps + ((e % 4 == 0) ? diag : 0.0)) * inv_mass;
+  double Gi = (ps + ((e % 4 == 0) ? diag : 0.0)) * inv_mass;
+  if (p.bflags & (BF_ISO | BF_VOLC)) {
+    const double t = __shfl_sync(0xffffffffu, Gi, 0) + __shfl_sync(0xffffffffu, Gi, 4) +
+                     __shfl_sync(0xffffffffu, Gi, 8);
+    if (p.bflags & BF_ISO) Gi = (e == 0) ? t : 0.0;  // one number: the trace
+    else if (e % 4 == 0) Gi -= t / 3;                // traceless
+  }
   if (z6) vp += (Gi - R * inv_mass) * dt / 4;
   else vp += Gi * dt / 4;
   if (z6) vp *= fric;
@@ -695,7 +701,13 @@ __device__ void baro_half(const BArgs& a, Shared<T>& sh, const BSys& sy, const B
     double z6[6];
     if (lang) lbaro_draws(p, sys, a.nsys, step, call0, z6);
     wupdate_baro_vel(c, p, chain, chain ? *cv0p : 0.0, lang ? z6 : nullptr);
-    const double r = wsym_exp(c[C_VP + wentry()], p.dt / 2);
+    double r;
+    if (p.bflags & BF_ISO) {
+      const double f = exp_small(c[C_VP + 0] * p.dt / 2);
+      r = (wentry() % 4 == 0) ? f : 0.0;
+    } else {
+      r = wsym_exp(c[C_VP + wentry()], p.dt / 2);
+    }
     if (threadIdx.x < 9) sh.mat[threadIdx.x] = r;
     __syncwarp();
     wscale_domain(c, sh.mat);
@@ -706,9 +718,16 @@ __device__ void baro_half(const BArgs& a, Shared<T>& sh, const BSys& sy, const B
   __syncthreads();
   forces<T, MODEL>(a, sh, sy);
   if (threadIdx.x < 32) {
+    // mtk_vel_scaling, entry e on lane e
     const int e = wentry();
-    const double tr = c[C_VP + 0] + c[C_VP + 4] + c[C_VP + 8];
-    const double r = wsym_exp(c[C_VP + e] + ((e % 4 == 0) ? tr / c[C_NDOF] : 0.0), -p.dt / 2);
+    double r;
+    if (p.bflags & BF_ISO) {
+      const double f = exp_small(-((1.0 + 3.0 / c[C_NDOF]) * c[C_VP + 0]) * p.dt / 2);
+      r = (e % 4 == 0) ? f : 0.0;
+    } else {
+      const double tr = (p.bflags & BF_VOLC) ? 0.0 : c[C_VP + 0] + c[C_VP + 4] + c[C_VP + 8];
+      r = wsym_exp(c[C_VP + e] + ((e % 4 == 0) ? tr / c[C_NDOF] : 0.0), -p.dt / 2);
+    }
     if (threadIdx.x < 9) sh.mat[threadIdx.x] = r;
   }
   __syncthreads();
@@ -765,21 +784,26 @@ __device__ void berendsen_baro(const BArgs& a, Shared<T>& sh, const BSys& sy, co
 
 // Barostat pre/post call of the MTK or Langevin barostat (the Berendsen barostat acts in
 // post only). The Langevin barostat adds the change of epot + ekin over its call to its
-// correction (npt.py:375-395); the MTK barostat sets its correction after post.
+// correction (npt.py:375-395); the MTK barostat sets its correction after post. An MTK
+// barostat with its own chain runs that chain after the half step in pre and before it in
+// post, and its barostat velocity feels that chain's first velocity (npt.py:616-651).
 template <typename T, int MODEL>
 __device__ void baro_call(const BArgs& a, Shared<T>& sh, const BSys& sy, const BMD& p, double* cv0p,
                           unsigned sys, long long step, int call0) {
   double* c = sh.ctl;
-  const bool chain = p.thermo == TH_NHC;
+  const bool bch = p.bflags & BF_CHAIN;
+  const bool chain = p.thermo == TH_NHC || bch;
   if (threadIdx.x == 0) {
-    *cv0p = c[C_CVEL + 0];
+    if (bch && call0 != 0) mtk_chain_step(c, p);
+    *cv0p = bch ? c[C_BCVEL + 0] : c[C_CVEL + 0];
     c[C_SAVE] = c[C_EPOT] + c[C_EKIN];
   }
   __syncthreads();
   baro_half<T, MODEL>(a, sh, sy, p, chain, cv0p, sys, step, call0);
   if (threadIdx.x == 0) {
+    if (bch && call0 == 0) mtk_chain_step(c, p);
     if (p.baro == BA_LANGEVIN) c[C_ECB] += c[C_SAVE] - c[C_EPOT] - c[C_EKIN];
-    else if (call0 != 0) c[C_ECB] = ekin_baro(c) + p.press * c[C_VOL];
+    else if (call0 != 0) c[C_ECB] = mtk_econs(c, p);
   }
   __syncthreads();
 }
@@ -807,7 +831,7 @@ __global__ void __launch_bounds__(BT, (sizeof(T) == 4 && MODEL >= 1) ? 512 / BT 
       // ---- pre hooks: barostat, then thermostat (TBCombination.pre)
       if (BARO == BA_MTK || BARO == BA_LANGEVIN) baro_call<T, MODEL>(a, sh, sy, p, &cv0, b, step, 0);
       if (THERMO == TH_LANGEVIN) thermostat<T, TH_LANGEVIN>(a, sh, sy, p, step, 0u, false, kT, b);
-      if (THERMO == TH_NHC) thermostat<T, TH_NHC>(a, sh, sy, p, step, 0u, BARO == BA_MTK, kT, b);
+      if (THERMO == TH_NHC) thermostat<T, TH_NHC>(a, sh, sy, p, step, 0u, mtk_couples_chain(p), kT, b);
       if (THERMO == TH_BERENDSEN) thermostat<T, TH_BERENDSEN>(a, sh, sy, p, step, 0u, false, kT, b);
       if (THERMO == TH_CSVR) thermostat<T, TH_CSVR>(a, sh, sy, p, step, 0u, false, kT, b);
       // ---- velocity Verlet
@@ -817,13 +841,13 @@ __global__ void __launch_bounds__(BT, (sizeof(T) == 4 && MODEL >= 1) ? 512 / BT 
       kinetic<T>(a, c, sh.red, sy, KV_KICK, nullptr, p.dt);
       // ---- post hooks: thermostat, then barostat
       if (THERMO == TH_LANGEVIN) thermostat<T, TH_LANGEVIN>(a, sh, sy, p, step, 1u, false, kT, b);
-      if (THERMO == TH_NHC) thermostat<T, TH_NHC>(a, sh, sy, p, step, 1u, BARO == BA_MTK, kT, b);
+      if (THERMO == TH_NHC) thermostat<T, TH_NHC>(a, sh, sy, p, step, 1u, mtk_couples_chain(p), kT, b);
       if (BARO == BA_MTK || BARO == BA_LANGEVIN) baro_call<T, MODEL>(a, sh, sy, p, &cv0, b, step, 2);
       if (BARO == BA_BERENDSEN) berendsen_baro<T, MODEL>(a, sh, sy, p);
       if (threadIdx.x == 0 && p.rec) {
         double* r = p.rec + ((size_t)b * p.nsteps + (st - 1)) * BR_LEN;
         double corr = c[C_ECT] + c[C_ECB];
-        if (THERMO == TH_NHC && BARO != BA_NONE) corr += c[C_BNDOF] * kT * c[C_CPOS + 0];
+        if (THERMO == TH_NHC && BARO != BA_NONE && !(p.bflags & BF_CHAIN)) corr += c[C_BNDOF] * kT * c[C_CPOS + 0];
         r[BR_EPOT] = c[C_EPOT];
         r[BR_EKIN] = c[C_EKIN];
         r[BR_ECORR] = corr;

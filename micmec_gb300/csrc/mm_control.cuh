@@ -40,7 +40,11 @@ enum {
   C_BTEMP = 67,       // Langevin barostat: temperature
   C_SAVE = 68,        // scratch of the hook bookkeeping (energy before a hook call)
   C_SRES = 69,        // cell relaxation: largest residual stress component
-  C_LEN = 72
+  C_BCPOS = 70,       // 3 MTK barostat's own chain (baro_thermo): positions
+  C_BCVEL = 73,       // 3 velocities
+  C_BCMASS = 76,      // 3 masses
+  C_BCTEMP = 79,      // its temperature (kelvin)
+  C_LEN = 80
 };
 // thermostat / barostat kinds
 enum { TH_NONE = 0, TH_LANGEVIN = 1, TH_NHC = 2, TH_BERENDSEN = 3, TH_CSVR = 4 };
@@ -51,9 +55,15 @@ enum { BA_NONE = 0, BA_MTK = 1, BA_BERENDSEN = 2, BA_LANGEVIN = 3 };
 enum { HN_R = 0, HN_S = 1, HN_B = 2, HN_LEN = 26 };
 enum { BR_EPOT = 0, BR_EKIN = 1, BR_ECORR = 2, BR_VOL = 3, BR_VT = 4, BR_KT = 13, BR_RV = 22, BR_LEN = 31 };
 
+// Options of the MTK barostat (MTKBarostat, npt.py:513-757): isotropic domain fluctuations
+// (the barostat velocity is one number, kept in C_VP + 0), a volume constraint (a traceless
+// barostat velocity), and a Nose-Hoover chain of its own on the barostat velocity.
+enum { BF_ISO = 1, BF_VOLC = 2, BF_CHAIN = 4 };
+
 struct BMD {
   double dt, temp, timecon, press;
   int nsteps, thermo, baro, chain;
+  int bflags, bchain;  // MTK options (BF_*) and the length of the barostat's own chain
   unsigned long long seed;
   long long step0;
   const double* noise;   // replay: [nsteps][2][Ntot][3] or null
@@ -66,7 +76,24 @@ constexpr double kBoltzmannHa = 1.3806505e-23 / 4.35974381e-18;  // Hartree / K
 // Hook kinds the step kernels run: thermostats none / Langevin / NHC (chain 1..3) /
 // Berendsen / CSVR, barostats none / MTK / Berendsen / Langevin; CSVR alone (the
 // reference's TBCombination does not pair it with a barostat, npt.py:163-177).
-inline bool hooks_valid(int thermo, double timecon, int baro, int chain) {
+// The barostat argument of the C ABI: the kind (BA_*) in bits 0-3; for the MTK barostat the
+// options BF_* in bits 4-6 and the length (1..3) of its own chain in bits 8-11. Splits it
+// into p.baro, p.bflags and p.bchain; false if the combination is not supported.
+inline bool parse_baro(int code, BMD& p) {
+  p.baro = code & 0xF;
+  p.bflags = (code >> 4) & 0x7;
+  p.bchain = (code >> 8) & 0xF;
+  if (code & ~0xF7F) return false;
+  if (p.bflags && p.baro != BA_MTK) return false;
+  if ((p.bflags & BF_ISO) && (p.bflags & BF_VOLC)) return false;  // no degree of freedom left
+  if ((p.bflags & BF_CHAIN) ? (p.bchain < 1 || p.bchain > 3) : (p.bchain != 0)) return false;
+  return true;
+}
+
+inline bool hooks_valid(int thermo, double timecon, int baro_code, int chain) {
+  BMD q{};
+  if (!parse_baro(baro_code, q)) return false;
+  const int baro = q.baro;
   if (thermo < TH_NONE || thermo > TH_CSVR || baro < BA_NONE || baro > BA_LANGEVIN) return false;
   if (thermo == TH_NHC && (chain < 1 || chain > 3)) return false;
   if ((thermo == TH_LANGEVIN || thermo == TH_BERENDSEN || thermo == TH_CSVR) && !(timecon > 0.0)) return false;
@@ -252,10 +279,18 @@ __device__ inline void update_baro_vel(double* c, const BMD& p, bool chain, doub
     const int tri[9] = {0, 1, 3, 1, 2, 4, 3, 4, 5};  // (i, j) -> lower-triangle slot of (max, min)
     for (int i = 0; i < 9; ++i) R[i] = z6[tri[i]] * sc;
   }
+  double G[9];
+  for (int i = 0; i < 9; ++i) G[i] = (ps[i] + ((i % 4 == 0) ? diag : 0.0)) * inv_mass;
+  if (p.bflags & BF_ISO) {  // one number: the trace
+    const double t = G[0] + G[4] + G[8];
+    for (int i = 0; i < 9; ++i) G[i] = (i == 0) ? t : 0.0;
+  } else if (p.bflags & BF_VOLC) {  // traceless
+    const double t3 = (G[0] + G[4] + G[8]) / 3;
+    for (int i = 0; i < 9; i += 4) G[i] -= t3;
+  }
   for (int i = 0; i < 9; ++i) {
-    const double Gi = (ps[i] + ((i % 4 == 0) ? diag : 0.0)) * inv_mass;
-    if (z6) c[C_VP + i] += (Gi - R[i] * inv_mass) * dt / 4;
-    else c[C_VP + i] += Gi * dt / 4;
+    if (z6) c[C_VP + i] += (G[i] - R[i] * inv_mass) * dt / 4;
+    else c[C_VP + i] += G[i] * dt / 4;
   }
   if (z6)
     for (int i = 0; i < 9; ++i) c[C_VP + i] *= fric;
@@ -352,49 +387,118 @@ __device__ inline double ekin_baro(const double* c) {
 // differ from the integrator's when a Langevin barostat later widens them (npt.py:86-90)
 __device__ inline double chain_ndof(const double* c) { return c[C_CNDOF] > 0.0 ? c[C_CNDOF] : c[C_NDOF]; }
 
-// one bead update of the Nose-Hoover chain (nvt.py:411-435), thread 0; inv_mass[k] = 1 /
+// A Nose-Hoover chain in the control block: slots of its positions, velocities and masses,
+// its length, degrees of freedom and kT.
+struct ChainRef {
+  int pos, vel, mass, len;
+  double ndof, kT;
+};
+// the particle thermostat's chain
+__device__ inline ChainRef particle_chain(const double* c, const BMD& p, double kT) {
+  return ChainRef{C_CPOS, C_CVEL, C_CMASS, p.chain, chain_ndof(c), kT};
+}
+// the MTK barostat's own chain (its degrees of freedom are the barostat's, npt.py:579-583)
+__device__ inline ChainRef baro_chain(const double* c, const BMD& p) {
+  return ChainRef{C_BCPOS, C_BCVEL, C_BCMASS, p.bchain, c[C_BNDOF], kBoltzmannHa * c[C_BCTEMP]};
+}
+
+// one bead update of a Nose-Hoover chain (nvt.py:411-435), thread 0; inv_mass[k] = 1 /
 // (mass of bead k). The friction factor of the next bead is the same before and after the
 // force term, so it is formed once.
-__device__ inline void nhc_bead(double* c, const BMD& p, int k, double ekin, bool g1, double G1_add, double kT,
-                                const double (&inv_mass)[3]) {
-  const int L = p.chain;
+__device__ inline void nhc_bead(double* c, const BMD& p, const ChainRef& ch, int k, double ekin, bool g1,
+                                double G1_add, const double (&inv_mass)[3]) {
   double g;
   if (k == 0) {
-    g = 2 * ekin - chain_ndof(c) * kT;
+    g = 2 * ekin - ch.ndof * ch.kT;
     if (g1) g += G1_add;
   } else {
-    g = c[C_CMASS + k - 1] * c[C_CVEL + k - 1] * c[C_CVEL + k - 1] - kT;
+    g = c[ch.mass + k - 1] * c[ch.vel + k - 1] * c[ch.vel + k - 1] - ch.kT;
   }
   g *= inv_mass[k];
-  if (k == L - 1) {
-    c[C_CVEL + k] += g * p.dt / 4;
+  if (k == ch.len - 1) {
+    c[ch.vel + k] += g * p.dt / 4;
   } else {
-    const double fr = exp_small(-c[C_CVEL + k + 1] * p.dt / 8);
-    c[C_CVEL + k] *= fr;
-    c[C_CVEL + k] += g * p.dt / 4;
-    c[C_CVEL + k] *= fr;
+    const double fr = exp_small(-c[ch.vel + k + 1] * p.dt / 8);
+    c[ch.vel + k] *= fr;
+    c[ch.vel + k] += g * p.dt / 4;
+    c[ch.vel + k] *= fr;
   }
 }
 
-// Full NHChain call (nvt.py:410-451): returns the velocity scale factor; updates ekin in c.
-__device__ inline double nhc_call(double* c, const BMD& p, bool g1, double G1_add, double kT) {
-  double ekin = c[C_EKIN];
+// Full NHChain call (nvt.py:410-451) on the kinetic energy ekin: returns the velocity scale
+// factor, and ekin after the scaling in ekin_out.
+__device__ inline double chain_call(double* c, const BMD& p, const ChainRef& ch, bool g1, double G1_add,
+                                    double ekin, double& ekin_out) {
   double inv_mass[3] = {0.0, 0.0, 0.0};
-  for (int k = 0; k < p.chain; ++k) inv_mass[k] = 1.0 / c[C_CMASS + k];
-  for (int k = p.chain - 1; k >= 0; --k) nhc_bead(c, p, k, ekin, g1, G1_add, kT, inv_mass);
-  for (int k = 0; k < p.chain; ++k) c[C_CPOS + k] += c[C_CVEL + k] * p.dt / 2;
-  const double factor = exp_small(-c[C_CVEL + 0] * p.dt / 2);
+  for (int k = 0; k < ch.len; ++k) inv_mass[k] = 1.0 / c[ch.mass + k];
+  for (int k = ch.len - 1; k >= 0; --k) nhc_bead(c, p, ch, k, ekin, g1, G1_add, inv_mass);
+  for (int k = 0; k < ch.len; ++k) c[ch.pos + k] += c[ch.vel + k] * p.dt / 2;
+  const double factor = exp_small(-c[ch.vel + 0] * p.dt / 2);
   ekin *= factor * factor;
-  for (int k = 0; k < p.chain; ++k) nhc_bead(c, p, k, ekin, g1, G1_add, kT, inv_mass);
-  c[C_EKIN] = ekin;
+  for (int k = 0; k < ch.len; ++k) nhc_bead(c, p, ch, k, ekin, g1, G1_add, inv_mass);
+  ekin_out = ekin;
   return factor;
 }
 
-__device__ inline double nhc_econs(const double* c, const BMD& p, double kT) {
+// The particle thermostat's chain call: returns the velocity scale factor; updates ekin in c.
+__device__ inline double nhc_call(double* c, const BMD& p, bool g1, double G1_add, double kT) {
+  double ek;
+  const double f = chain_call(c, p, particle_chain(c, p, kT), g1, G1_add, c[C_EKIN], ek);
+  c[C_EKIN] = ek;
+  return f;
+}
+
+// conserved-energy correction of a chain (NHChain.get_econs_correction, nvt.py:453-458)
+__device__ inline double chain_econs(const double* c, const ChainRef& ch) {
   double s = 0.0, sp = 0.0;
-  for (int k = 0; k < p.chain; ++k) s += c[C_CVEL + k] * c[C_CVEL + k] * c[C_CMASS + k];
-  for (int k = 1; k < p.chain; ++k) sp += c[C_CPOS + k];
-  return 0.5 * s + kT * (chain_ndof(c) * c[C_CPOS + 0] + sp);
+  for (int k = 0; k < ch.len; ++k) s += c[ch.vel + k] * c[ch.vel + k] * c[ch.mass + k];
+  for (int k = 1; k < ch.len; ++k) sp += c[ch.pos + k];
+  return 0.5 * s + ch.kT * (ch.ndof * c[ch.pos + 0] + sp);
+}
+__device__ inline double nhc_econs(const double* c, const BMD& p, double kT) {
+  return chain_econs(c, particle_chain(c, p, kT));
+}
+
+// MTK options. The barostat's own chain acts on its kinetic energy in the pre call after
+// the half step and in the post call before it (npt.py:616-651); the scaled velocity it
+// returns is not used (the chain couples through its velocity, chainvel0).
+__device__ inline void mtk_chain_step(double* c, const BMD& p) {
+  double unused;
+  chain_call(c, p, baro_chain(c, p), false, 0.0, ekin_baro(c), unused);
+}
+// barostat correction of the conserved energy after its post call (npt.py:644-651)
+__device__ inline double mtk_econs(const double* c, const BMD& p) {
+  double e = ekin_baro(c);
+  if (!(p.bflags & BF_VOLC)) e += p.press * c[C_VOL];
+  if (p.bflags & BF_CHAIN) e += chain_econs(c, baro_chain(c, p));
+  return e;
+}
+// the coupling term the particle chain receives from the MTK barostat (add_press_cont,
+// npt.py:738-743): none when the barostat has its own chain
+__host__ __device__ inline bool mtk_couples_chain(const BMD& p) { return p.baro == BA_MTK && !(p.bflags & BF_CHAIN); }
+
+// Scaling of positions (and domain) and of velocities in an MTK half step, row-vector form
+// x <- x M (npt.py:686-720): anisotropic exp(vp dt / 2) and exp(-(vp + tr(vp) / ndof) dt / 2)
+// (without the trace term under the volume constraint); isotropic exp(vp dt / 2) I and
+// exp(-(1 + 3 / ndof) vp dt / 2) I.
+__device__ inline void mtk_pos_scaling(const double* c, const BMD& p, double* M) {
+  if (p.bflags & BF_ISO) {
+    const double f = exp_small(c[C_VP + 0] * p.dt / 2);
+    for (int i = 0; i < 9; ++i) M[i] = (i % 4 == 0) ? f : 0.0;
+  } else {
+    sym_exp(c + C_VP, p.dt / 2, M);
+  }
+}
+__device__ inline void mtk_vel_scaling(const double* c, const BMD& p, double* M) {
+  if (p.bflags & BF_ISO) {
+    const double f = exp_small(-((1.0 + 3.0 / c[C_NDOF]) * c[C_VP + 0]) * p.dt / 2);
+    for (int i = 0; i < 9; ++i) M[i] = (i % 4 == 0) ? f : 0.0;
+    return;
+  }
+  double S[9];
+  const double tr = (p.bflags & BF_VOLC) ? 0.0 : c[C_VP + 0] + c[C_VP + 4] + c[C_VP + 8];
+  for (int i = 0; i < 9; ++i) S[i] = c[C_VP + i] + ((i % 4 == 0) ? tr / c[C_NDOF] : 0.0);
+  sym_exp(S, -p.dt / 2, M);
 }
 
 

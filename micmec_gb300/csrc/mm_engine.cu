@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(kEN, 1) k_eng_nodes32(ETopo32 t, NodeOp o, con
 }
 
 enum { CT_CV0, CT_BARO_VEL, CT_BARO_POS, CT_BARO_VSCALE, CT_NHC, CT_NHC_ECONS, CT_SAVE_EKIN, CT_LANG_CORR, CT_ECB,
-       CT_RECORD, CT_BER_T, CT_BER_T_CORR, CT_CSVR, CT_BBARO, CT_BBARO_CORR, CT_LBARO_SAVE, CT_LBARO_CORR };
+       CT_RECORD, CT_BER_T, CT_BER_T_CORR, CT_CSVR, CT_BBARO, CT_BBARO_CORR, CT_LBARO_SAVE, CT_LBARO_CORR, CT_BCHAIN };
 
 // One-thread controller: barostat / chain algebra on the control block (FP64). `arg` is
 // the G1 flag of CT_NHC and the draw index (0..3 within the step) of CT_BARO_VEL.
@@ -349,10 +349,10 @@ __global__ void k_eng_ctl(int op, BMD p, int arg, long long step, double* __rest
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   double* c = ctl;
   const double kT = kBoltzmannHa * p.temp;
-  const bool chain = p.thermo == TH_NHC;
+  const bool chain = p.thermo == TH_NHC || (p.bflags & BF_CHAIN);
   switch (op) {
-    case CT_CV0:
-      scal[0] = c[C_CVEL + 0];
+    case CT_CV0:  // the chain velocity the barostat velocity feels: its own chain's, else the thermostat's
+      scal[0] = (p.bflags & BF_CHAIN) ? c[C_BCVEL + 0] : c[C_CVEL + 0];
       break;
     case CT_BARO_VEL: {
       double z6[6];
@@ -362,17 +362,16 @@ __global__ void k_eng_ctl(int op, BMD p, int arg, long long step, double* __rest
       break;
     }
     case CT_BARO_POS:
-      sym_exp(c + C_VP, p.dt / 2, mat);
+      mtk_pos_scaling(c, p, mat);
       scale_domain(c, mat);
       for (int i = 0; i < 9; ++i) box[i] = c[C_L + i];
       break;
-    case CT_BARO_VSCALE: {
-      double S[9];
-      const double tr = c[C_VP + 0] + c[C_VP + 4] + c[C_VP + 8];
-      for (int i = 0; i < 9; ++i) S[i] = c[C_VP + i] + ((i % 4 == 0) ? tr / c[C_NDOF] : 0.0);
-      sym_exp(S, -p.dt / 2, mat);
+    case CT_BARO_VSCALE:
+      mtk_vel_scaling(c, p, mat);
       break;
-    }
+    case CT_BCHAIN:
+      mtk_chain_step(c, p);
+      break;
     case CT_NHC: {
       const double G1 = arg ? 2 * ekin_baro(c) - c[C_BNDOF] * kT : 0.0;
       mat[0] = nhc_call(c, p, arg != 0, G1, kT);
@@ -388,7 +387,7 @@ __global__ void k_eng_ctl(int op, BMD p, int arg, long long step, double* __rest
       c[C_ECT] += scal[1] - c[C_EKIN];
       break;
     case CT_ECB:
-      c[C_ECB] = ekin_baro(c) + p.press * c[C_VOL];
+      c[C_ECB] = mtk_econs(c, p);
       break;
     case CT_BER_T:  // Berendsen thermostat factor; ekin before the scaling kept
       scal[1] = c[C_EKIN];
@@ -418,7 +417,8 @@ __global__ void k_eng_ctl(int op, BMD p, int arg, long long step, double* __rest
     case CT_RECORD: {
       if (!rec) break;
       double corr = c[C_ECT] + c[C_ECB];
-      if (p.thermo == TH_NHC && p.baro != BA_NONE) corr += c[C_BNDOF] * kT * c[C_CPOS + 0];
+      if (p.thermo == TH_NHC && p.baro != BA_NONE && !(p.bflags & BF_CHAIN))
+        corr += c[C_BNDOF] * kT * c[C_CPOS + 0];
       rec[BR_EPOT] = c[C_EPOT];
       rec[BR_EKIN] = c[C_EKIN];
       rec[BR_ECORR] = corr;
@@ -498,10 +498,14 @@ struct Engine {
     ctlop(CT_BARO_VEL, call0 + 1, nullptr, step);
   }
   // barostat pre (call0 = 0) or post (call0 = 2) call of the MTK or Langevin barostat
+  // (the MTK barostat's own chain: after the half step in pre, before it in post)
   void baro(long long step, int call0) {
-    if (p.thermo == TH_NHC) ctlop(CT_CV0);
+    const bool bch = p.bflags & BF_CHAIN;
+    if (bch && call0 != 0) ctlop(CT_BCHAIN);
+    if (p.thermo == TH_NHC || bch) ctlop(CT_CV0);
     if (p.baro == BA_LANGEVIN) ctlop(CT_LBARO_SAVE);
     baro_half(step, call0);
+    if (bch && call0 == 0) ctlop(CT_BCHAIN);
     if (p.baro == BA_LANGEVIN) ctlop(CT_LBARO_CORR);
     else if (call0 != 0) ctlop(CT_ECB);
   }
@@ -517,7 +521,7 @@ struct Engine {
       nodes(OP_LANGEVIN, 1, step, call);
       ctlop(CT_LANG_CORR);
     } else if (p.thermo == TH_NHC) {
-      ctlop(CT_NHC, p.baro == BA_MTK);
+      ctlop(CT_NHC, mtk_couples_chain(p));
       nodes(OP_SCALE_VS, 1);
       if (call == 1) ctlop(CT_NHC_ECONS);
     } else if (p.thermo == TH_BERENDSEN && call == 0) {
@@ -588,7 +592,7 @@ extern "C" mm_status mm_md_engine(mm_handle* h, double* pos, double* vel, int ns
   p.press = press;
   p.nsteps = nsteps;
   p.thermo = thermo;
-  p.baro = baro;
+  parse_baro(baro, p);  // kind and MTK options
   p.chain = chain;
   p.seed = seed;
   p.step0 = step0;
@@ -621,14 +625,14 @@ extern "C" mm_status mm_md_engine(mm_handle* h, double* pos, double* vel, int ns
   E.nodes(OP_KINETIC, 1);  // kinetic totals of the initial velocities
   for (int s = 1; s <= nsteps; ++s) {
     const long long step = step0 + s;
-    if (baro == BA_MTK || baro == BA_LANGEVIN) E.baro(step, 0);
+    if (p.baro == BA_MTK || p.baro == BA_LANGEVIN) E.baro(step, 0);
     E.thermo(step, 0);
     E.nodes(OP_KICK_DRIFT, 0);
     E.forces();
     E.nodes(OP_KICK, 1);
     E.thermo(step, 1);
-    if (baro == BA_MTK || baro == BA_LANGEVIN) E.baro(step, 2);
-    if (baro == BA_BERENDSEN) E.berendsen_baro();
+    if (p.baro == BA_MTK || p.baro == BA_LANGEVIN) E.baro(step, 2);
+    if (p.baro == BA_BERENDSEN) E.berendsen_baro();
     E.ctlop(CT_RECORD, 0, records ? records + (size_t)(s - 1) * BR_LEN : nullptr);
   }
   launch_state_to_pos(h, pos, st);

@@ -181,8 +181,9 @@ class VerletIntegrator(Iterative):
     batch_max_cells = 32768
 
     def _batch_spec(self, vhooks, part):
-        """Hook set the persistent kernels run: a thermostat (NHC, Langevin, Berendsen, CSVR) and/or an
-        anisotropic barostat (MTK, Berendsen, Langevin), alone or in a TBCombination."""
+        """Hook set the persistent kernels run: a thermostat (NHC, Langevin, Berendsen, CSVR) and/or a
+        barostat (MTK with its options, anisotropic Berendsen, anisotropic Langevin), alone or in a
+        TBCombination."""
         from micmec_gb300.sampling.npt import BerendsenBarostat, LangevinBarostat, MTKBarostat, TBCombination
         from micmec_gb300.sampling.nvt import BerendsenThermostat, CSVRThermostat, LangevinThermostat, NHCThermostat
 
@@ -210,7 +211,13 @@ class VerletIntegrator(Iterative):
         if baro is not None:
             if type(baro) not in (MTKBarostat, BerendsenBarostat, LangevinBarostat):
                 return None
-            if not baro.anisotropic or baro.vol_constraint or getattr(baro, "baro_thermo", None) is not None:
+            if type(baro) is MTKBarostat:
+                bt = baro.baro_thermo
+                if not baro.anisotropic and baro.vol_constraint:
+                    return None
+                if bt is not None and (type(bt) is not NHCThermostat or not 1 <= bt.chain.length <= 3):
+                    return None
+            elif not baro.anisotropic or baro.vol_constraint:
                 return None
             if not part.pbc:
                 return None
@@ -223,8 +230,8 @@ class VerletIntegrator(Iterative):
 
     def _hook_control(self, thermo, baro):
         """Control block (layout of the batch/engine kernels) and kernel arguments from the
-        initialised hooks: (ctl, thermostat kind, barostat kind, temp, timecon, seed)."""
-        from micmec_gb300.batch import CTL, CTL_LEN
+        initialised hooks: (ctl, thermostat kind, barostat code, temp, timecon, seed)."""
+        from micmec_gb300.batch import CTL, CTL_LEN, baro_code
         from micmec_gb300.sampling.npt import BerendsenBarostat, LangevinBarostat, MTKBarostat
         from micmec_gb300.sampling.nvt import BerendsenThermostat, CSVRThermostat, LangevinThermostat, NHCThermostat
 
@@ -245,8 +252,21 @@ class VerletIntegrator(Iterative):
             c[CTL["chain_ndof"]] = thermo.chain.ndof
         if baro is not None:
             bkind = {MTKBarostat: "mtk", BerendsenBarostat: "berendsen", LangevinBarostat: "langevin"}[type(baro)]
-            if getattr(baro, "vel_press", None) is not None:
-                c[CTL["vel_press"]] = np.asarray(baro.vel_press).ravel()
+            vp = getattr(baro, "vel_press", None)
+            if vp is not None:
+                if baro.anisotropic:
+                    c[CTL["vel_press"]] = np.asarray(vp).ravel()
+                else:  # the isotropic MTK barostat's scalar velocity
+                    c[CTL["vel_press"].start] = float(vp)
+            bt = getattr(baro, "baro_thermo", None)
+            if bt is not None:
+                n = bt.chain.length
+                c[CTL["bchain_pos"].start:CTL["bchain_pos"].start + n] = bt.chain.pos
+                c[CTL["bchain_vel"].start:CTL["bchain_vel"].start + n] = bt.chain.vel
+                c[CTL["bchain_mass"].start:CTL["bchain_mass"].start + n] = bt.chain.masses
+                c[CTL["bchain_temp"]] = bt.chain.temp
+            if bkind == "mtk":
+                bkind = baro_code("mtk", baro.anisotropic, baro.vol_constraint, 0 if bt is None else bt.chain.length)
             c[CTL["mass_press"]] = baro.mass_press
             c[CTL["baro_ndof"]] = baro.baro_ndof
             c[CTL["econs_baro"]] = baro.econs_correction
@@ -299,7 +319,15 @@ class VerletIntegrator(Iterative):
             thermo.chain.pos[:] = c[CTL["chain_pos"]]
             thermo.chain.vel[:] = c[CTL["chain_vel"]]
         if baro is not None and getattr(baro, "vel_press", None) is not None:
-            baro.vel_press = c[CTL["vel_press"]].reshape(3, 3).copy()
+            if baro.anisotropic:
+                baro.vel_press = c[CTL["vel_press"]].reshape(3, 3).copy()
+            else:
+                baro.vel_press = float(c[CTL["vel_press"].start])
+        bt = getattr(baro, "baro_thermo", None)
+        if bt is not None:
+            n = bt.chain.length
+            bt.chain.pos[:] = c[CTL["bchain_pos"].start:CTL["bchain_pos"].start + n]
+            bt.chain.vel[:] = c[CTL["bchain_vel"].start:CTL["bchain_vel"].start + n]
 
     def _run_batch(self, nsteps, spec):
         """Thermostat / barostat hooks on the device: the system as a one-element batch (one persistent CTA)."""
@@ -338,7 +366,7 @@ class VerletIntegrator(Iterative):
         import torch
 
         from micmec_gb300 import _native as nat
-        from micmec_gb300.batch import CTL, REC_LEN, _BARO, _THERMO
+        from micmec_gb300.batch import CTL, REC_LEN, _THERMO, baro_code
 
         part = self.mmf.parts[0]
         thermo, baro, hook = spec["thermo"], spec["baro"], spec["hook"]
@@ -353,7 +381,7 @@ class VerletIntegrator(Iterative):
         noise = None if noise is None else torch.from_numpy(noise).to(dev)
         hook_noise = None if hook_noise is None else torch.from_numpy(np.ascontiguousarray(hook_noise)).to(dev)
         st = nat.lib().mm_md_engine(part.handle, pos_d.data_ptr(), vel_d.data_ptr(), int(nsteps), float(self.timestep),
-                                    _THERMO[kind], float(temp), float(timecon), _BARO[bkind],
+                                    _THERMO[kind], float(temp), float(timecon), baro_code(bkind),
                                     0.0 if baro is None else float(baro.press), 3, int(seed), nat.ptr(noise),
                                     nat.ptr(hook_noise), c.ctypes.data, rec.data_ptr(), int(self.counter),
                                     torch.cuda.current_stream().cuda_stream)

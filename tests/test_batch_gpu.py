@@ -79,6 +79,46 @@ def test_batch_mtk_matches_reference(name):
     assert np.allclose(rv[0], g["rvecs_end"], rtol=1e-9)
 
 
+@pytest.mark.parametrize("name", ["md_mtk_iso_nanocell", "md_nhc_mtk_volc_nanocell", "md_nhc_mtk_bthermo_nanocell"])
+def test_batch_mtk_options_match_reference(name):
+    """setup_md / md with the MTK barostat's options, in two copies of the system."""
+    from micmec_gb300.batch import CTL
+
+    g, b = _golden_batch(name, copies=2)
+    T, P = float(g["meta/temp"]), float(g["meta/press"])
+    n = len(g["records"]) - 1
+    opts = {}
+    if name == "md_mtk_iso_nanocell":
+        thermo, tt, tb, chain0 = None, 100.0, float(g["meta/timecon"]), None
+        opts["anisotropic"] = False
+        vp0 = float(g["meta/vel_press0"])
+    else:
+        thermo, tt, tb = "nhc", float(g["meta/timecon_thermo"]), float(g["meta/timecon_baro"])
+        chain0 = [g["meta/chain_vel0"]] * 2
+        vp0 = g["meta/vel_press0"]
+        if "volc" in name:
+            opts["vol_constraint"] = True
+        else:
+            opts.update(baro_chainlength=3, baro_chain_timecon=float(g["meta/timecon_baro_thermo"]),
+                        baro_chain_vel0=g["meta/baro_chain_vel0"])
+    b.setup_md(vel=[g["vel0"]] * 2, thermostat=thermo, temp=T, timecon=tt, chain_vel0=chain0, barostat="mtk",
+               baro_timecon=tb, vel_press0=vp0, **opts)
+    rec = b.md(n, timestep=float(g["timestep"]), thermostat=thermo, temp=T, timecon=tt,
+               barostat=b.hooks["barostat"], press=P, record=True)
+    for i in range(2):
+        _check(g, rec[i], n, 1e-7)
+    _, _, rv = b.get_state()
+    assert np.allclose(rv[1], g["rvecs_end"], rtol=1e-9)
+    c = b.control()[1]
+    vp = c[CTL["vel_press"]]
+    if "iso" in name:
+        assert np.allclose(vp[0], g["vel_press_end"], rtol=1e-6) and not vp[1:].any()
+    else:
+        assert np.allclose(vp.reshape(3, 3), g["vel_press_end"], rtol=1e-6, atol=1e-14)
+    if "bthermo" in name:
+        assert np.allclose(c[CTL["bchain_pos"]], g["baro_chain_pos_end"], rtol=1e-6, atol=1e-12)
+
+
 @pytest.mark.parametrize("name", ["md_berendsen_nanocell", "md_csvr_nanocell", "md_berendsen_mtk_nanocell",
                                   "md_nhc_bbaro_nanocell", "md_lbaro_nanocell", "md_nhc_lbaro_nanocell"])
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])

@@ -136,6 +136,40 @@ def test_mtk_matches_reference(name, device):
     assert np.allclose(s.domain.rvecs, g["rvecs_end"], rtol=1e-9)
 
 
+MTK_OPTION_NAMES = ["md_mtk_iso_nanocell", "md_nhc_mtk_volc_nanocell", "md_nhc_mtk_bthermo_nanocell"]
+
+
+@pytest.mark.parametrize("device", ["batch", "engine", "host"])
+@pytest.mark.parametrize("name", MTK_OPTION_NAMES)
+def test_mtk_options_match_reference(name, device):
+    """The MTK barostat isotropic, under a volume constraint, and with a chain of its own."""
+    from test_hooks_cpu import hooks_for
+
+    from micmec_gb300.sampling.verlet import VerletIntegrator
+
+    g, s, ff = _setup(name)
+    rec = Rec()
+    n = len(g["records"]) - 1
+    hooks = hooks_for(name, g, ff)
+    vi = VerletIntegrator(ff, float(g["timestep"]), hooks=hooks + [rec.hook], vel0=g["vel0"].copy(),
+                          device=device != "host")
+    if device == "engine":
+        vi.batch_max_cells = 0
+    if device != "host":
+        assert vi._device_plan()[1]["engine"] == ("batch" if device == "batch" else "lattice")
+    vi.run(n)
+    _compare(g, rec, n, 1e-7)
+    assert np.allclose(s.domain.rvecs, g["rvecs_end"], rtol=1e-9)
+    baro = hooks[-1]
+    assert np.allclose(baro.vel_press, g["vel_press_end"], rtol=1e-6, atol=1e-14)
+    if "chain_pos_end" in g.files:
+        assert np.allclose(hooks[0].chain.pos, g["chain_pos_end"], rtol=1e-6, atol=1e-12)
+        assert np.allclose(hooks[0].chain.vel, g["chain_vel_end"], rtol=1e-6, atol=1e-14)
+    if "baro_chain_pos_end" in g.files:
+        assert np.allclose(baro.baro_thermo.chain.pos, g["baro_chain_pos_end"], rtol=1e-6, atol=1e-12)
+        assert np.allclose(baro.baro_thermo.chain.vel, g["baro_chain_vel_end"], rtol=1e-6, atol=1e-14)
+
+
 def _lattice(n, nstates, seed, sigma=0.05):
     from micmec_gb300 import lattices, units
     from micmec_gb300.system import System
