@@ -5,15 +5,18 @@ reference's ``HDF5Writer`` (micmec/sampling/trajectory.py:31-85) and
 ``System.to_hdf5`` / ``from_hdf5`` (micmec/system.py:262-370) use: nested groups,
 ``create_group``, ``create_dataset(name, shape, maxshape, dtype)`` or ``(name, data=...)``,
 ``in``, ``[...]`` lookups with "a/b" paths, datasets with ``shape``, ``dtype``,
-``resize(n, axis=0)``, row assignment and slicing, and ``attrs`` dictionaries. The file
-on disk is a NumPy ``.npz`` archive (one array per dataset, keyed by its path; attributes
-under ``path@name``, a dataset's maxshape under ``path@.maxshape``), written on ``flush`` /
-``close``; it is not an HDF5 file.
+``resize(n, axis=0)``, row assignment and slicing, and ``attrs`` dictionaries. The tree is
+held in memory and written on ``flush`` / ``close`` as an HDF5 file
+(:mod:`micmec_gb300.hdf5`: the classic format the HDF5 library writes by default, which h5py
+reads); a file opened for reading or appending is read the same way. Datasets are stored
+contiguous with their current shape, and read back resizable along their first axis.
 """
 
 import os
 
 import numpy as np
+
+from micmec_gb300 import hdf5
 
 __all__ = ["File", "Group", "Dataset"]
 
@@ -117,15 +120,6 @@ class Group(object):
         node._items[last] = Dataset(data=data, shape=shape, maxshape=maxshape, dtype=dtype)
         return node._items[last]
 
-    def _flat(self, prefix=""):
-        for name, item in self._items.items():
-            path = prefix + name
-            if isinstance(item, Group):
-                yield path + "/", None, item.attrs
-                yield from item._flat(path + "/")
-            else:
-                yield path, item, item.attrs
-
 
 class File(Group):
     """``File(name, mode)``: "w" new, "a" read existing (or new) and write back, "r" read only."""
@@ -134,7 +128,10 @@ class File(Group):
         Group.__init__(self)
         self.filename = filename
         self.mode = mode
-        if mode in ("r", "a") and os.path.exists(filename):
+        if mode in ("r", "a") and os.path.exists(filename) and hdf5.is_hdf5(filename):
+            self._load(hdf5.read(filename), self)
+        elif mode in ("r", "a") and os.path.exists(filename):
+            # the NumPy-archive files of earlier versions of this module
             with np.load(filename, allow_pickle=False) as z:
                 for key in z.files:
                     path, _, attr = key.partition("@")
@@ -151,22 +148,32 @@ class File(Group):
         elif mode == "r":
             raise IOError('Cannot read from file "%s".' % filename)
 
+    @staticmethod
+    def _load(hg, group):
+        group.attrs.update(hg.attrs)
+        for name, item in hg.members.items():
+            if isinstance(item, hdf5.HGroup):
+                File._load(item, group.create_group(name))
+            else:
+                data = np.asarray(item.data)
+                maxshape = (None,) + data.shape[1:] if data.ndim else ()
+                ds = group.create_dataset(name, data=data, maxshape=maxshape)
+                ds.attrs.update(item.attrs)
+
+    @staticmethod
+    def _tree(group):
+        out = hdf5.HGroup(attrs=group.attrs)
+        for name, item in group.items():
+            if isinstance(item, Group):
+                out.members[name] = File._tree(item)
+            else:
+                out.members[name] = hdf5.HDataset(np.asarray(item), item.attrs)
+        return out
+
     def flush(self):
         if self.mode == "r":
             return
-        arrays = {}
-        for name, value in self.attrs.items():
-            arrays["/@" + name] = np.asarray(value)
-        for path, ds, attrs in self._flat():
-            if ds is not None:
-                arrays[path] = np.asarray(ds)
-                arrays[path + "@.maxshape"] = np.array([-1 if m is None else m for m in ds.maxshape], dtype=np.int64)
-            else:
-                arrays[path] = np.zeros(0)
-            for name, value in attrs.items():
-                arrays[path + "@" + name] = np.asarray(value)
-        with open(self.filename, "wb") as f:
-            np.savez(f, **arrays)
+        hdf5.write(self.filename, self._tree(self))
 
     def close(self):
         self.flush()

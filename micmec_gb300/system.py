@@ -1,9 +1,10 @@
 """``System``: a micromechanical system (nodes, cells, types, domain).
 
 Same constructor, attributes and file I/O as the reference's ``System``
-(micmec/system.py:38-370): CHK text files, "HDF5" system groups (through any
-``h5py.File``-like object; ``.h5`` file names use ``micmec_gb300.h5lite``, a NumPy-archive
-stand-in for h5py, which is not installed) and XYZ snapshots.
+(micmec/system.py:38-370): CHK text files, HDF5 system groups (through any
+``h5py.File``-like object; ``.h5`` file names use ``micmec_gb300.h5lite``, the h5py subset
+this package needs, which writes and reads HDF5 files itself since h5py is not installed) and
+XYZ snapshots.
 """
 
 import numpy as np
