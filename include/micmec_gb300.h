@@ -204,9 +204,10 @@ mm_status mm_md_step_host(mm_handle* h, double* pos, double* vel, double* gpos, 
  *  energy            : device double[1], written.
  * Working memory is one static device array of MM_NOALLOC_SCRATCH_BYTES bytes per
  * GPU, held until the process exits. The first call on a device looks up the
- * array's address (make it before any stream capture); the address is kept for the
- * process's life, so a process that calls cudaDeviceReset does not use this entry
- * point afterwards. Calls share the array: calls that overlap on the GPU race. The
+ * array's address; the address is kept for the process's life, so a process that calls
+ * cudaDeviceReset does not use this entry point afterwards. Calls cannot be captured into
+ * a CUDA graph (each copies its parameters from host memory and synchronises `stream`): a
+ * call on a stream that is being captured returns MM_ERR_ARG. Calls share the array: calls that overlap on the GPU race. The
  * call synchronises `stream` before it returns. Returns MM_ERR_NAN when the energy,
  * gradient or virial holds a NaN (as mm_compute_host).
  */

@@ -14,10 +14,12 @@
 //
 // Set-up: the first call on each device looks up the array's device address with
 // cudaGetSymbolAddress while that device is current (the array's name in host code
-// is only a host-side stand-in, not a device address). Make that first call before
-// any stream capture. The address is kept for the life of the process: after a
-// cudaDeviceReset the module is loaded again and the kept address is stale, so a
-// process that resets a device does not call this entry point afterwards.
+// is only a host-side stand-in, not a device address). No call can be captured into a
+// CUDA graph (each copies its parameters from host memory and synchronises the stream):
+// a call on a stream that is being captured returns MM_ERR_ARG. The address is kept for
+// the life of the process: after a cudaDeviceReset the module is loaded again and the kept
+// address is stale, so a process that resets a device does not call this entry point
+// afterwards.
 //
 // Every call shares the one array and leaves its contents behind; everything a call
 // needs is rewritten or cleared by that call (the status words are cleared first).
@@ -155,6 +157,17 @@ extern "C" mm_status mm_compute_noalloc(const int32_t* lattice_shape, const int3
       mm::set_error("mm_compute_noalloc: nstates out of range");
       return MM_ERR_ARG;
     }
+  {
+    // a call copies its parameters from host memory and synchronises the stream, neither of
+    // which a stream capture allows
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    const cudaError_t e = cudaStreamIsCapturing((cudaStream_t)stream, &cap);
+    if (e != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+      (void)cudaGetLastError();
+      mm::set_error("mm_compute_noalloc: the stream is being captured; calls cannot be captured");
+      return MM_ERR_ARG;
+    }
+  }
   unsigned char* base = nullptr;
   mm_status s = scratch_address(&base);
   if (s != MM_OK) return s;

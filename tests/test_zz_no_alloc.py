@@ -8,7 +8,8 @@ entry point (mm_compute via ForcePartMechanical) on two calls in a row, with the
 tolerances of the other force tests, for both energy models; the gradient and
 virial buffers start nonzero, since the call adds into them. The largest lattice
 the static array holds (32^3 cells, FP64) is run too, and an out-of-range cell type
-is refused before any energy is evaluated. This file is collected last on purpose.
+is refused before any energy is evaluated, and so is a call on a stream that is being
+captured into a CUDA graph. This file is collected last on purpose.
 """
 import ctypes
 
@@ -19,6 +20,7 @@ pytestmark = pytest.mark.gpu
 
 MM_OK, MM_ERR_NAN, MM_ERR_ARG = 0, 1, 2
 MODELS = {"original": 0, "nanocell": 1}
+_CAPTURE_BUFFERS = {}
 
 
 def _lib():
@@ -164,3 +166,45 @@ def test_noalloc_rejects_lattices_beyond_the_scratch_size():
                               pos.data_ptr(), None, None, energy.data_ptr(), None)
     assert st == MM_ERR_ARG
     assert b"32768" in L.mm_last_error()
+
+
+@pytest.mark.filterwarnings("ignore:The CUDA Graph is empty")  # nothing is captured, by design
+def test_noalloc_refuses_a_stream_under_capture():
+    import torch
+
+    from micmec_gb300.pes.mmff import ForcePartMechanical
+
+    L = _lib()
+    s, _ = _system(4, 17)
+    fp = ForcePartMechanical(s)
+    zeros_g, zeros_v = np.zeros((s.nnodes, 3)), np.zeros((3, 3))
+    index = {k: i for i, k in enumerate(fp.type_ids)}
+    _CAPTURE_BUFFERS.update(
+        ctype=torch.tensor([index[int(t)] for t in s.types], dtype=torch.int32, device=fp.device),
+        pos=torch.from_numpy(np.ascontiguousarray(s.pos)).to(fp.device),
+        energy=torch.zeros(1, dtype=torch.float64, device=fp.device))
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(side):
+        status = []
+        with torch.cuda.graph(graph, stream=side):
+            status.append(_noalloc_on_stream(L, s, fp, side))
+    assert status == [MM_ERR_ARG]
+    assert b"captured" in L.mm_last_error()
+    st, e, _, _ = _noalloc(L, s, fp, s.pos, "fp64", "nanocell", zeros_g, zeros_v)  # usable afterwards
+    assert st == MM_OK and np.isfinite(e)
+
+
+def _noalloc_on_stream(L, s, fp, stream):
+    """One call with buffers allocated before the capture began (only the call is captured)."""
+    from micmec_gb300.pes.mmff import type_parameters
+
+    ids = fp.type_ids
+    nstates, h0, C, df, temp = type_parameters(s.params, ids)
+    shape = np.ascontiguousarray(fp.lattice_shape, dtype=np.int32)
+    rvecs = np.ascontiguousarray(s.domain.rvecs, dtype=np.float64)
+    b = _CAPTURE_BUFFERS
+    return L.mm_compute_noalloc(shape.ctypes.data, b["ctype"].data_ptr(), len(ids), nstates.ctypes.data,
+                                h0.ctypes.data, C.ctypes.data, df.ctypes.data, temp.ctypes.data, rvecs.ctypes.data,
+                                1, 0, b["pos"].data_ptr(), None, None, b["energy"].data_ptr(), stream.cuda_stream)
