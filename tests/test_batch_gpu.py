@@ -80,11 +80,13 @@ def test_batch_mtk_matches_reference(name):
 
 
 @pytest.mark.parametrize("name", ["md_mtk_iso_nanocell", "md_nhc_mtk_volc_nanocell", "md_nhc_mtk_bthermo_nanocell"])
-def test_batch_mtk_options_match_reference(name):
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_batch_mtk_options_match_reference(name, precision):
     """setup_md / md with the MTK barostat's options, in two copies of the system."""
     from micmec_gb300.batch import CTL
 
-    g, b = _golden_batch(name, copies=2)
+    g, b = _golden_batch(name, copies=2, precision=precision)
+    rtol = 1e-7 if precision == "fp64" else 2e-5
     T, P = float(g["meta/temp"]), float(g["meta/press"])
     n = len(g["records"]) - 1
     opts = {}
@@ -106,17 +108,19 @@ def test_batch_mtk_options_match_reference(name):
     rec = b.md(n, timestep=float(g["timestep"]), thermostat=thermo, temp=T, timecon=tt,
                barostat=b.hooks["barostat"], press=P, record=True)
     for i in range(2):
-        _check(g, rec[i], n, 1e-7)
+        _check(g, rec[i], n, rtol)
     _, _, rv = b.get_state()
-    assert np.allclose(rv[1], g["rvecs_end"], rtol=1e-9)
+    assert np.abs(rv[1] - g["rvecs_end"]).max() <= (1e-9 if precision == "fp64" else 1e-7) * np.abs(g["rvecs_end"]).max()
     c = b.control()[1]
     vp = c[CTL["vel_press"]]
+    vtol = 1e-6 if precision == "fp64" else 1e-3  # the barostat velocity integrates the FP32 virial
     if "iso" in name:
-        assert np.allclose(vp[0], g["vel_press_end"], rtol=1e-6) and not vp[1:].any()
+        assert np.allclose(vp[0], g["vel_press_end"], rtol=vtol) and not vp[1:].any()
     else:
-        assert np.allclose(vp.reshape(3, 3), g["vel_press_end"], rtol=1e-6, atol=1e-14)
+        ref = g["vel_press_end"]
+        assert np.abs(vp.reshape(3, 3) - ref).max() <= vtol * np.abs(ref).max()
     if "bthermo" in name:
-        assert np.allclose(c[CTL["bchain_pos"]], g["baro_chain_pos_end"], rtol=1e-6, atol=1e-12)
+        assert np.allclose(c[CTL["bchain_pos"]], g["baro_chain_pos_end"], rtol=vtol, atol=1e-12)
 
 
 @pytest.mark.parametrize("name", ["md_berendsen_nanocell", "md_csvr_nanocell", "md_berendsen_mtk_nanocell",
