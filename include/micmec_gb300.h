@@ -276,13 +276,13 @@ mm_status mm_batch_get_state(mm_batch* b, double* pos, double* vel, double* rvec
 mm_status mm_batch_control(mm_batch* b, double* ctl, int write);
 /*
  * nsteps MD steps of every system. thermo: 0 none, 1 Langevin, 2 Nose-Hoover chain of
- * length `chain`, 3 Berendsen, 4 CSVR (no barostat); baro: 0 none, 1 anisotropic MTK,
- * 2 anisotropic Berendsen, 3 anisotropic Langevin barostat, at pressure `press`; for the
- * MTK barostat, baro | MM_MTK_ISO (isotropic: the barostat velocity is the scalar at
- * control slot 39, the rest of the tensor zero) or | MM_MTK_VOLC (volume constraint), and
- * | MM_MTK_CHAIN | (length << 8) (a Nose-Hoover chain of its own on the barostat
- * velocity, length 1..3, state at control slots 70..79; MTKBarostat(baro_thermo=...),
- * micmec/sampling/npt.py:513-757). The
+ * length `chain`, 3 Berendsen, 4 CSVR (no barostat); baro: 0 none, 1 MTK,
+ * 2 Berendsen, 3 Langevin barostat, at pressure `press`, anisotropic unless baro |
+ * MM_BARO_ISO (isotropic: the MTK and Langevin barostat velocity is the scalar at control
+ * slot 39, the rest of the tensor zero; the Berendsen scaling a multiple of the identity) or
+ * | MM_BARO_VOLC (volume constraint); for the MTK barostat also | MM_MTK_CHAIN |
+ * (length << 8) (a Nose-Hoover chain of its own on the barostat velocity, length 1..3, state
+ * at control slots 70..79; MTKBarostat(baro_thermo=...); micmec/sampling/npt.py:180-757). The
  * controller block must hold ndof, chain masses/state and ndof, barostat mass,
  * velocity, dof, and for the Langevin barostat its time constant and temperature (as
  * the reference's hook init sets them). noise (device, (nsteps, 2, sum N, 3)) replays
@@ -296,8 +296,8 @@ mm_status mm_batch_control(mm_batch* b, double* ctl, int write);
  * 140-166; nvt.py:110-274, 361-532; npt.py:52-757).
  */
 #define MM_HOOK_NOISE 26
-#define MM_MTK_ISO 0x10
-#define MM_MTK_VOLC 0x20
+#define MM_BARO_ISO 0x10
+#define MM_BARO_VOLC 0x20
 #define MM_MTK_CHAIN 0x40
 mm_status mm_batch_md(mm_batch* b, int nsteps, double timestep, int thermo, double temp, double timecon, int baro,
                       double press, int chain, uint64_t seed, int64_t step0, const double* noise,

@@ -3,8 +3,8 @@
 ``BatchSystems`` packs hundreds of fully periodic lattices of uneven size
 (defect configurations, strain-scan points, replicas) into one device batch.
 ``md`` runs velocity-Verlet steps of every system with the reference's hooks
-(none / Langevin / Nose-Hoover chain thermostat, optionally the anisotropic MTK
-barostat) in one persistent kernel (optionally replayed from a CUDA graph);
+(none / Langevin / Nose-Hoover chain / Berendsen / CSVR thermostat, and the MTK,
+Berendsen or Langevin barostat, anisotropic, isotropic or volume-constrained) in one persistent kernel (optionally replayed from a CUDA graph);
 ``relax`` minimises every system's energy over node positions with nonlinear
 conjugate gradients. By default every system is its own CTA (launched longest
 first); ``autotune`` picks the CTA size (128 or 256 threads) and the number of
@@ -31,8 +31,8 @@ CTL = dict(L=slice(0, 9), rvecs=slice(9, 18), volume=18, epot=19, ekin=20, vtens
            chain_ndof=65, timecon_press=66, temp_press=67, stress_res=69, bchain_pos=slice(70, 73),
            bchain_vel=slice(73, 76), bchain_mass=slice(76, 79), bchain_temp=79)
 CTL_LEN = 80
-# options of the MTK barostat in the barostat code (kind | options | chain length << 8)
-MTK_ISO, MTK_VOLC, MTK_CHAIN = 0x10, 0x20, 0x40
+# barostat options in the barostat code (kind | options | MTK chain length << 8)
+BARO_ISO, BARO_VOLC, MTK_CHAIN = 0x10, 0x20, 0x40
 REC = dict(epot=0, ekin=1, ecorr=2, volume=3, vtens=slice(4, 13), ktens=slice(13, 22), rvecs=slice(22, 31))
 REC_LEN = 31
 _THERMO = {None: 0, "langevin": 1, "nhc": 2, "berendsen": 3, "csvr": 4}
@@ -40,17 +40,19 @@ _BARO = {None: 0, "mtk": 1, "berendsen": 2, "langevin": 3}
 
 
 def baro_code(barostat, anisotropic=True, vol_constraint=False, chainlength=0):
-    """Barostat argument of the kernels: the kind, and for the MTK barostat its options
-    (isotropic, volume constraint, a Nose-Hoover chain of ``chainlength`` beads of its own)."""
+    """Barostat argument of the kernels: the kind and its options (isotropic, volume constraint;
+    for the MTK barostat also a Nose-Hoover chain of ``chainlength`` beads of its own)."""
     if barostat is None or isinstance(barostat, (int, np.integer)):
         return int(barostat or 0)
     code = _BARO[barostat]
-    if (not anisotropic or vol_constraint or chainlength) and barostat != "mtk":
-        raise ValueError("isotropic / volume-constrained / chained variants are MTK barostat options")
+    if chainlength and barostat != "mtk":
+        raise ValueError("a chain of the barostat's own is an MTK barostat option")
+    if not anisotropic and vol_constraint:
+        raise ValueError("an isotropic barostat under a volume constraint has no degree of freedom left")
     if not anisotropic:
-        code |= MTK_ISO
+        code |= BARO_ISO
     if vol_constraint:
-        code |= MTK_VOLC
+        code |= BARO_VOLC
     if chainlength:
         code |= MTK_CHAIN | (int(chainlength) << 8)
     return code
@@ -189,11 +191,11 @@ class BatchSystems(object):
                  seed=0, clean=True, beta=4.57e-5 / bar, anisotropic=True, vol_constraint=False, baro_chainlength=0,
                  baro_chain_timecon=100 * femtosecond, baro_chain_temp=None, baro_chain_vel0=None):
         """Initial velocities and hook constants for every system (as the hooks' init does).
-        beta: the Berendsen barostat's compressibility. For the MTK barostat: ``anisotropic``
-        False (a scalar barostat velocity), ``vol_constraint`` (a traceless one), and
-        ``baro_chainlength`` > 0 for a Nose-Hoover chain of its own (time constant, temperature
-        and initial velocities ``baro_chain_*``), as MTKBarostat(anisotropic, vol_constraint,
-        baro_thermo) sets them up (npt.py:513-611)."""
+        beta: the Berendsen barostat's compressibility. ``anisotropic`` False (a scalar barostat
+        velocity, or an isotropic Berendsen scaling) and ``vol_constraint`` (a traceless velocity
+        or scaling increment) for every barostat, and for the MTK barostat ``baro_chainlength`` > 0
+        for a Nose-Hoover chain of its own (time constant, temperature and initial velocities
+        ``baro_chain_*``), as the barostats' init sets them up (npt.py:180-611)."""
         code = baro_code(barostat, anisotropic, vol_constraint, baro_chainlength)
         bndof = (6 if anisotropic else 1) - (1 if vol_constraint else 0)
         rng = np.random.default_rng(seed)
@@ -219,7 +221,7 @@ class BatchSystems(object):
                 else:
                     nd = n3 if (thermostat in (None, "langevin") and barostat is None) else n3 - 3
             chain_nd = nd
-            if barostat == "mtk" and not anisotropic:  # scalar barostat velocity in the first slot
+            if barostat in ("mtk", "langevin") and not anisotropic:  # scalar velocity in the first slot
                 vp = np.zeros((3, 3))
                 if vel_press0 is not None:
                     vp[0, 0] = vel_press0[i] if np.ndim(vel_press0) == 1 else vel_press0
@@ -249,6 +251,8 @@ class BatchSystems(object):
                 c[i, CTL["mass_press"]] = 3.0 * baro_timecon / beta * np.sqrt(nd)
             elif barostat == "langevin":
                 c[i, CTL["mass_press"]] = (nd + 3) / 3 * boltzmann * temp * (baro_timecon / (2 * np.pi)) ** 2
+                if vol_constraint:
+                    vp -= np.trace(vp) / 3 * np.eye(3)
                 c[i, CTL["vel_press"]] = vp.ravel()
                 c[i, CTL["timecon_press"]] = baro_timecon
                 c[i, CTL["temp_press"]] = temp
@@ -284,8 +288,8 @@ class BatchSystems(object):
            barostat=None, press=0.0, chainlength=3, seed=1, step0=0, noise=None, hook_noise=None, record=False,
            use_graph=True):
         """nsteps MD steps of every system. thermostat: None, "langevin", "nhc", "berendsen", "csvr";
-        barostat: None, "mtk", "berendsen", "langevin" (anisotropic), or a ``baro_code`` (MTK
-        options; ``setup_md`` stores the one it set up in ``hooks["barostat"]``). The control block holds the
+        barostat: None, "mtk", "berendsen", "langevin" (anisotropic), or a ``baro_code`` (with the
+        barostat's options; ``setup_md`` stores the one it set up in ``hooks["barostat"]``). The control block holds the
         hook state (``control`` / ``set_control``). noise: (nsteps, 2, sum N, 3) Langevin normals;
         hook_noise: (nsteps, nsys, HOOK_NOISE_LEN) CSVR / Langevin-barostat draws."""
         torch = self.torch

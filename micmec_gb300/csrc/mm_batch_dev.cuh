@@ -624,8 +624,15 @@ __device__ __forceinline__ void wupdate_baro_vel(double* c, const BMD& p, bool c
   if (p.bflags & (BF_ISO | BF_VOLC)) {
     const double t = __shfl_sync(0xffffffffu, Gi, 0) + __shfl_sync(0xffffffffu, Gi, 4) +
                      __shfl_sync(0xffffffffu, Gi, 8);
-    if (p.bflags & BF_ISO) Gi = (e == 0) ? t : 0.0;  // one number: the trace
-    else if (e % 4 == 0) Gi -= t / 3;                // traceless
+    const double tr = __shfl_sync(0xffffffffu, R, 0) + __shfl_sync(0xffffffffu, R, 4) +
+                      __shfl_sync(0xffffffffu, R, 8);
+    if (p.bflags & BF_ISO) {  // one number: the trace of G, the first entry of R
+      Gi = (e == 0) ? t : 0.0;
+      R = (e == 0) ? R : 0.0;
+    } else if (e % 4 == 0) {  // traceless
+      Gi -= t / 3;
+      R -= tr / 3;
+    }
   }
   if (z6) vp += (Gi - R * inv_mass) * dt / 4;
   else vp += Gi * dt / 4;
@@ -639,12 +646,25 @@ __device__ __forceinline__ void wupdate_baro_vel(double* c, const BMD& p, bool c
 // berendsen_mu, entry e on lane e.
 __device__ __forceinline__ double wberendsen_mu(const double* c, const BMD& p) {
   const int e = wentry(), i = e / 3, j = e % 3;
-  auto m = [&](int k) {
+  auto dm = [&](int k) {
     const double ptens = (c[C_KT + k] - c[C_VT + k]) / c[C_VOL];
-    const double dmu = p.dt / c[C_MPRESS] * (((k % 4 == 0) ? p.press : 0.0) - ptens);
-    return ((k % 4 == 0) ? 1.0 : 0.0) - dmu;
+    return p.dt / c[C_MPRESS] * (((k % 4 == 0) ? p.press : 0.0) - ptens);
   };
-  return 0.5 * (m(i * 3 + j) + m(j * 3 + i));
+  double d_ij = dm(i * 3 + j), d_ji = dm(j * 3 + i);
+  if (p.bflags & BF_VOLC) {  // traceless increment (the trace formed redundantly by every lane)
+    const double t3 = (dm(0) + dm(4) + dm(8)) / 3;
+    if (i == j) {
+      d_ij -= t3;
+      d_ji -= t3;
+    }
+  }
+  const double mu = 0.5 * ((((i == j) ? 1.0 : 0.0) - d_ij) + (((i == j) ? 1.0 : 0.0) - d_ji));
+  if (p.bflags & BF_ISO) {  // the cube root of the mean diagonal, times the identity
+    const double tr = __shfl_sync(0xffffffffu, mu, 0) + __shfl_sync(0xffffffffu, mu, 4) +
+                      __shfl_sync(0xffffffffu, mu, 8);
+    return (i == j) ? cbrt(tr / 3.0) : 0.0;
+  }
+  return mu;
 }
 
 // scale_domain: L <- L M, rv <- rv M (lane e: entry e), volume from the new rv.

@@ -55,15 +55,17 @@ enum { BA_NONE = 0, BA_MTK = 1, BA_BERENDSEN = 2, BA_LANGEVIN = 3 };
 enum { HN_R = 0, HN_S = 1, HN_B = 2, HN_LEN = 26 };
 enum { BR_EPOT = 0, BR_EKIN = 1, BR_ECORR = 2, BR_VOL = 3, BR_VT = 4, BR_KT = 13, BR_RV = 22, BR_LEN = 31 };
 
-// Options of the MTK barostat (MTKBarostat, npt.py:513-757): isotropic domain fluctuations
-// (the barostat velocity is one number, kept in C_VP + 0), a volume constraint (a traceless
-// barostat velocity), and a Nose-Hoover chain of its own on the barostat velocity.
+// Barostat options: isotropic domain fluctuations (the MTK and Langevin barostat velocity is
+// one number, kept in C_VP + 0; the Berendsen scaling a multiple of the identity), a volume
+// constraint (a traceless barostat velocity or scaling increment), and for the MTK barostat
+// a Nose-Hoover chain of its own on the barostat velocity (MTKBarostat, npt.py:513-757;
+// BerendsenBarostat, npt.py:180-292; LangevinBarostat, npt.py:295-510).
 enum { BF_ISO = 1, BF_VOLC = 2, BF_CHAIN = 4 };
 
 struct BMD {
   double dt, temp, timecon, press;
   int nsteps, thermo, baro, chain;
-  int bflags, bchain;  // MTK options (BF_*) and the length of the barostat's own chain
+  int bflags, bchain;  // barostat options (BF_*) and the length of the MTK barostat's own chain
   unsigned long long seed;
   long long step0;
   const double* noise;   // replay: [nsteps][2][Ntot][3] or null
@@ -76,15 +78,17 @@ constexpr double kBoltzmannHa = 1.3806505e-23 / 4.35974381e-18;  // Hartree / K
 // Hook kinds the step kernels run: thermostats none / Langevin / NHC (chain 1..3) /
 // Berendsen / CSVR, barostats none / MTK / Berendsen / Langevin; CSVR alone (the
 // reference's TBCombination does not pair it with a barostat, npt.py:163-177).
-// The barostat argument of the C ABI: the kind (BA_*) in bits 0-3; for the MTK barostat the
-// options BF_* in bits 4-6 and the length (1..3) of its own chain in bits 8-11. Splits it
-// into p.baro, p.bflags and p.bchain; false if the combination is not supported.
+// The barostat argument of the C ABI: the kind (BA_*) in bits 0-3, the options BF_* in bits
+// 4-6 (BF_CHAIN for the MTK barostat only) and the length (1..3) of the MTK barostat's own
+// chain in bits 8-11. Splits it into p.baro, p.bflags and p.bchain; false if the
+// combination is not supported.
 inline bool parse_baro(int code, BMD& p) {
   p.baro = code & 0xF;
   p.bflags = (code >> 4) & 0x7;
   p.bchain = (code >> 8) & 0xF;
   if (code & ~0xF7F) return false;
-  if (p.bflags && p.baro != BA_MTK) return false;
+  if (p.bflags && p.baro == BA_NONE) return false;
+  if ((p.bflags & BF_CHAIN) && p.baro != BA_MTK) return false;
   if ((p.bflags & BF_ISO) && (p.bflags & BF_VOLC)) return false;  // no degree of freedom left
   if ((p.bflags & BF_CHAIN) ? (p.bchain < 1 || p.bchain > 3) : (p.bchain != 0)) return false;
   return true;
@@ -281,12 +285,18 @@ __device__ inline void update_baro_vel(double* c, const BMD& p, bool chain, doub
   }
   double G[9];
   for (int i = 0; i < 9; ++i) G[i] = (ps[i] + ((i % 4 == 0) ? diag : 0.0)) * inv_mass;
-  if (p.bflags & BF_ISO) {  // one number: the trace
+  if (p.bflags & BF_ISO) {  // one number: the trace of G, the first entry of R
     const double t = G[0] + G[4] + G[8];
-    for (int i = 0; i < 9; ++i) G[i] = (i == 0) ? t : 0.0;
+    for (int i = 0; i < 9; ++i) {
+      G[i] = (i == 0) ? t : 0.0;
+      R[i] = (i == 0) ? R[0] : 0.0;
+    }
   } else if (p.bflags & BF_VOLC) {  // traceless
-    const double t3 = (G[0] + G[4] + G[8]) / 3;
-    for (int i = 0; i < 9; i += 4) G[i] -= t3;
+    const double t3 = (G[0] + G[4] + G[8]) / 3, r3 = (R[0] + R[4] + R[8]) / 3;
+    for (int i = 0; i < 9; i += 4) {
+      G[i] -= t3;
+      R[i] -= r3;
+    }
   }
   for (int i = 0; i < 9; ++i) {
     if (z6) c[C_VP + i] += (G[i] - R[i] * inv_mass) * dt / 4;
@@ -333,14 +343,22 @@ __device__ inline void scale_domain(double* c, const double* M) {
 // Berendsen barostat scaling matrix (npt.py:266-277), anisotropic, no volume constraint:
 // mu = sym(I - dt / W (P I - (K - V) / vol)), K = sum m v (x) v, V the virial.
 __device__ inline void berendsen_mu(const double* c, const BMD& p, double* mu) {
-  double m[9];
+  double dmu[9], m[9];
   for (int i = 0; i < 9; ++i) {
     const double ptens = (c[C_KT + i] - c[C_VT + i]) / c[C_VOL];
-    const double dmu = p.dt / c[C_MPRESS] * (((i % 4 == 0) ? p.press : 0.0) - ptens);
-    m[i] = ((i % 4 == 0) ? 1.0 : 0.0) - dmu;
+    dmu[i] = p.dt / c[C_MPRESS] * (((i % 4 == 0) ? p.press : 0.0) - ptens);
   }
+  if (p.bflags & BF_VOLC) {  // traceless increment
+    const double t3 = (dmu[0] + dmu[4] + dmu[8]) / 3;
+    for (int i = 0; i < 9; i += 4) dmu[i] -= t3;
+  }
+  for (int i = 0; i < 9; ++i) m[i] = ((i % 4 == 0) ? 1.0 : 0.0) - dmu[i];
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) mu[i * 3 + j] = 0.5 * (m[i * 3 + j] + m[j * 3 + i]);
+  if (p.bflags & BF_ISO) {  // the cube root of the mean diagonal, times the identity
+    const double f = cbrt((mu[0] + mu[4] + mu[8]) / 3.0);
+    for (int i = 0; i < 9; ++i) mu[i] = (i % 4 == 0) ? f : 0.0;
+  }
 }
 
 // Berendsen thermostat factor (nvt.py:152-159): sqrt(1 + dt / timecon (T / T_inst - 1)).

@@ -239,12 +239,12 @@ class LangevinBarostat(VerletHook):
             iterative.ndof = iterative.pos.size
         self.mass_press = (iterative.ndof + 3) / 3 * boltzmann * self.temp * (self.timecon / (2 * np.pi)) ** 2
         if self.vel_press0 is not None:
-            self.vel_press = self.vel_press0.copy()
+            self.vel_press = np.array(self.vel_press0, dtype=float).copy()
         else:
             self.vel_press = get_random_vel_press(self.mass_press, self.temp)
         if self.vol_constraint:
             self.vel_press -= np.trace(self.vel_press) / 3 * np.eye(3)
-        if not self.anisotropic:
+        if not self.anisotropic and np.ndim(self.vel_press) == 2:  # (vel_press0 may be the scalar already)
             self.vel_press = self.vel_press[0][0]
         iterative.gpos[:] = 0.0
         iterative.vtens[:] = 0.0

@@ -182,8 +182,8 @@ class VerletIntegrator(Iterative):
 
     def _batch_spec(self, vhooks, part):
         """Hook set the persistent kernels run: a thermostat (NHC, Langevin, Berendsen, CSVR) and/or a
-        barostat (MTK with its options, anisotropic Berendsen, anisotropic Langevin), alone or in a
-        TBCombination."""
+        barostat (MTK, Berendsen, Langevin, each anisotropic, isotropic or volume-constrained; the MTK
+        barostat with a chain of its own), alone or in a TBCombination."""
         from micmec_gb300.sampling.npt import BerendsenBarostat, LangevinBarostat, MTKBarostat, TBCombination
         from micmec_gb300.sampling.nvt import BerendsenThermostat, CSVRThermostat, LangevinThermostat, NHCThermostat
 
@@ -211,13 +211,10 @@ class VerletIntegrator(Iterative):
         if baro is not None:
             if type(baro) not in (MTKBarostat, BerendsenBarostat, LangevinBarostat):
                 return None
-            if type(baro) is MTKBarostat:
-                bt = baro.baro_thermo
-                if not baro.anisotropic and baro.vol_constraint:
-                    return None
-                if bt is not None and (type(bt) is not NHCThermostat or not 1 <= bt.chain.length <= 3):
-                    return None
-            elif not baro.anisotropic or baro.vol_constraint:
+            if not baro.anisotropic and baro.vol_constraint:
+                return None
+            bt = getattr(baro, "baro_thermo", None)
+            if bt is not None and (type(bt) is not NHCThermostat or not 1 <= bt.chain.length <= 3):
                 return None
             if not part.pbc:
                 return None
@@ -265,8 +262,6 @@ class VerletIntegrator(Iterative):
                 c[CTL["bchain_vel"].start:CTL["bchain_vel"].start + n] = bt.chain.vel
                 c[CTL["bchain_mass"].start:CTL["bchain_mass"].start + n] = bt.chain.masses
                 c[CTL["bchain_temp"]] = bt.chain.temp
-            if bkind == "mtk":
-                bkind = baro_code("mtk", baro.anisotropic, baro.vol_constraint, 0 if bt is None else bt.chain.length)
             c[CTL["mass_press"]] = baro.mass_press
             c[CTL["baro_ndof"]] = baro.baro_ndof
             c[CTL["econs_baro"]] = baro.econs_correction
@@ -277,6 +272,7 @@ class VerletIntegrator(Iterative):
                     seed = baro.seed
             if thermo is None:
                 temp = baro.temp
+            bkind = baro_code(bkind, baro.anisotropic, baro.vol_constraint, 0 if bt is None else bt.chain.length)
         return c, kind, bkind, temp, timecon, seed
 
     def _replays(self, thermo, baro, nsteps):

@@ -321,6 +321,41 @@ def make_md_fixtures():
     run_md("langevin_mtk_nanocell", "nanocell", 50, lang_mtk, 25, record_noise=True, extra=mtk_extra)
 
 
+def _hook_end_state(arrays, vi):
+    """End state of a hook run: domain, barostat velocity, chain state, and the recorded draws
+    of the Langevin barostat (its initial velocity and four unit-normal tensors per step) and
+    of the CSVR thermostat."""
+    tril = [(i, j) for i in range(3) for j in range(i + 1)]
+    hook = [h for h in vi.hooks if h.name in ("TBCombination", "Langevin", "Berendsen", "MTTK", "CSVR")][0]
+    baro = getattr(hook, "barostat", hook if getattr(hook, "method", "") == "barostat" else None)
+    thermo = getattr(hook, "thermostat", hook if getattr(hook, "method", "") == "thermostat" else None)
+    arrays["rvecs_end"] = vi.mmf.system.domain.rvecs
+    if baro is not None and getattr(baro, "vel_press", None) is not None:
+        arrays["vel_press_end"] = np.asarray(baro.vel_press)
+    if thermo is not None and hasattr(thermo, "chain"):
+        arrays["chain_pos_end"] = thermo.chain.pos
+        arrays["chain_vel_end"] = thermo.chain.vel
+    draws = vi.noise_draws
+    if isinstance(baro, LangevinBarostat):
+        # first (3, 3) draw: the initial barostat velocity (get_random_vel_press); then
+        # four unit-normal tensors per step (getR, lower triangle used)
+        mats = [d for d in draws if d.shape == (3, 3)]
+        arrays["vel_press0"] = baro.vel_press0
+        arrays["baro_noise"] = np.array([[m[i, j] for (i, j) in tril] for m in mats[1:]]).reshape(-1, 4, 6)
+    if isinstance(thermo, CSVRThermostat):
+        R = [float(d) for d in draws if d.shape == ()]
+        S = [float((d ** 2).sum()) for d in draws if d.ndim == 1]
+        arrays["csvr_noise"] = np.array([R, S]).T
+
+
+class _LB(LangevinBarostat):
+    """The Langevin barostat, keeping its initial velocity (drawn by its init)."""
+
+    def init(self, iterative):
+        LangevinBarostat.init(self, iterative)
+        self.vel_press0 = np.array(self.vel_press, dtype=float).copy()
+
+
 def make_hook_fixtures():
     """The rest of the hook set TBCombination accepts (npt.py:163-177) and the CSVR thermostat."""
     T = 300.0 * units.kelvin
@@ -330,34 +365,8 @@ def make_hook_fixtures():
     chain_vel0 = rng.normal(0, 1e-5, 3)
     vp = rng.normal(0, 1e-6, (3, 3))
     vp = 0.5 * (vp + vp.T)
-    tril = [(i, j) for i in range(3) for j in range(i + 1)]
-
-    def end_state(arrays, vi):
-        hook = [h for h in vi.hooks if h.name in ("TBCombination", "Langevin", "Berendsen", "MTTK", "CSVR")][0]
-        baro = getattr(hook, "barostat", hook if getattr(hook, "method", "") == "barostat" else None)
-        thermo = getattr(hook, "thermostat", hook if getattr(hook, "method", "") == "thermostat" else None)
-        arrays["rvecs_end"] = vi.mmf.system.domain.rvecs
-        if baro is not None and getattr(baro, "vel_press", None) is not None:
-            arrays["vel_press_end"] = np.asarray(baro.vel_press)
-        if thermo is not None and hasattr(thermo, "chain"):
-            arrays["chain_pos_end"] = thermo.chain.pos
-            arrays["chain_vel_end"] = thermo.chain.vel
-        draws = vi.noise_draws
-        if isinstance(baro, LangevinBarostat):
-            # first (3, 3) draw: the initial barostat velocity (get_random_vel_press); then
-            # four unit-normal tensors per step (getR, lower triangle used)
-            mats = [d for d in draws if d.shape == (3, 3)]
-            arrays["vel_press0"] = baro.vel_press0
-            arrays["baro_noise"] = np.array([[m[i, j] for (i, j) in tril] for m in mats[1:]]).reshape(-1, 4, 6)
-        if isinstance(thermo, CSVRThermostat):
-            R = [float(d) for d in draws if d.shape == ()]
-            S = [float((d ** 2).sum()) for d in draws if d.ndim == 1]
-            arrays["csvr_noise"] = np.array([R, S]).T
-
-    class LB(LangevinBarostat):
-        def init(self, iterative):
-            LangevinBarostat.init(self, iterative)
-            self.vel_press0 = np.array(self.vel_press, dtype=float).copy()
+    end_state = _hook_end_state
+    LB = _LB
 
     def berendsen(ff):
         return [BerendsenThermostat(2 * T, timecon=50 * fs)], {"temp": 2 * T, "timecon": 50 * fs}
@@ -521,6 +530,45 @@ def make_mtk_variant_fixtures():
     run_md("nhc_mtk_bthermo_nanocell", "nanocell", 100, bthermo, 25, extra=extra)
 
 
+def make_baro_variant_fixtures():
+    """The Berendsen and Langevin barostats isotropic and under a volume constraint
+    (npt.py:180-510), alone or with a Nose-Hoover chain."""
+    T = 300.0 * units.kelvin
+    fs = units.femtosecond
+    press = 100e6 * units.pascal
+    rng = np.random.default_rng(9)
+    chain_vel0 = rng.normal(0, 1e-5, 3)
+
+    def nhc():
+        return NHCThermostat(T, timecon=100 * fs, chainlength=3, chain_vel0=chain_vel0.copy())
+
+    meta = {"temp": T, "press": press, "timecon_baro": 1000 * fs, "timecon_thermo": 100 * fs,
+            "chain_vel0": chain_vel0}
+
+    def bbaro_iso(ff):
+        return [TBCombination(nhc(), BerendsenBarostat(ff, T, press, timecon=1000 * fs, anisotropic=False))], meta
+
+    run_md("nhc_bbaro_iso_nanocell", "nanocell", 100, bbaro_iso, 25, extra=_hook_end_state)
+
+    def bbaro_volc(ff):
+        return [TBCombination(nhc(), BerendsenBarostat(ff, T, press, timecon=1000 * fs, vol_constraint=True))], meta
+
+    run_md("nhc_bbaro_volc_nanocell", "nanocell", 100, bbaro_volc, 25, extra=_hook_end_state)
+
+    def lbaro_iso(ff):
+        # a slower barostat: with 1,000 fs the reference's isotropic Langevin barostat runs away
+        # on this 27-cell system (exp overflow at npt.py:448)
+        return [_LB(ff, T, press, timecon=5000 * fs, anisotropic=False)], {"temp": T, "press": press,
+                                                                           "timecon": 5000 * fs}
+
+    run_md("lbaro_iso_nanocell", "nanocell", 100, lbaro_iso, 25, extra=_hook_end_state)
+
+    def lbaro_volc(ff):
+        return [TBCombination(nhc(), _LB(ff, T, press, timecon=1000 * fs, vol_constraint=True))], meta
+
+    run_md("nhc_lbaro_volc_nanocell", "nanocell", 100, lbaro_volc, 25, extra=_hook_end_state)
+
+
 # ------------------------------------------------------------------ units and sampling utilities
 
 
@@ -597,7 +645,7 @@ def make_sampling_utils_fixture():
 
 if __name__ == "__main__":
     which = sys.argv[1:] or ["forces", "builder", "md", "hooks", "gle", "opt", "cellopt", "units", "sutils",
-                             "mtkvar"]
+                             "mtkvar", "barovar"]
     if "forces" in which:
         make_force_fixtures()
     if "builder" in which:
@@ -618,3 +666,5 @@ if __name__ == "__main__":
         make_sampling_utils_fixture()
     if "mtkvar" in which:
         make_mtk_variant_fixtures()
+    if "barovar" in which:
+        make_baro_variant_fixtures()

@@ -123,6 +123,39 @@ def test_batch_mtk_options_match_reference(name, precision):
         assert np.allclose(c[CTL["bchain_pos"]], g["baro_chain_pos_end"], rtol=vtol, atol=1e-12)
 
 
+@pytest.mark.parametrize("name", ["md_nhc_bbaro_iso_nanocell", "md_nhc_bbaro_volc_nanocell", "md_lbaro_iso_nanocell",
+                                  "md_nhc_lbaro_volc_nanocell"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_batch_berendsen_langevin_barostat_options_match_reference(name, precision):
+    """setup_md / md with the Berendsen and Langevin barostats isotropic or volume-constrained."""
+    from micmec_gb300.batch import HOOK_NOISE_LEN
+
+    g, b = _golden_batch(name, precision=precision)
+    T, P = float(g["meta/temp"]), float(g["meta/press"])
+    n = len(g["records"]) - 1
+    baro = "berendsen" if "bbaro" in name else "langevin"
+    thermo = "nhc" if "nhc" in name else None
+    tt = float(g["meta/timecon_thermo"]) if thermo else 100.0
+    tb = float(g["meta/timecon_baro"]) if thermo else float(g["meta/timecon"])
+    opts = {"anisotropic": False} if "iso" in name else {"vol_constraint": True}
+    vp0 = None
+    if baro == "langevin":
+        vp0 = g["vel_press0"] if "volc" in name else float(g["vel_press0"])
+    chain0 = [g["meta/chain_vel0"]] if thermo else None
+    b.setup_md(vel=[g["vel0"]], thermostat=thermo, temp=T, timecon=tt, chain_vel0=chain0, barostat=baro,
+               baro_timecon=tb, vel_press0=vp0, **opts)
+    hook = None
+    if baro == "langevin":
+        hook = np.zeros((n, 1, HOOK_NOISE_LEN))
+        hook[:, 0, 2:26] = g["baro_noise"][:n].reshape(n, 24)
+    rec = b.md(n, timestep=float(g["timestep"]), thermostat=thermo, temp=T, timecon=tt,
+               barostat=b.hooks["barostat"], press=P, hook_noise=hook, record=True)
+    _check(g, rec[0], n, 1e-7 if precision == "fp64" else 2e-5)
+    _, _, rv = b.get_state()
+    ref = g["rvecs_end"]
+    assert np.abs(rv[0] - ref).max() <= (1e-9 if precision == "fp64" else 1e-7) * np.abs(ref).max()
+
+
 @pytest.mark.parametrize("name", ["md_berendsen_nanocell", "md_csvr_nanocell", "md_berendsen_mtk_nanocell",
                                   "md_nhc_bbaro_nanocell", "md_lbaro_nanocell", "md_nhc_lbaro_nanocell"])
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])

@@ -83,6 +83,9 @@ def hooks_for(name, g, ff):
     if name == "md_lbaro_nanocell":
         return [LangevinBarostat(ff, T, press, timecon=float(g["meta/timecon"]), vel_press0=g["vel_press0"],
                                  replay_noise=g["baro_noise"])]
+    if name == "md_lbaro_iso_nanocell":
+        return [LangevinBarostat(ff, T, press, timecon=float(g["meta/timecon"]), anisotropic=False,
+                                 vel_press0=g["vel_press0"], replay_noise=g["baro_noise"])]
     if name == "md_mtk_iso_nanocell":
         return [MTKBarostat(ff, T, press, timecon=float(g["meta/timecon"]), anisotropic=False,
                             vel_press0=float(g["meta/vel_press0"]))]
@@ -105,6 +108,13 @@ def hooks_for(name, g, ff):
         return [nhc, MTKBarostat(ff, T, press, timecon=tb, baro_thermo=bt, vel_press0=g["meta/vel_press0"].copy())]
     if name == "md_nhc_bbaro_nanocell":
         return [nhc, BerendsenBarostat(ff, T, press, timecon=tb)]
+    if name == "md_nhc_bbaro_iso_nanocell":
+        return [nhc, BerendsenBarostat(ff, T, press, timecon=tb, anisotropic=False)]
+    if name == "md_nhc_bbaro_volc_nanocell":
+        return [nhc, BerendsenBarostat(ff, T, press, timecon=tb, vol_constraint=True)]
+    if name == "md_nhc_lbaro_volc_nanocell":
+        return [nhc, LangevinBarostat(ff, T, press, timecon=tb, vol_constraint=True, vel_press0=g["vel_press0"],
+                                      replay_noise=g["baro_noise"])]
     if name == "md_nhc_lbaro_nanocell":
         return [nhc, LangevinBarostat(ff, T, press, timecon=tb, vel_press0=g["vel_press0"],
                                       replay_noise=g["baro_noise"])]
@@ -114,7 +124,8 @@ def hooks_for(name, g, ff):
 NAMES = ["md_langevin_nanocell", "md_nhc_nanocell", "md_mtk_nanocell", "md_nhc_mtk_nanocell",
          "md_langevin_mtk_nanocell", "md_berendsen_nanocell", "md_csvr_nanocell", "md_berendsen_mtk_nanocell",
          "md_nhc_bbaro_nanocell", "md_lbaro_nanocell", "md_nhc_lbaro_nanocell", "md_gle_nanocell",
-         "md_andersen_nanocell", "md_mtk_iso_nanocell", "md_nhc_mtk_volc_nanocell", "md_nhc_mtk_bthermo_nanocell"]
+         "md_andersen_nanocell", "md_mtk_iso_nanocell", "md_nhc_mtk_volc_nanocell", "md_nhc_mtk_bthermo_nanocell",
+         "md_nhc_bbaro_iso_nanocell", "md_nhc_bbaro_volc_nanocell", "md_lbaro_iso_nanocell", "md_nhc_lbaro_volc_nanocell"]
 
 
 @pytest.mark.parametrize("name", NAMES)

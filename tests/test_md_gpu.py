@@ -136,14 +136,17 @@ def test_mtk_matches_reference(name, device):
     assert np.allclose(s.domain.rvecs, g["rvecs_end"], rtol=1e-9)
 
 
-MTK_OPTION_NAMES = ["md_mtk_iso_nanocell", "md_nhc_mtk_volc_nanocell", "md_nhc_mtk_bthermo_nanocell"]
+BARO_OPTION_NAMES = ["md_mtk_iso_nanocell", "md_nhc_mtk_volc_nanocell", "md_nhc_mtk_bthermo_nanocell",
+                     "md_nhc_bbaro_iso_nanocell", "md_nhc_bbaro_volc_nanocell", "md_lbaro_iso_nanocell",
+                     "md_nhc_lbaro_volc_nanocell"]
 
 
 @pytest.mark.parametrize("device,precision", [("batch", "fp64"), ("engine", "fp64"), ("host", "fp64"),
                                               ("batch", "fp32"), ("engine", "fp32")])
-@pytest.mark.parametrize("name", MTK_OPTION_NAMES)
-def test_mtk_options_match_reference(name, device, precision):
-    """The MTK barostat isotropic, under a volume constraint, and with a chain of its own."""
+@pytest.mark.parametrize("name", BARO_OPTION_NAMES)
+def test_barostat_options_match_reference(name, device, precision):
+    """The MTK, Berendsen and Langevin barostats isotropic and under a volume constraint, and
+    the MTK barostat with a chain of its own."""
     from test_hooks_cpu import hooks_for
 
     from micmec_gb300.sampling.verlet import VerletIntegrator
@@ -169,7 +172,8 @@ def test_mtk_options_match_reference(name, device, precision):
         a, b = np.asarray(a, dtype=float), np.asarray(b, dtype=float)
         return np.abs(a - b).max() <= vtol * np.abs(b).max() + atol
 
-    assert close(baro.vel_press, g["vel_press_end"], 1e-14)
+    if "vel_press_end" in g.files:
+        assert close(baro.vel_press, g["vel_press_end"], 1e-14)
     if "chain_pos_end" in g.files:
         assert close(hooks[0].chain.pos, g["chain_pos_end"], 1e-12)
         assert close(hooks[0].chain.vel, g["chain_vel_end"], 1e-14)
