@@ -17,24 +17,40 @@ __all__ = ["BaseHDF5Writer", "HDF5Writer", "XYZWriter"]
 
 
 class BaseHDF5Writer(Hook):
+    """Records the iterative's state items, one row per call, in growing datasets of the
+    ``trajectory`` group of ``f`` (created at the first call, with the items' attributes on
+    the group). Items without a value or with an empty axis are not recorded."""
+
     modifies_state = False
 
     def __init__(self, f, start=0, step=1):
         self.f = f
+        self._keys = None  # recorded state items, fixed when the group is found or made
         Hook.__init__(self, start, step)
 
-    def __call__(self, iterative):
+    @staticmethod
+    def _recordable(item):
+        return item.value is not None and not (len(item.shape) > 0 and min(item.shape) == 0)
+
+    def _group(self, iterative):
         if "trajectory" not in self.f:
             self.init_trajectory(iterative)
-        tgrp = self.f["trajectory"]
-        row = min(tgrp[key].shape[0] for key in iterative.state if key in tgrp.keys())
-        for key, item in iterative.state.items():
-            if item.value is None:
+        grp = self.f["trajectory"]
+        if self._keys is None:
+            self._keys = [key for key in iterative.state if key in grp.keys()]
+        return grp
+
+    def __call__(self, iterative):
+        grp = self._group(iterative)
+        # the frame's row: the shortest dataset's length, so that a frame an earlier run left
+        # half written (some datasets one row longer) is written again in place
+        row = min(grp[key].shape[0] for key in self._keys)
+        for key in self._keys:
+            item = iterative.state[key]
+            if not self._recordable(item):
                 continue
-            if len(item.shape) > 0 and min(item.shape) == 0:
-                continue
-            ds = tgrp[key]
-            if ds.shape[0] <= row:
+            ds = grp[key]
+            if ds.shape[0] == row:
                 ds.resize(row + 1, axis=0)
             ds[row] = item.value
 
@@ -42,18 +58,17 @@ class BaseHDF5Writer(Hook):
         system.to_hdf5(grp)
 
     def init_trajectory(self, iterative):
-        tgrp = self.f.create_group("trajectory")
+        grp = self.f.create_group("trajectory")
         for key, item in iterative.state.items():
-            if item.value is None:
-                continue
-            if len(item.shape) > 0 and min(item.shape) == 0:
-                continue
-            tgrp.create_dataset(key, (0,) + item.shape, maxshape=(None,) + item.shape, dtype=item.dtype)
-            for name, value in item.iter_attrs(iterative):
-                tgrp.attrs[name] = value
+            if self._recordable(item):
+                grp.create_dataset(key, (0,) + item.shape, maxshape=(None,) + item.shape, dtype=item.dtype)
+                for name, value in item.iter_attrs(iterative):
+                    grp.attrs[name] = value
 
 
 class HDF5Writer(BaseHDF5Writer):
+    """Also writes the system once, under ``system`` (System.to_hdf5)."""
+
     def __call__(self, iterative):
         if "system" not in self.f:
             self.dump_system(iterative.mmf.system, self.f)
