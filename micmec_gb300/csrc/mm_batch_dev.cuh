@@ -125,11 +125,7 @@ struct Shared {
 
 template <typename T>
 __device__ void load_tables(Shared<T>& sh, const TypeTable* tt, int ntypes, const double* L) {
-  for (int idx = threadIdx.x; idx < ntypes * MM_MAX_STATES; idx += blockDim.x) {
-    const int ty = idx / MM_MAX_STATES, s = idx % MM_MAX_STATES;
-    fill_state_params<T>(sh.tp[ty].s[s], tt[ty].s[s], L);
-    if (s == 0) fill_type_scalars<T>(sh.tp[ty], tt[ty]);
-  }
+  fill_params_block<T>(sh.tp, tt, ntypes, L);
   if (threadIdx.x < 9) sh.L[threadIdx.x] = (T)L[threadIdx.x];
 }
 

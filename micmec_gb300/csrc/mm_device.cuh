@@ -70,34 +70,78 @@ struct TypeTable {
   int pad;
 };
 
-// Cell-precision copy of one (type, state) entry for the lattice matrix L
-// (B = L - h0 formed in FP64, then rounded).
-template <typename T>
-__device__ __forceinline__ void fill_state_params(StateParams<T>& dst, const StateTable& src, const double* L) {
-#pragma unroll
-  for (int i = 0; i < 9; ++i) {
-    dst.hinv[i] = (T)src.hinv[i];
-    dst.B[i] = (T)(L[i] - src.h0[i]);
-  }
-#pragma unroll
-  for (int i = 0; i < 36; ++i) dst.A[i] = (T)src.A[i];
-  dst.v0 = (T)src.v0;
-  dst.df = (T)src.df;
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    dst.hd[i] = (T)src.hinv[4 * i];
-    dst.pad0[i] = T(0);
-    dst.pad1[i] = T(0);
-  }
-  dst.cub[0] = (T)(src.A[0] - src.A[1]);
-  dst.cub[1] = (T)src.A[1];
-  dst.cub[2] = (T)src.A[21];
-}
 template <typename T>
 __device__ __forceinline__ void fill_type_scalars(TypeParams<T>& dst, const TypeTable& src) {
   dst.kT = (T)src.kT;
   dst.lkT = (T)(1.4426950408889634 / src.kT);
   dst.nstates = src.nstates;
+}
+
+// Cell-precision copy of one (type, state) entry for the lattice matrix L. Entry e of
+// StateParams (in its field order) is (T)(x - y), formed in FP64 and then rounded: B = L - h0,
+// cub[0] = A00 - A01, and y = 0 for the others (x - 0.0 is x exactly): v0, df, hd = diagonal
+// of h0^-1, cub[1] = A01, cub[2] = A33, A, hinv; the pads are 0.
+constexpr int kStateParamElems = 68;
+static_assert(sizeof(StateParams<float>) == kStateParamElems * sizeof(float), "StateParams<float> layout");
+static_assert(sizeof(StateParams<double>) == kStateParamElems * sizeof(double), "StateParams<double> layout");
+__device__ __forceinline__ void state_param_source(const StateTable& src, const double* L, int e, double& x,
+                                                   double& y) {
+  x = 0.0;
+  y = 0.0;
+  if (e < 9) {  // B
+    x = L[e];
+    y = src.h0[e];
+  } else if (e == 9) {
+    x = src.v0;
+  } else if (e == 10) {
+    x = src.df;
+  } else if (e < 14) {  // hd
+    x = src.hinv[4 * (e - 11)];
+  } else if (e == 14) {  // cub
+    x = src.A[0];
+    y = src.A[1];
+  } else if (e == 15) {
+    x = src.A[1];
+  } else if (e == 16) {
+    x = src.A[21];
+  } else if (e >= 20 && e < 56) {  // A (pad0 is 17..19)
+    x = src.A[e - 20];
+  } else if (e >= 56 && e < 65) {  // hinv (pad1 is 65..67)
+    x = src.hinv[e - 56];
+  }
+}
+
+// The block's copy of the parameter tables for lattice matrix L, every state of every type:
+// entries spread over all threads, each thread's loads issued before its conversions
+// (FP64 operations are slow and unpipelined per warp on this part, so a routine that
+// gives one thread a whole (type, state) entry keeps the block waiting thousands of
+// cycles). The type scalars (one FP64 division each) go to the last threads.
+template <typename T>
+__device__ void fill_params_block(TypeParams<T>* tp, const TypeTable* __restrict__ tt, int ntypes,
+                                  const double* __restrict__ L) {
+  constexpr int kPer = MM_MAX_STATES * kStateParamElems, kBatch = 4;
+  const int total = ntypes * kPer;
+  for (int base = threadIdx.x; base < total; base += kBatch * blockDim.x) {
+    double x[kBatch], y[kBatch];
+#pragma unroll
+    for (int k = 0; k < kBatch; ++k) {
+      const int idx = base + k * blockDim.x;
+      x[k] = y[k] = 0.0;
+      if (idx < total) {
+        const int ty = idx / kPer, r = idx - ty * kPer, s = r / kStateParamElems;
+        state_param_source(tt[ty].s[s], L, r - s * kStateParamElems, x[k], y[k]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kBatch; ++k) {
+      const int idx = base + k * blockDim.x;
+      if (idx < total) {
+        const int ty = idx / kPer, r = idx - ty * kPer;
+        reinterpret_cast<T*>(tp[ty].s)[r] = (T)(x[k] - y[k]);
+      }
+    }
+  }
+  for (int ty = (int)(blockDim.x - 1 - threadIdx.x); ty < ntypes; ty += blockDim.x) fill_type_scalars<T>(tp[ty], tt[ty]);
 }
 
 // Elastic energy of one state (state_energy, which also returns D and the stress s) and

@@ -110,11 +110,7 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // the current lattice matrix L: B = L - h0 is formed in FP64, then rounded.
 template <typename T>
 __device__ void load_params(TypeParams<T>* tp, const TypeTable* tt, int ntypes, const double* box) {
-  for (int idx = threadIdx.x; idx < ntypes * MM_MAX_STATES; idx += blockDim.x) {
-    const int ty = idx / MM_MAX_STATES, s = idx % MM_MAX_STATES;
-    fill_state_params<T>(tp[ty].s[s], tt[ty].s[s], box);
-    if (s == 0) fill_type_scalars<T>(tp[ty], tt[ty]);
-  }
+  fill_params_block<T>(tp, tt, ntypes, box);
 }
 
 // ------------------------------------------------------------------ kernels
