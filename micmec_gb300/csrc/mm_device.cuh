@@ -412,6 +412,41 @@ __device__ __forceinline__ void block_sum_f2_pairs(F2 (&v)[NV], double* smem) {
     }
   }
 }
+// Block sum of 8 compensated values as a reduce-scatter: at each of the first three
+// exchanges a lane keeps half of its values and adds its partner's copy of them (4, 2, then
+// 1 pair exchanged instead of 8 at every level), so lane l ends with value l >> 2 of its
+// warp; then warp w adds the warps' totals of values w, w + nw, ... in warp order. Fixed
+// order throughout. emit(i, total) runs on lane 0 of the warp that owns value i.
+// smem must hold 8 * (blockDim.x / 32) doubles; blockDim.x is a multiple of 32.
+template <typename Emit>
+__device__ __forceinline__ void block_scatter_sum8(const F2 (&v)[8], double* smem, Emit emit) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  auto xchg = [](F2 keep, F2 send, int mask) {
+    return f2_add(keep, F2{__shfl_xor_sync(0xffffffffu, send.hi, mask), __shfl_xor_sync(0xffffffffu, send.lo, mask)});
+  };
+  F2 a[4], b[2], c;
+  const bool u16 = lane & 16, u8 = lane & 8, u4 = lane & 4;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) a[i] = xchg(u16 ? v[i + 4] : v[i], u16 ? v[i] : v[i + 4], 16);  // value 4 b4 + i
+#pragma unroll
+  for (int i = 0; i < 2; ++i) b[i] = xchg(u8 ? a[i + 2] : a[i], u8 ? a[i] : a[i + 2], 8);  // 4 b4 + 2 b3 + i
+  c = xchg(u4 ? b[1] : b[0], u4 ? b[0] : b[1], 4);                                          // lane >> 2
+  c = xchg(c, c, 2);
+  c = xchg(c, c, 1);
+  F2* s2 = reinterpret_cast<F2*>(smem);
+  if ((lane & 3) == 0) s2[(lane >> 2) * nw + wid] = c;
+  __syncthreads();
+  for (int i = wid; i < 8; i += nw) {
+    F2 t = lane < nw ? s2[i * nw + lane] : F2{0.0f, 0.0f};
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      if (off >= nw) continue;  // the partners hold zeros
+      t = f2_add(t, F2{__shfl_down_sync(0xffffffffu, t.hi, off), __shfl_down_sync(0xffffffffu, t.lo, off)});
+    }
+    if (lane == 0) emit(i, t);
+  }
+}
+
 // The same with the totals converted to FP64 in thread 0 (one conversion per value).
 template <int NV>
 __device__ __forceinline__ void block_sum_f2(F2 (&v)[NV], double (&out)[NV], double* smem) {

@@ -509,14 +509,20 @@ __global__ void __launch_bounds__(kCell1Threads, sizeof(T) == 4 ? kCell1MinBlock
 #pragma unroll
       for (int i = 0; i < kCellPart; ++i) cpart[i * gridDim.x + blockIdx.x] = v[i];
   } else {
-    F2 f[kCellPart];
-    f[0] = eacc;
+    // values 0..7 as a reduce-scatter (the owning warps store them), 8 and 9 by thread 0;
+    // the consumer is the next kernel, so no fence
+    static_assert(kCellPart == 10, "energy + 9 virial components");
+    F2 f8[8], f2[2];
+    f8[0] = eacc;
 #pragma unroll
-    for (int i = 1; i < kCellPart; ++i) f[i] = F2{(float)acc[i], 0.0f};
-    block_sum_f2_pairs<kCellPart>(f, red);
+    for (int i = 1; i < 8; ++i) f8[i] = F2{(float)acc[i], 0.0f};
+    f2[0] = F2{(float)acc[8], 0.0f};
+    f2[1] = F2{(float)acc[9], 0.0f};
+    block_scatter_sum8(f8, red, [&](int i, F2 t) { store_pair(cpart + i * gridDim.x + blockIdx.x, t); });
+    block_sum_f2_pairs<2>(f2, red + 8 * (kCell1Threads / 32));
     if (threadIdx.x == 0)
 #pragma unroll
-      for (int i = 0; i < kCellPart; ++i) store_pair(cpart + i * gridDim.x + blockIdx.x, f[i]);
+      for (int i = 0; i < 2; ++i) store_pair(cpart + (8 + i) * gridDim.x + blockIdx.x, f2[i]);
   }
 }
 
@@ -906,18 +912,20 @@ __global__ void __launch_bounds__(kMDThreads, 1) k_md_nodes(Topo t, MDArgs p, co
     for (int i = 0; i < kNodePart; ++i) tot[i] = accum[i];
     block_sum<kNodePart>(tot, red);
   } else {
-    // accum[1] is not summed: thread 0 forms it from the kinetic tensor's diagonal
+    // accum[1] is not summed: the final sum forms it from the kinetic tensor's diagonal.
+    // Warp j stores the block total of value j (observable j, or j + 1 from j = 1 on) and
+    // fences its own store before the barrier that precedes the ticket.
+    static_assert(kNodePart - 1 == 8, "eight compensated node observables");
     F2 acc[kNodePart - 1];
     acc[0] = accum[0];
 #pragma unroll
     for (int i = 2; i < kNodePart; ++i) acc[i - 1] = accum[i];
-    block_sum_f2_pairs<kNodePart - 1>(acc, red);
-    if (threadIdx.x == 0) {
-      store_pair(npart + 0 * nb + blockIdx.x, acc[0]);
-      store_pair(npart + 1 * nb + blockIdx.x, F2{0.0f, 0.0f});
-#pragma unroll
-      for (int i = 2; i < kNodePart; ++i) store_pair(npart + i * nb + blockIdx.x, acc[i - 1]);
-    }
+    block_scatter_sum8(acc, red, [&](int j, F2 tj) {
+      store_pair(npart + (j == 0 ? 0 : j + 1) * nb + blockIdx.x, tj);
+      if (j == 0) store_pair(npart + 1 * nb + blockIdx.x, F2{0.0f, 0.0f});
+      __threadfence();
+    });
+    __syncthreads();
   }
   if (threadIdx.x == 0) {
     if constexpr (sizeof(T) == 8) {
