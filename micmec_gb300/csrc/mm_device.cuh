@@ -961,17 +961,28 @@ __device__ __forceinline__ U4 philox4x32_10(U4 ctr, uint32_t k0, uint32_t k1) {
   return ctr;
 }
 
+// Uniform in (0, 1) from the top 23 bits of a 32-bit word: 1 + m 2^-23 in [1, 2) built
+// from its bit pattern, minus (1 - 2^-24) (exact), so u = (m + 1/2) 2^-23. Integer and
+// FP32 add only (no conversion instruction).
+__device__ __forceinline__ float uniform_open(uint32_t w) {
+  return __uint_as_float(0x3f800000u | (w >> 9)) - 0.99999994f;
+}
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float y;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 // Three standard normals for (node, step, call) via Box-Muller on Philox output.
 __device__ __forceinline__ void normal3(uint64_t seed, uint32_t node, uint32_t step, uint32_t call, float (&z)[3]) {
   U4 r = philox4x32_10(U4{node, step, call, 0x4d4d4543u}, (uint32_t)seed, (uint32_t)(seed >> 32));
-  const float s = 2.3283064365386963e-10f;  // 2^-32
-  const float u1 = ((float)r.x + 0.5f) * s, u2 = ((float)r.y + 0.5f) * s;
-  const float u3 = ((float)r.z + 0.5f) * s, u4 = ((float)r.w + 0.5f) * s;
-  // Box-Muller with the hardware approximations of log2, sin and cos (absolute errors
-  // ~1e-6 on these ranges, far below what the thermostat's statistics resolve); angles
-  // 2 pi (u - 1/2) in [-pi, pi), where those approximations are most accurate; the
-  // clamp keeps an approximate log of u ~ 1 from turning -2 log u negative.
-  const float r1 = sqrtf(fmaxf(-2.0f * __logf(u1), 0.0f)), r2 = sqrtf(fmaxf(-2.0f * __logf(u3), 0.0f));
+  const float u1 = uniform_open(r.x), u2 = uniform_open(r.y), u3 = uniform_open(r.z), u4 = uniform_open(r.w);
+  // Box-Muller with the hardware approximations of log2, sqrt, sin and cos (absolute
+  // errors ~1e-6 on these ranges, far below what the thermostat's statistics resolve);
+  // angles 2 pi (u - 1/2) in [-pi, pi), where those approximations are most accurate; the
+  // clamp keeps an approximate log of u ~ 1 from turning -2 log u negative. The radius is
+  // at most sqrt(-2 ln 2^-24) = 5.8 (the normal's mass beyond it is 8e-9).
+  const float r1 = sqrt_approx(fmaxf(-2.0f * __logf(u1), 0.0f)), r2 = sqrt_approx(fmaxf(-2.0f * __logf(u3), 0.0f));
   const float twopi = 6.2831853071795865f;
   float s1, c1;
   __sincosf(twopi * (u2 - 0.5f), &s1, &c1);

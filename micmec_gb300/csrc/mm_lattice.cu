@@ -448,9 +448,11 @@ __global__ void __launch_bounds__(kCell1Threads, sizeof(T) == 4 ? kCell1MinBlock
   __shared__ T Ls[9];
   // Averaged-matrix model, FP32, structured lattice: the next cell's 24 corner displacements
   // are copied into this thread's slots of two alternating buffers (cp.async) while the
-  // current cell is evaluated. 64^3 launch: 20.5 -> 19.1 us; the eight-matrix model's
-  // longer arithmetic already hides the loads (27.6 -> 28.7 us with the copies), so it
-  // loads directly.
+  // current cell is evaluated. 64^3 launch: 20.5 -> 19.1 us. The eight-matrix model's
+  // longer arithmetic already hides the loads: 27.4 -> 28.7 us with these copies, and the
+  // same with only the first cell's corners copied while the block builds its parameter
+  // table (the staging buffer's shared memory costs more than the hidden latency gains),
+  // so it loads directly.
   constexpr bool kPrefetch = STRUCT && sizeof(T) == 4 && MODEL == 0;
   __shared__ __align__(16) float pre[kPrefetch ? 2 : 1][kPrefetch ? 24 : 1][kPrefetch ? kCell1Threads : 1];
   auto prefetch = [&](int c, int buf) {
