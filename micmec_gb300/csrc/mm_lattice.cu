@@ -637,18 +637,24 @@ template <typename T>
 __device__ __forceinline__ void md_nodes_final(const MDArgs& p, const double* npart, int nb, const double* cell_tot,
                                                unsigned* ticket, double* carry, double* record) {
   __shared__ double tn[kNodePart];
+  __shared__ double tc[kCellPart + 1];  // cell totals, then the conserved-energy carry
   __threadfence();
+  // warps 0 .. kNodePart-1 sum the node partials; warp kNodePart loads the cell totals and
+  // the carry meanwhile (the block has 32 warps)
+  static_assert(kNodePart < kMDThreads / 32 && kCellPart < 32, "one idle warp loads the totals");
+  if ((int)(threadIdx.x >> 5) == kNodePart) {
+    const int lane = threadIdx.x & 31;
+    if (lane < kCellPart) tc[lane] = __ldcg(cell_tot + lane);
+    else if (lane == kCellPart) tc[kCellPart] = __ldcg(carry);
+  }
   sum_partials_by_warp<kNodePart, 0, sizeof(T) == 4>(npart, nb, nullptr, 0, tn);
   if (threadIdx.x == 0) {
-    double tc[kCellPart];
-#pragma unroll
-    for (int i = 0; i < kCellPart; ++i) tc[i] = __ldcg(cell_tot + i);
     const double ek = (sizeof(T) == 4) ? 0.5 * (tn[3] + tn[4] + tn[5]) : tn[1];
     *ticket = 0u;
     if (record) {
       record[MM_REC_EPOT] = tc[0];
       record[MM_REC_EKIN] = ek;
-      record[MM_REC_DECONS] = (p.finish ? (tn[0] - ek) : 0.0) + (p.finish ? carry[0] : 0.0);
+      record[MM_REC_DECONS] = (p.finish ? (tn[0] - ek) : 0.0) + (p.finish ? tc[kCellPart] : 0.0);
 #pragma unroll
       for (int i = 0; i < 9; ++i) record[MM_REC_VTENS + i] = tc[1 + i];
       const double k[9] = {tn[3], tn[8], tn[7], tn[8], tn[4], tn[6], tn[7], tn[6], tn[5]};
