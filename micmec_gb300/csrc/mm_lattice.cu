@@ -466,11 +466,17 @@ __global__ void __launch_bounds__(kCell1Threads, sizeof(T) == 4 ? kCell1MinBlock
     }
     cp_async_commit();
   };
-  const int stride = gridDim.x * blockDim.x;
+  // block b owns the 32-cell chunks [C b / nb, C (b + 1) / nb) of the C = ceil(M / 32):
+  // every SM's resident blocks get the same number of warp passes (+-1) whatever the number
+  // of passes per thread, and each warp's cells start on a chunk boundary
+  const int nchunk = (t.M + 31) / 32;
+  const int c_begin = (int)(((long long)nchunk * blockIdx.x) / gridDim.x) * 32;
+  const int c_end = min(t.M, (int)(((long long)nchunk * (blockIdx.x + 1)) / gridDim.x) * 32);
+  const int stride = blockDim.x;
   pdl_enter();
   if constexpr (kPrefetch) {
-    const int c0 = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c0 < t.M) prefetch(c0, 0);
+    const int c0 = c_begin + threadIdx.x;
+    if (c0 < c_end) prefetch(c0, 0);
   }
   load_params<T>(tp, tt, ntypes, box);
   if (threadIdx.x < 9) Ls[threadIdx.x] = (T)box[threadIdx.x];
@@ -480,7 +486,7 @@ __global__ void __launch_bounds__(kCell1Threads, sizeof(T) == 4 ? kCell1MinBlock
   for (int i = 0; i < kCellPart; ++i) acc[i] = T(0);
   F2 eacc{0.0f, 0.0f};  // FP32 cells: a thread's cell energies summed with compensation
   int buf = 0;
-  for (int cell = blockIdx.x * blockDim.x + threadIdx.x; cell < t.M; cell += stride) {
+  for (int cell = c_begin + threadIdx.x; cell < c_end; cell += stride) {
     T du[8][3];
     if constexpr (kPrefetch) {
       cp_async_wait_all();
@@ -489,7 +495,7 @@ __global__ void __launch_bounds__(kCell1Threads, sizeof(T) == 4 ? kCell1MinBlock
 #pragma unroll
         for (int x = 0; x < 3; ++x) du[b][x] = pre[buf][b * 3 + x][threadIdx.x];
       buf ^= 1;
-      if (cell + stride < t.M) prefetch(cell + stride, buf);
+      if (cell + stride < c_end) prefetch(cell + stride, buf);
     } else if (STRUCT) {
       int i, j, k;
       split_index(t, cell, i, j, k);
