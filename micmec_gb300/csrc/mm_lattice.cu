@@ -711,11 +711,14 @@ __global__ void __launch_bounds__(kMDThreads, 1) k_md_nodes(Topo t, MDArgs p, co
   Acc accum[kNodePart];
 #pragma unroll
   for (int i = 0; i < kNodePart; ++i) accum[i] = Acc{};
-  // block b owns the contiguous node range [N b / nb, N (b + 1) / nb): equal shares
-  // for all SMs; its threads stride through it
-  const int n_end = (int)(((long long)t.N * (blockIdx.x + 1)) / nb);
-  const int n_first_end = (int)(((long long)t.N * blockIdx.x) / nb) + (int)blockDim.x;  // first pass
-  for (int n = (int)(((long long)t.N * blockIdx.x) / nb) + threadIdx.x; n < n_end; n += blockDim.x) {
+  // block b owns the 32-node chunks [C b / nb, C (b + 1) / nb) of the C = ceil(N / 32):
+  // equal shares for all SMs (+-1 chunk), each warp's nodes starting on a chunk boundary;
+  // its threads stride through them
+  const int nchunk = (t.N + 31) / 32;
+  const int n_begin = (int)(((long long)nchunk * blockIdx.x) / nb) * 32;
+  const int n_end = min(t.N, (int)(((long long)nchunk * (blockIdx.x + 1)) / nb) * 32);
+  const int n_first_end = n_begin + (int)blockDim.x;  // first pass
+  for (int n = n_begin + threadIdx.x; n < n_end; n += blockDim.x) {
   R obs[kNodePart];
 #pragma unroll
   for (int i = 0; i < kNodePart; ++i) obs[i] = R(0);
