@@ -1144,7 +1144,8 @@ void launch_cells(mm_handle* h, cudaStream_t st, double* ecell) {
 constexpr int kCell8MaxPerSM = 4, kCell1MaxPerSM = 16;
 
 int cell_blocks(const mm_handle* h) {
-  // one-thread kernel: grid-stride with at most kCell1MaxPerSM resident blocks per SM
+  // one-thread kernel: at most kCell1MaxPerSM resident blocks per SM, each owning a run of
+  // 32-cell chunks
   const int sms = h->num_sms > 0 ? h->num_sms : 152;
   const int g1 = std::min((h->M + kCell1Threads - 1) / kCell1Threads, sms * kCell1MaxPerSM);
   if (h->model == MM_MODEL_NANOCELL)  // or the eight-lane kernel: grid-stride over groups of cells
@@ -1153,8 +1154,9 @@ int cell_blocks(const mm_handle* h) {
 }
 int node_blocks(const mm_handle* h) { return (h->N + kNodeThreads - 1) / kNodeThreads; }
 
-// The nanocell kernel grid-strides over groups of cells with exactly as many blocks
-// as fit on the GPU at once (so no partial second wave), at most 4 per SM.
+// The one-thread cell kernel (each block a run of 32-cell chunks) and the eight-lane kernel
+// (grid-stride over groups of cells) run exactly as many blocks as fit on the GPU at once
+// (so no partial second wave), at most 16 and 4 per SM.
 int cell_grid(mm_handle* h) {
   if (h->model != MM_MODEL_NANOCELL && h->cell_kernel != 1) return (h->M + kCellThreads - 1) / kCellThreads;
   int& occ = h->cell_occ[h->simple ? 1 : 0];
