@@ -119,7 +119,7 @@ __device__ __forceinline__ void state_param_source(const StateTable& src, const 
 template <typename T>
 __device__ void fill_params_block(TypeParams<T>* tp, const TypeTable* __restrict__ tt, int ntypes,
                                   const double* __restrict__ L) {
-  constexpr int kPer = MM_MAX_STATES * kStateParamElems, kBatch = 4;
+  constexpr int kPer = MM_MAX_STATES * kStateParamElems, kBatch = 8;
   const int total = ntypes * kPer;
   for (int base = threadIdx.x; base < total; base += kBatch * blockDim.x) {
     double x[kBatch], y[kBatch];
