@@ -80,7 +80,8 @@ mm_status mm_create(int nnodes, int ncells, const int32_t* node_coords, const in
                     const double* free_energy, const double* temp_eff, const double* masses, int model,
                     int precision, mm_handle** out);
 
-/* Release all device memory of a handle. */
+/* Release all device memory of a handle (no reference counterpart: Python frees the
+   ForcePartMechanical's arrays). */
 mm_status mm_destroy(mm_handle* h);
 
 /*
@@ -112,7 +113,9 @@ mm_status mm_compute(mm_handle* h, const double* pos, double* gpos, double* vten
  */
 mm_status mm_compute_host(mm_handle* h, const double* pos, double* gpos, double* vtens, double* energy);
 
-/* Per-cell energies (M) and corner gradients (M,8,3) of the last compute: device outputs. */
+/* Per-cell energies (M) and corner gradients (M,8,3) of the last compute: device outputs.
+   The reference keeps the same arrays as ForcePartMechanical.epot_cells / gpos_cells
+   (micmec/pes/mmff.py:243-244, 288-301). */
 mm_status mm_cell_results(mm_handle* h, double* epot_cells, double* gpos_cells, void* stream);
 
 /*
@@ -140,6 +143,8 @@ mm_status mm_md_run(mm_handle* h, double* pos, double* vel, int nsteps, double t
  *                  then a clean end-of-step state); with finish = 0 the next step is
  *                  already started, so further mm_md_advance calls continue seamlessly.
  *  mm_md_end     : write the end-of-step state to pos/vel (device (N,3)).
+ * Replaces VerletIntegrator.initialize / propagate / the state read-back of a run
+ * (micmec/sampling/verlet.py:119-166, iterative.py:74-100) when they are driven step by step.
  */
 mm_status mm_md_begin(mm_handle* h, const double* pos, const double* vel, double timestep, int thermo, double temp,
                       double timecon, uint64_t seed, const double* noise, int64_t step0, void* stream);
@@ -257,7 +262,8 @@ mm_status mm_batch_create(int nsys, const int32_t* shapes, const int32_t* cell_t
                           const int32_t* nstates, const double* h0, const double* C, const double* free_energy,
                           const double* temp_eff, const double* masses, int model, int precision, mm_batch** out);
 mm_status mm_batch_destroy(mm_batch* b);
-/* Host (sum N,3) positions, velocities (or NULL: zero) and (nsys,3,3) domain vectors. */
+/* Host (sum N,3) positions, velocities (or NULL: zero) and (nsys,3,3) domain vectors: the
+   System.pos / VerletIntegrator vel / Domain rvecs of each system (micmec/system.py). */
 mm_status mm_batch_set_state(mm_batch* b, const double* pos, const double* vel, const double* rvecs);
 mm_status mm_batch_get_state(mm_batch* b, double* pos, double* vel, double* rvecs);
 /*
@@ -309,7 +315,9 @@ mm_status mm_batch_md(mm_batch* b, int nsteps, double timestep, int thermo, doub
  */
 mm_status mm_batch_set_params(mm_batch* b, const int32_t* nstates, const double* h0, const double* C,
                               const double* free_energy, const double* temp_eff);
-/* Relax node positions of every system (domain fixed) until max |gradient| < gtol. */
+/* Relax node positions of every system (domain fixed) until max |gradient| < gtol: the
+   reference's CartesianDOF with an optimiser (micmec/sampling/opt.py:147-443), here
+   Polak-Ribiere+ conjugate gradients with a secant line search. */
 mm_status mm_batch_relax(mm_batch* b, int max_iter, double gtol, void* stream);
 /*
  * Relax node positions and domain of every system together (the reference's
@@ -323,7 +331,8 @@ mm_status mm_batch_relax(mm_batch* b, int max_iter, double gtol, void* stream);
 mm_status mm_batch_relax_cell(mm_batch* b, int max_iter, double gtol, double stol, double press, int full,
                               void* stream);
 /* Choose the CTA size (128/256) and the CTA count (1, 2, 4 per SM or one per system; the default
-   after mm_batch_create is one per system) by timing probe_steps MD steps (state restored). */
+   after mm_batch_create is one per system) by timing probe_steps MD steps (state restored).
+   mm_batch_config reports the choice. No reference counterpart (launch configuration). */
 mm_status mm_batch_autotune(mm_batch* b, int probe_steps, double timestep, int thermo, double temp, double timecon,
                             int baro, double press, int chain, double* best_ms);
 mm_status mm_batch_config(mm_batch* b, int* cta_threads, int* nctas);
@@ -353,16 +362,18 @@ mm_status mm_set_params(mm_handle* h, const double* h0, const double* C, const d
 mm_status mm_adjoint(mm_handle* h, const double* pos, const double* lam, const double* dlattice, double* energy,
                      double* gpos, double* hvp, double* vtens, double* pgrad, void* stream);
 
-/* Last CUDA error string of the calling thread's last failing call. */
+/* Last CUDA error string of the calling thread's last failing call (the reference raises
+   Python exceptions instead; no counterpart). */
 const char* mm_last_error(void);
 
-/* Library version string. */
+/* Library version string (no reference counterpart). */
 const char* mm_version(void);
 
 /*
  * Self-test of the device-side FP64 <-> FP32 conversions the FP32 node update uses
  * (integer-pipe restatements of IEEE 754 round-to-nearest-even and exact widening):
  * dout[i] = (float)din[i], fout[i] = (double)fin[i] for i < n. All pointers device.
+ * No reference counterpart (test support).
  */
 mm_status mm_selftest_convert(const double* din, float* dout, const float* fin, double* fout, int n, void* stream);
 
@@ -371,6 +382,7 @@ mm_status mm_selftest_convert(const double* din, float* dout, const float* fin, 
  * R = exp(f S) of n row-major 3x3 matrices S (9 doubles each) by the one-thread form
  * (r_thread) and by the form with lane e of a warp forming entry e (r_warp); the two are
  * the same expressions in the same order and agree bit for bit. All pointers device.
+ * No reference counterpart (test support).
  */
 mm_status mm_selftest_sym_exp(const double* S, int n, double f, double* r_thread, double* r_warp, void* stream);
 
