@@ -1010,11 +1010,36 @@ template <typename T, int THERMO>
 __global__ void k_md_host_begin(Topo t, MDArgs p, double* pos, const double* __restrict__ vel,
                                 const double* __restrict__ gpos, const double* __restrict__ box,
                                 double* __restrict__ u, double* __restrict__ v, T* __restrict__ disp,
-                                const double* __restrict__ invm, const double* __restrict__ c2) {
+                                const double* __restrict__ invm, const double* __restrict__ c2,
+                                const float4* __restrict__ nodef) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= t.N) return;
   int la, lb, lc;
   lattice_of(t, n, la, lb, lc);
+  if constexpr (sizeof(T) == 4) {
+    // FP32 cells: the start half of k_md_nodes' update. The half step's velocity increment
+    // is formed in FP32 (v' = c1 v + q, q = (dt/2) a + amp z, a = -g / m; c1 = 1 and z = 0
+    // without a thermostat) and added to the FP64 state; the FP32 displacement is rounded on
+    // the integer pipe. FP64 work per component: the lattice site X, u = pos - X, v', u' and
+    // the output position X + u' (the FP64 pipe of this part bounds the kernel otherwise).
+    const float4 nf = nodef[n];  // mass, 1/mass, Langevin amplitude
+    float z[3] = {0.f, 0.f, 0.f};
+    if (THERMO == MM_THERMO_LANGEVIN) normal3(p.seed, (uint32_t)n, (uint32_t)p.step, 0u, z);
+    const double cv = (THERMO == MM_THERMO_LANGEVIN) ? p.c1 : 1.0;
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+      const double X = la * box[x] + lb * box[3 + x] + lc * box[6 + x];
+      const double uu = pos[3 * n + x] - X;
+      const float q = p.hf * (-d2f_rn(gpos[3 * n + x]) * nf.y) + nf.z * z[x];
+      const double vv = fma(cv, vel[3 * n + x], f2d(q));
+      const double un = fma(p.dt, vv, uu);
+      u[x * t.N + n] = un;
+      disp[x * t.N + n] = d2f_rn(un);
+      v[x * t.N + n] = vv;
+      pos[3 * n + x] = X + un;
+    }
+    return;
+  }
   double uu[3], vv[3], gg[3];
 #pragma unroll
   for (int x = 0; x < 3; ++x) {
@@ -1306,18 +1331,22 @@ void launch_md_host_begin(mm_handle* h, double dt, double c1, uint64_t seed, int
   a.noise_step0 = step;
   a.finish = 0;
   a.start = 1;
-  const int nb = node_blocks(h);
   const bool lang = thermo == MM_THERMO_LANGEVIN;
+  a.hf = (float)(0.5 * dt);
+  a.c1f = lang ? (float)c1 : 1.0f;
+  a.cv = lang ? c1 : 1.0;
+  const int nb = node_blocks(h);
+  const float4* nf = (const float4*)h->d_nodef;
   if (h->prec == MM_PREC_FP32) {
     if (lang)
-      k_md_host_begin<float, MM_THERMO_LANGEVIN><<<nb, kNodeThreads, 0, st>>>(t, a, pos, vel, gpos, h->d_box, h->d_u, h->d_v, (float*)h->d_disp, h->d_invm, h->d_c2);
+      k_md_host_begin<float, MM_THERMO_LANGEVIN><<<nb, kNodeThreads, 0, st>>>(t, a, pos, vel, gpos, h->d_box, h->d_u, h->d_v, (float*)h->d_disp, h->d_invm, h->d_c2, nf);
     else
-      k_md_host_begin<float, MM_THERMO_NONE><<<nb, kNodeThreads, 0, st>>>(t, a, pos, vel, gpos, h->d_box, h->d_u, h->d_v, (float*)h->d_disp, h->d_invm, h->d_c2);
+      k_md_host_begin<float, MM_THERMO_NONE><<<nb, kNodeThreads, 0, st>>>(t, a, pos, vel, gpos, h->d_box, h->d_u, h->d_v, (float*)h->d_disp, h->d_invm, h->d_c2, nf);
   } else {
     if (lang)
-      k_md_host_begin<double, MM_THERMO_LANGEVIN><<<nb, kNodeThreads, 0, st>>>(t, a, pos, vel, gpos, h->d_box, h->d_u, h->d_v, (double*)h->d_disp, h->d_invm, h->d_c2);
+      k_md_host_begin<double, MM_THERMO_LANGEVIN><<<nb, kNodeThreads, 0, st>>>(t, a, pos, vel, gpos, h->d_box, h->d_u, h->d_v, (double*)h->d_disp, h->d_invm, h->d_c2, nf);
     else
-      k_md_host_begin<double, MM_THERMO_NONE><<<nb, kNodeThreads, 0, st>>>(t, a, pos, vel, gpos, h->d_box, h->d_u, h->d_v, (double*)h->d_disp, h->d_invm, h->d_c2);
+      k_md_host_begin<double, MM_THERMO_NONE><<<nb, kNodeThreads, 0, st>>>(t, a, pos, vel, gpos, h->d_box, h->d_u, h->d_v, (double*)h->d_disp, h->d_invm, h->d_c2, nf);
   }
 }
 
